@@ -1,0 +1,296 @@
+"""cgmlst-hamming-gpu for GB300: Python bindings of libtch (ctypes).
+
+The library is the product; this module only binds its C ABI (include/tch.h)
+for Python callers, the tests and the benchmark.  It never computes a
+distance itself and has no CPU fallback: if ``lib/libtch.so`` is missing the
+import of any entry point raises.
+
+    import importlib
+    tch = importlib.import_module("cgmlst-hamming-gpu_gb300")
+    x, nd = tch.dense_ranks(calls)                  # u64 ids -> u16 ranks
+    enc = tch.encode_host(x, nd, tau=64)            # O, P bits + rare CSR
+    H = tch.run(enc, stripe=512)                    # tch_run: full u16 matrix
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libtch.so")
+CLI_PATH = os.path.join(HERE, "bin", "cgmlst-hamming-gpu")
+
+KERNELS = {"auto": 0, "popc": 1, "mma_b1": 2, "tc_f8": 3, "tc_i8": 4, "tc_f16": 5}
+
+# The reference host's analytic-model rates, measured on an L4 (main.rs:170-171).
+REF_GEMM_RATE = 5.9e14
+REF_RARE_RATE = 3.5e9
+
+CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_size_t,
+                      ctypes.POINTER(ctypes.c_uint16))
+
+
+class TchError(RuntimeError):
+    pass
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("L", ctypes.c_int), ("tau", ctypes.c_int), ("kernel", ctypes.c_int),
+                ("n_pad", ctypes.c_size_t), ("k_presence", ctypes.c_size_t), ("k_onehot", ctypes.c_size_t),
+                ("d_onehot", ctypes.c_size_t), ("n_rare", ctypes.c_size_t), ("rare_sorted", ctypes.c_int),
+                ("device_bytes", ctypes.c_size_t)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class HostEncoding(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("L", ctypes.c_int), ("tau", ctypes.c_int), ("D", ctypes.c_size_t),
+                ("n_pad", ctypes.c_size_t), ("K1", ctypes.c_size_t), ("K2", ctypes.c_size_t),
+                ("n_rare", ctypes.c_size_t), ("O", ctypes.POINTER(ctypes.c_uint8)),
+                ("P", ctypes.POINTER(ctypes.c_uint8)), ("start", ctypes.POINTER(ctypes.c_uint32)),
+                ("js", ctypes.POINTER(ctypes.c_uint32))]
+
+
+_lib = None
+
+
+def compile_native(verbose: bool = False):
+    """Compile libtch.so and the CLI in-tree (nvcc for sm_103a, g++)."""
+    from .build import build as _build
+
+    return _build(verbose)
+
+
+def lib():
+    """The loaded libtch.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise TchError(f"{LIB_PATH} is missing: build it first (build.py / __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        c_int, c_size, c_void, c_char_p, c_double = (ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p,
+                                                     ctypes.c_char_p, ctypes.c_double)
+        P = ctypes.POINTER
+        L.tch_device_count.argtypes, L.tch_device_count.restype = [], c_int
+        L.tch_free_vram.argtypes, L.tch_free_vram.restype = [c_int], c_size
+        L.tch_run.argtypes = [c_int, c_int, c_size, c_void, c_size, c_void, c_size, c_void, c_void, c_size, c_int,
+                              CB, c_void, P(c_double), P(c_int), c_char_p, c_int]
+        L.tch_run.restype = c_int
+        L.tch_version.argtypes, L.tch_version.restype = [], c_int
+        L.tch_kernel_name.argtypes, L.tch_kernel_name.restype = [c_int], c_char_p
+        L.tch_kernel_available.argtypes, L.tch_kernel_available.restype = [c_int], c_int
+        L.tch_set_kernel.argtypes, L.tch_set_kernel.restype = [c_int], c_int
+        L.tch_get_kernel.argtypes, L.tch_get_kernel.restype = [], c_int
+        L.tch_solver_from_bits.argtypes = [c_int, c_int, c_size, c_void, c_size, c_void, c_size, c_void, c_void,
+                                           c_size, c_int, P(c_void), c_char_p, c_int]
+        L.tch_solver_from_bits.restype = c_int
+        L.tch_solver_info.argtypes, L.tch_solver_info.restype = [c_void, P(Info)], c_int
+        L.tch_solver_stripe.argtypes = [c_void, c_int, c_int, c_void, c_size, c_void, c_char_p, c_int]
+        L.tch_solver_stripe.restype = c_int
+        L.tch_solver_check.argtypes, L.tch_solver_check.restype = [c_void, c_char_p, c_int], c_int
+        L.tch_solver_run.argtypes = [c_void, c_int, CB, c_void, P(c_double), c_char_p, c_int]
+        L.tch_solver_run.restype = c_int
+        L.tch_solver_destroy.argtypes, L.tch_solver_destroy.restype = [c_void], None
+        L.tch_dense_ranks.argtypes = [c_void, c_int, c_int, c_void, c_void, c_int, c_char_p, c_int]
+        L.tch_dense_ranks.restype = c_int
+        L.tch_choose_tau.argtypes = [c_void, c_void, c_int, c_int, c_int, c_size, c_double, c_double, c_int, P(c_int),
+                                     c_char_p, c_int]
+        L.tch_choose_tau.restype = c_int
+        L.tch_encode_host.argtypes = [c_void, c_void, c_int, c_int, c_int, c_int, P(HostEncoding), c_char_p, c_int]
+        L.tch_encode_host.restype = c_int
+        L.tch_host_encoding_free.argtypes, L.tch_host_encoding_free.restype = [P(HostEncoding)], None
+        _lib = L
+    return _lib
+
+
+def _errbuf():
+    return ctypes.create_string_buffer(1024)
+
+
+def _check(rc, err):
+    if rc:
+        raise TchError(err.value.decode(errors="replace"))
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else None
+
+
+def device_count() -> int:
+    return lib().tch_device_count()
+
+
+def free_vram(device: int = 0) -> int:
+    return lib().tch_free_vram(device)
+
+
+def kernel_id(kernel) -> int:
+    if isinstance(kernel, str):
+        return KERNELS[kernel]
+    return int(kernel)
+
+
+def kernel_name(k: int) -> str:
+    return lib().tch_kernel_name(k).decode()
+
+
+def kernel_available(kernel) -> bool:
+    return bool(lib().tch_kernel_available(kernel_id(kernel)))
+
+
+def set_kernel(kernel) -> None:
+    if lib().tch_set_kernel(kernel_id(kernel)):
+        raise TchError(f"kernel {kernel!r} not available")
+
+
+# ---------------------------------------------------------------------------------------
+# host encoder (main.rs:134-198, 366-444)
+# ---------------------------------------------------------------------------------------
+
+def dense_ranks(calls: np.ndarray, threads: int = 0):
+    calls = np.ascontiguousarray(calls, dtype=np.uint64)
+    n, L = calls.shape
+    x = np.zeros((n, L), dtype=np.uint16)
+    nd = np.zeros(L, dtype=np.uint32)
+    err = _errbuf()
+    _check(lib().tch_dense_ranks(_ptr(calls), n, L, _ptr(x), _ptr(nd), threads, err, len(err)), err)
+    return x, nd
+
+
+def choose_tau(x, nd, stripe=512, free_bytes=None, gemm_rate=REF_GEMM_RATE, rare_rate=REF_RARE_RATE,
+               verbose=False, device=0) -> int:
+    x = np.ascontiguousarray(x, dtype=np.uint16)
+    nd = np.ascontiguousarray(nd, dtype=np.uint32)
+    n, L = x.shape
+    if free_bytes is None:
+        free_bytes = free_vram(device)
+    tau = ctypes.c_int(0)
+    err = _errbuf()
+    _check(lib().tch_choose_tau(_ptr(x), _ptr(nd), n, L, stripe, free_bytes, gemm_rate, rare_rate, int(verbose),
+                                ctypes.byref(tau), err, len(err)), err)
+    return tau.value
+
+
+class Encoding:
+    """The reference's tch_run operands, copied out of the C encoder."""
+
+    def __init__(self, h: HostEncoding):
+        self.n, self.L, self.tau, self.D = h.n, h.L, h.tau, h.D
+        self.n_pad, self.K1, self.K2, self.n_rare = h.n_pad, h.K1, h.K2, h.n_rare
+        self.O = np.ctypeslib.as_array(h.O, shape=(max(h.n_pad * h.K1 // 8, 1),))[: h.n_pad * h.K1 // 8].copy()
+        self.P = np.ctypeslib.as_array(h.P, shape=(max(h.n_pad * h.K2 // 8, 1),))[: h.n_pad * h.K2 // 8].copy()
+        self.start = np.ctypeslib.as_array(h.start, shape=(h.n + 1,)).copy()
+        self.js = np.ctypeslib.as_array(h.js, shape=(max(h.n_rare, 1),))[: h.n_rare].copy()
+
+
+def encode_host(x, nd, tau: int, threads: int = 0) -> Encoding:
+    x = np.ascontiguousarray(x, dtype=np.uint16)
+    nd = np.ascontiguousarray(nd, dtype=np.uint32)
+    n, L = x.shape
+    h = HostEncoding()
+    err = _errbuf()
+    _check(lib().tch_encode_host(_ptr(x), _ptr(nd), n, L, tau, threads, ctypes.byref(h), err, len(err)), err)
+    try:
+        return Encoding(h)
+    finally:
+        lib().tch_host_encoding_free(ctypes.byref(h))
+
+
+# ---------------------------------------------------------------------------------------
+# the reference ABI: tch_run
+# ---------------------------------------------------------------------------------------
+
+class StripeSink:
+    """Collects tch_run's stripes into a full n x n u16 matrix (upper triangle
+    filled, the rest zero), the way the reference host's on_stripe callback
+    copies each row's columns r+1.. (main.rs:204-211)."""
+
+    def __init__(self, n: int, keep_raw: bool = False):
+        self.n = n
+        self.H = np.zeros((n, n), dtype=np.uint16)
+        self.calls = []
+        self.keep_raw = keep_raw
+        self.raw = []
+
+    def __call__(self, ctx, r0, rows, w, ptr):
+        s = np.ctypeslib.as_array(ptr, shape=(rows * w,)).reshape(rows, w)
+        self.calls.append((r0, rows, w))
+        for r in range(rows):
+            self.H[r0 + r, r0 + r + 1:] = s[r, r + 1:]
+        if self.keep_raw:
+            self.raw.append(s.copy())
+
+
+def run(enc: Encoding, stripe: int = 512, device: int = 0, sink: StripeSink | None = None):
+    """tch_run on an Encoding; returns (H upper-triangle matrix, gpu_secs, rare_on_gpu, sink)."""
+    sink = sink or StripeSink(enc.n)
+    cb = CB(sink)
+    secs = ctypes.c_double(0)
+    rare_gpu = ctypes.c_int(-1)
+    err = _errbuf()
+    rc = lib().tch_run(device, enc.n, enc.n_pad, _ptr(enc.O), enc.K1, _ptr(enc.P), enc.K2, _ptr(enc.start),
+                       _ptr(enc.js), enc.n_rare, stripe, cb, None, ctypes.byref(secs), ctypes.byref(rare_gpu), err,
+                       len(err))
+    _check(rc, err)
+    return sink.H, secs.value, rare_gpu.value, sink
+
+
+# ---------------------------------------------------------------------------------------
+# solver (device-resident operands)
+# ---------------------------------------------------------------------------------------
+
+class Solver:
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def from_encoding(cls, enc: Encoding, kernel="auto", device: int = 0):
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        _check(lib().tch_solver_from_bits(device, enc.n, enc.n_pad, _ptr(enc.O), enc.K1, _ptr(enc.P), enc.K2,
+                                          _ptr(enc.start), _ptr(enc.js), enc.n_rare, kernel_id(kernel),
+                                          ctypes.byref(h), err, len(err)), err)
+        return cls(h)
+
+    def info(self) -> dict:
+        i = Info()
+        lib().tch_solver_info(self._h, ctypes.byref(i))
+        return i.as_dict()
+
+    def stripe(self, r0: int, rows: int, d_out: int, ldo: int, stream: int = 0):
+        """One stripe into device memory at address d_out (row stride ldo u16)."""
+        err = _errbuf()
+        _check(lib().tch_solver_stripe(self._h, r0, rows, ctypes.c_void_p(d_out), ldo,
+                                       ctypes.c_void_p(stream) if stream else None, err, len(err)), err)
+
+    def check(self):
+        err = _errbuf()
+        _check(lib().tch_solver_check(self._h, err, len(err)), err)
+
+    def run(self, stripe: int = 512, sink: StripeSink | None = None):
+        sink = sink or StripeSink(self.info()["n"])
+        cb = CB(sink)
+        secs = ctypes.c_double(0)
+        err = _errbuf()
+        _check(lib().tch_solver_run(self._h, stripe, cb, None, ctypes.byref(secs), err, len(err)), err)
+        return sink.H, secs.value
+
+    def close(self):
+        if self._h:
+            lib().tch_solver_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,94 @@
+// Internal declarations shared by the translation units of libtch.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <algorithm>
+
+#include "tch.h"
+
+namespace tch {
+
+// Error-recording helpers: every public entry point returns 0 / non-zero and
+// writes a message into the caller's buffer.
+struct Err {
+    char* buf;
+    int len;
+    int set(const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+};
+
+#define TCH_CK(e, x)                                                                        \
+    do {                                                                                   \
+        cudaError_t ck_ = (x);                                                             \
+        if (ck_ != cudaSuccess) {                                                          \
+            (e).set("%s: %s (%s:%d)", #x, cudaGetErrorString(ck_), __FILE__, __LINE__);    \
+            goto fail;                                                                     \
+        }                                                                                  \
+    } while (0)
+
+inline size_t up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+
+// Bits reported through the device error word.
+enum DevErr : int {
+    DEVERR_RARE_PAIR = 1,  // a rare partner j outside (i, n)
+    DEVERR_OVERFLOW = 2,   // a distance outside [0, 65535]
+    DEVERR_TIMEOUT = 4,    // a bounded wait gave up
+};
+
+// Rare-pair CSR on the device.
+struct RareCSR {
+    const uint32_t* start = nullptr;  // n + 1
+    const uint32_t* js = nullptr;     // n_rare
+    size_t n_rare = 0;
+    bool sorted = false;              // every row ascending -> fused subtraction
+};
+
+// Bit-packed operands in the reference layout, u32 words, LSB first.
+struct BitOperands {
+    const uint32_t* P = nullptr;  // n_pad x wP words
+    const uint32_t* O = nullptr;  // n_pad x wO words
+    int wP = 0, wO = 0;
+};
+
+// Byte operands of the tensor-core kernels: one row = [presence | one-hot],
+// each part padded to a multiple of 128 bytes, row stride kb bytes.
+struct ByteOperands {
+    const uint8_t* X = nullptr;  // n_rows x kb bytes (element encoding per kernel)
+    size_t n_rows = 0;           // multiple of 256
+    int kb = 0;                  // bytes per row
+    int kp = 0;                  // presence bytes (prefix of the row)
+    int elem_shift = 0;          // log2(elements per byte) for the kernel's type (0 here)
+};
+
+struct StripeArgs {
+    int n = 0, r0 = 0, rows = 0;
+    uint16_t* out = nullptr;
+    size_t ldo = 0;
+    int* err = nullptr;
+};
+
+// ---- k_popc.cu --------------------------------------------------------------------
+cudaError_t launch_popc_stripe(const BitOperands& ops, const RareCSR& rare, const StripeArgs& a,
+                               cudaStream_t st);
+// Unsorted CSR: separate pass with 32-bit atomics on the u16 stripe.
+cudaError_t launch_rare_atomic(const RareCSR& rare, const StripeArgs& a, cudaStream_t st);
+// Sets *flag to 0 if every CSR row is ascending (and stays 1 otherwise).
+cudaError_t launch_rare_check_sorted(const RareCSR& rare, int n, int* d_unsorted, cudaStream_t st);
+
+// ---- k_expand.cu ------------------------------------------------------------------
+// Bit rows -> byte operand rows for the tensor-core kernels.
+//   one = encoding of +1, neg_onehot: encode the one-hot part as -1 (kernels
+//   without a negate bit subtract through the operand itself).
+cudaError_t launch_expand_bits(const BitOperands& bits, int n, size_t n_rows, uint8_t* X, int kb, int kp,
+                               int k_presence_bits, int k_onehot_bits, uint8_t one, uint8_t one_neg,
+                               cudaStream_t st);
+
+// ---- k_tc.cu ----------------------------------------------------------------------
+bool tc_kernel_compiled(int kernel);
+cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t* Xneg, const RareCSR& rare,
+                             const StripeArgs& a, int num_sms, cudaStream_t st);
+
+}  // namespace tch

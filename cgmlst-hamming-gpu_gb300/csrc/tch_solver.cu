@@ -1,0 +1,475 @@
+// libtch: the C ABI, the solver object and the double-buffered stripe pipeline.
+//
+// tch_run keeps the reference's contract (tensorcore/rs/cuda/tch.cu:68-170):
+// same arguments, same stripe order and callback timing, same error
+// convention, the same host fallback for rare pairs that do not fit in device
+// memory (tch.cu:105, 140-144).  Inside it, the work is organised GB300-first:
+//
+//   * operands are uploaded once and, for the tensor-core kernels, expanded
+//     from bits to bytes on the device (k_expand.cu);
+//   * each stripe is ONE fused kernel that writes u16 distances directly:
+//     P Pt - O Ot accumulates on the tensor pipe (or CUDA cores), the rare
+//     pairs are subtracted inside the tile, and the int32 matrix the
+//     reference materialises between its GEMMs, sub_rare and pack_u16 never
+//     exists (3 passes over an int32 stripe -> 0);
+//   * the u16 stripe is copied to pinned host memory on the stripe's own
+//     stream while the other stream computes the next stripe.
+
+#include <errno.h>
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "tch_internal.cuh"
+
+namespace tch {
+
+int Err::set(const char* fmt, ...) {
+    if (buf && len > 0) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, (size_t)len, fmt, ap);
+        va_end(ap);
+    }
+    return 1;
+}
+
+static int g_kernel = -1;  // process default, resolved lazily
+
+static const char* kKernelNames[TCH_KERNEL_COUNT] = {"auto", "popc", "mma_b1", "tc_f8", "tc_i8", "tc_f16"};
+
+static bool kernel_compiled(int k) {
+    switch (k) {
+        case TCH_KERNEL_POPC: return true;
+        case TCH_KERNEL_TC_F8:
+        case TCH_KERNEL_TC_I8:
+        case TCH_KERNEL_TC_F16: return tc_kernel_compiled(k);
+        default: return false;
+    }
+}
+
+static int default_kernel() {
+    if (g_kernel < 0) {
+        g_kernel = TCH_KERNEL_AUTO;
+        const char* env = getenv("TCH_KERNEL");
+        if (env)
+            for (int k = 0; k < TCH_KERNEL_COUNT; k++)
+                if (!strcmp(env, kKernelNames[k])) g_kernel = k;
+    }
+    return g_kernel;
+}
+
+// AUTO: the fastest kernel measured on GB300 that is compiled in and exact
+// for this problem (fp32 accumulation of 0/+-1 products is exact while every
+// partial sum stays below 2^24; a distance never exceeds the loci count, and
+// the presence part alone bounds every partial sum by L <= 65535).
+static int resolve_kernel(int k) {
+    if (k == TCH_KERNEL_AUTO) {
+        for (int cand : {TCH_KERNEL_TC_F8, TCH_KERNEL_TC_F16, TCH_KERNEL_TC_I8, TCH_KERNEL_POPC})
+            if (kernel_compiled(cand)) return cand;
+        return TCH_KERNEL_POPC;
+    }
+    return k;
+}
+
+static bool is_tc(int k) { return k == TCH_KERNEL_TC_F8 || k == TCH_KERNEL_TC_I8 || k == TCH_KERNEL_TC_F16; }
+
+}  // namespace tch
+
+using namespace tch;
+
+struct tch_solver {
+    int device = 0, n = 0, L = 0, tau = 0, kernel = TCH_KERNEL_POPC;
+    size_t n_pad = 0, K1 = 0, K2 = 0, D = 0;
+    uint32_t* dP = nullptr;  // bit operands (popc kernel)
+    uint32_t* dO = nullptr;
+    uint8_t* dX = nullptr;   // byte operands (tensor-core kernels)
+    uint8_t* dXneg = nullptr;
+    size_t x_rows = 0;
+    int kb = 0, kp = 0;
+    uint32_t* dStart = nullptr;
+    uint32_t* dJs = nullptr;
+    size_t n_rare = 0;
+    bool sorted = false;
+    bool rare_on_host = false;              // reference fallback (tch.cu:140-144)
+    const uint32_t* hStart = nullptr;       // borrowed for the host fallback
+    const uint32_t* hJs = nullptr;
+    int* dErr = nullptr;
+    int num_sms = 0;
+    size_t bytes = 0;
+};
+
+namespace tch {
+
+static cudaError_t dmalloc(tch_solver* s, void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e == cudaSuccess) s->bytes += bytes;
+    return e;
+}
+
+static void solver_free(tch_solver* s) {
+    if (!s) return;
+    int cur = -1;
+    cudaGetDevice(&cur);
+    cudaSetDevice(s->device);
+    cudaFree(s->dP);
+    cudaFree(s->dO);
+    cudaFree(s->dX);
+    cudaFree(s->dXneg);
+    cudaFree(s->dStart);
+    cudaFree(s->dJs);
+    cudaFree(s->dErr);
+    if (cur >= 0) cudaSetDevice(cur);
+    delete s;
+}
+
+// The element encodings of +1 and -1 for each tensor-core kernel's operand type.
+static void tc_encoding(int kernel, uint8_t* one, uint8_t* neg) {
+    switch (kernel) {
+        case TCH_KERNEL_TC_F8: *one = 0x38; *neg = 0xB8; break;  // e4m3 +1 / -1
+        case TCH_KERNEL_TC_I8: *one = 0x01; *neg = 0xFF; break;  // s8 +1 / -1
+        default: *one = 0x01; *neg = 0xFF; break;
+    }
+}
+
+// Operands on the device from the reference's bit layout (host buffers).
+static int solver_from_bits(int device, int n, size_t n_pad, const uint8_t* O, size_t K1, const uint8_t* P,
+                            size_t K2, const uint32_t* start, const uint32_t* js, size_t n_rare, int kernel,
+                            int stripe_for_fit, bool allow_host_rare, tch_solver** out, Err& e) {
+    tch_solver* s = nullptr;
+    int* dflag = nullptr;
+    int hflag = 0;
+    size_t freeb = 0, totb = 0;
+    bool rare_gpu = true;
+    *out = nullptr;
+    if (n < 0) return e.set("n must be >= 0 (got %d)", n);
+    if (n_pad < (size_t)n || (n_pad % 256) != 0) return e.set("n_pad must be a multiple of 256 and >= n");
+    if (K1 == 0 || K2 == 0 || (K1 % 1024) != 0 || (K2 % 1024) != 0)
+        return e.set("K1 and K2 must be positive multiples of 1024 (got %zu, %zu)", K1, K2);
+    if ((n > 0 && (!O || !P)) || (n_rare > 0 && (!start || !js))) return e.set("null input buffer");
+    if (n > 0 && start) {  // CSR bounds (host side; the device checks the partners)
+        for (int i = 0; i < n; i++)
+            if (start[i] > start[i + 1]) return e.set("rare CSR: start[%d] > start[%d]", i, i + 1);
+        if ((size_t)start[n] > n_rare) return e.set("rare CSR: start[n] = %u > n_rare = %zu", start[n], n_rare);
+    }
+    kernel = resolve_kernel(kernel);
+    if (!kernel_compiled(kernel)) return e.set("kernel %d (%s) is not available", kernel, tch_kernel_name(kernel));
+
+    s = new tch_solver();
+    s->device = device;
+    s->n = n;
+    s->n_pad = n_pad;
+    s->K1 = K1;
+    s->K2 = K2;
+    s->kernel = kernel;
+    s->n_rare = n_rare;
+    TCH_CK(e, cudaSetDevice(device));
+    TCH_CK(e, cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, device));
+    TCH_CK(e, dmalloc(s, (void**)&s->dErr, sizeof(int)));
+    TCH_CK(e, cudaMemset(s->dErr, 0, sizeof(int)));
+    TCH_CK(e, dmalloc(s, (void**)&s->dP, n_pad * K2 / 8));
+    TCH_CK(e, dmalloc(s, (void**)&s->dO, n_pad * K1 / 8));
+    if (n_pad) {
+        TCH_CK(e, cudaMemcpy(s->dP, P, n_pad * K2 / 8, cudaMemcpyHostToDevice));
+        TCH_CK(e, cudaMemcpy(s->dO, O, n_pad * K1 / 8, cudaMemcpyHostToDevice));
+    }
+    if (is_tc(kernel)) {
+        // [presence | one-hot] bytes per row; each part padded to 128 bytes
+        // (one 128-byte swizzle atom of K per pipeline stage)
+        BitOperands bits;
+        bits.P = s->dP;
+        bits.O = s->dO;
+        bits.wP = (int)(K2 / 32);
+        bits.wO = (int)(K1 / 32);
+        uint8_t one, neg;
+        tc_encoding(kernel, &one, &neg);
+        s->kp = (int)up(K2, 128);
+        s->kb = s->kp + (int)up(K1, 128);
+        s->x_rows = up((size_t)std::max(n, 1), 256);
+        TCH_CK(e, dmalloc(s, (void**)&s->dX, s->x_rows * (size_t)s->kb));
+        TCH_CK(e, launch_expand_bits(bits, n, s->x_rows, s->dX, s->kb, s->kp, (int)K2, (int)K1, one, one, 0));
+        if (kernel == TCH_KERNEL_TC_I8) {  // no negate bit for integer MMA: subtract through B
+            TCH_CK(e, dmalloc(s, (void**)&s->dXneg, s->x_rows * (size_t)s->kb));
+            TCH_CK(e, launch_expand_bits(bits, n, s->x_rows, s->dXneg, s->kb, s->kp, (int)K2, (int)K1, one, neg,
+                                         0));
+        }
+        TCH_CK(e, cudaDeviceSynchronize());
+        cudaFree(s->dP);
+        cudaFree(s->dO);
+        s->bytes -= n_pad * K2 / 8 + n_pad * K1 / 8;
+        s->dP = s->dO = nullptr;
+    }
+    // rare pairs: on the device when they fit (tch.cu:104-111), else on the host
+    TCH_CK(e, cudaMemGetInfo(&freeb, &totb));
+    {
+        const size_t need = (n_rare + (size_t)n + 1) * 4 + (size_t)stripe_for_fit * up((size_t)n, 8) * 2 * 2 +
+                            ((size_t)64 << 20);
+        rare_gpu = need < freeb;
+        const char* force = getenv("TCH_FORCE_HOST_RARE");  // test hook: behave as if they did not fit
+        if (force && force[0] == '1') rare_gpu = false;
+    }
+    if (!rare_gpu && !allow_host_rare)
+        { e.set("rare pairs (%zu) do not fit in device memory", n_rare); goto fail; }
+    if (rare_gpu) {
+        TCH_CK(e, dmalloc(s, (void**)&s->dStart, ((size_t)n + 1) * 4));
+        TCH_CK(e, dmalloc(s, (void**)&s->dJs, std::max<size_t>(n_rare, 1) * 4));
+        if (start) TCH_CK(e, cudaMemcpy(s->dStart, start, ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
+        else TCH_CK(e, cudaMemset(s->dStart, 0, ((size_t)n + 1) * 4));
+        if (n_rare) TCH_CK(e, cudaMemcpy(s->dJs, js, n_rare * 4, cudaMemcpyHostToDevice));
+        // ascending rows -> subtraction fused into the contraction's epilogue
+        TCH_CK(e, cudaMalloc(&dflag, sizeof(int)));
+        TCH_CK(e, cudaMemset(dflag, 0, sizeof(int)));
+        {
+            RareCSR rc;
+            rc.start = s->dStart;
+            rc.js = s->dJs;
+            rc.n_rare = n_rare;
+            TCH_CK(e, launch_rare_check_sorted(rc, n, dflag, 0));
+        }
+        TCH_CK(e, cudaMemcpy(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost));
+        cudaFree(dflag);
+        dflag = nullptr;
+        if (hflag & 2) { e.set("rare CSR: a partner j is not in (i, n)"); goto fail; }
+        s->sorted = (hflag & 1) == 0;
+    } else {
+        s->rare_on_host = true;
+        s->hStart = start;
+        s->hJs = js;
+        for (int i = 0; i < n; i++)
+            for (uint32_t p = start[i]; p < start[i + 1]; p++)
+                if (js[p] <= (uint32_t)i || js[p] >= (uint32_t)n) {
+                    e.set("rare CSR: a partner j is not in (i, n)");
+                    goto fail;
+                }
+    }
+    *out = s;
+    return 0;
+fail:
+    if (dflag) cudaFree(dflag);
+    solver_free(s);
+    return 1;
+}
+
+static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e) {
+    if (r0 < 0 || rows < 0 || r0 > s->n) return e.set("stripe out of range (r0=%d rows=%d n=%d)", r0, rows, s->n);
+    if (r0 + rows > s->n) rows = s->n - r0;
+    if (rows == 0) return 0;
+    if (ldo < (size_t)(s->n - r0)) return e.set("ldo %zu < stripe width %d", ldo, s->n - r0);
+    if (((uintptr_t)d_out & 15) != 0) return e.set("output pointer must be 16-byte aligned");
+    StripeArgs a;
+    a.n = s->n;
+    a.r0 = r0;
+    a.rows = rows;
+    a.out = d_out;
+    a.ldo = ldo;
+    a.err = s->dErr;
+    RareCSR rare;
+    if (!s->rare_on_host) {
+        rare.start = s->dStart;
+        rare.js = s->dJs;
+        rare.n_rare = s->n_rare;
+        rare.sorted = s->sorted;
+    }
+    cudaError_t ce;
+    if (s->kernel == TCH_KERNEL_POPC) {
+        BitOperands ops;
+        ops.P = s->dP;
+        ops.O = s->dO;
+        ops.wP = (int)(s->K2 / 32);
+        ops.wO = (int)(s->K1 / 32);
+        ce = launch_popc_stripe(ops, rare, a, st);
+    } else {
+        ByteOperands ops;
+        ops.X = s->dX;
+        ops.n_rows = s->x_rows;
+        ops.kb = s->kb;
+        ops.kp = s->kp;
+        ce = launch_tc_stripe(s->kernel, ops, s->dXneg, rare, a, s->num_sms, st);
+    }
+    if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
+    return 0;
+}
+
+static int solver_check(tch_solver* s, Err& e) {
+    int h = 0;
+    TCH_CK(e, cudaSetDevice(s->device));
+    TCH_CK(e, cudaDeviceSynchronize());
+    TCH_CK(e, cudaMemcpy(&h, s->dErr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+        cudaMemset(s->dErr, 0, sizeof(int));
+        return e.set("device reported error 0x%x (%s%s%s)", h, (h & DEVERR_RARE_PAIR) ? "invalid rare pair " : "",
+                     (h & DEVERR_OVERFLOW) ? "distance overflow " : "", (h & DEVERR_TIMEOUT) ? "wait timeout" : "");
+    }
+    return 0;
+fail:
+    return 1;
+}
+
+// Stripe pipeline through pinned host memory, two streams (tch.cu:113-149).
+static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_secs, Err& e) {
+    const int n = s->n;
+    const size_t ldo = up((size_t)std::max(n, 1), 8);
+    uint16_t* dU[2] = {nullptr, nullptr};
+    uint16_t* hU[2] = {nullptr, nullptr};
+    cudaStream_t st[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr}, t0 = nullptr, t1 = nullptr;
+    int rc = 1, prev = -1;
+    float ms = 0.f;
+    if (S <= 0) return e.set("stripe rows must be positive (got %d)", S);
+    if (!cb) return e.set("null callback");
+    S = std::min(S, std::max(n, 1));
+    TCH_CK(e, cudaSetDevice(s->device));
+    for (int b = 0; b < 2; b++) {
+        TCH_CK(e, cudaMalloc(&dU[b], (size_t)S * ldo * 2));
+        TCH_CK(e, cudaMallocHost(&hU[b], (size_t)S * ldo * 2));
+        TCH_CK(e, cudaStreamCreateWithFlags(&st[b], cudaStreamNonBlocking));
+        TCH_CK(e, cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming));
+    }
+    TCH_CK(e, cudaEventCreate(&t0));
+    TCH_CK(e, cudaEventCreate(&t1));
+    TCH_CK(e, cudaEventRecord(t0, st[0]));
+    TCH_CK(e, cudaStreamWaitEvent(st[1], t0, 0));
+    for (int r0 = 0;; r0 += S) {
+        if (r0 < n) {
+            const int rows = std::min(S, n - r0), b = (r0 / S) & 1;
+            const size_t w = (size_t)(n - r0);
+            if (solver_stripe(s, r0, rows, dU[b], ldo, st[b], e)) goto fail;
+            TCH_CK(e, cudaMemcpy2DAsync(hU[b], w * 2, dU[b], ldo * 2, w * 2, rows, cudaMemcpyDeviceToHost, st[b]));
+            TCH_CK(e, cudaEventRecord(done[b], st[b]));
+        }
+        if (prev >= 0) {  // consume the previous stripe while this one runs
+            const int rows = std::min(S, n - prev), b = (prev / S) & 1;
+            const size_t w = (size_t)(n - prev);
+            TCH_CK(e, cudaEventSynchronize(done[b]));
+            if (s->rare_on_host && s->hStart)
+                for (int r = 0; r < rows; r++) {
+                    const int i = prev + r;
+                    for (uint32_t p = s->hStart[i]; p < s->hStart[i + 1]; p++)
+                        hU[b][(size_t)r * w + (s->hJs[p] - prev)] -= 1;
+                }
+            cb(ctx, prev, rows, w, hU[b]);
+        }
+        if (r0 >= n) break;
+        prev = r0;
+    }
+    TCH_CK(e, cudaStreamWaitEvent(st[0], done[1], 0));
+    TCH_CK(e, cudaEventRecord(t1, st[0]));
+    TCH_CK(e, cudaEventSynchronize(t1));
+    TCH_CK(e, cudaEventElapsedTime(&ms, t0, t1));
+    if (gpu_secs) *gpu_secs = ms / 1e3;
+    if (solver_check(s, e)) goto fail;
+    rc = 0;
+fail:
+    for (int b = 0; b < 2; b++) {
+        if (st[b]) cudaStreamSynchronize(st[b]);
+        if (dU[b]) cudaFree(dU[b]);
+        if (hU[b]) cudaFreeHost(hU[b]);
+        if (st[b]) cudaStreamDestroy(st[b]);
+        if (done[b]) cudaEventDestroy(done[b]);
+    }
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+    return rc;
+}
+
+}  // namespace tch
+
+// ==================================================================================
+// exported C ABI
+// ==================================================================================
+
+extern "C" {
+
+int tch_device_count(void) {
+    int c = 0;
+    return cudaGetDeviceCount(&c) == cudaSuccess ? c : 0;
+}
+
+size_t tch_free_vram(int device) {
+    size_t f = 0, t = 0;
+    if (cudaSetDevice(device) != cudaSuccess || cudaMemGetInfo(&f, &t) != cudaSuccess) return 0;
+    return f;
+}
+
+int tch_run(int device, int n, size_t n_pad, const uint8_t* O, size_t K1, const uint8_t* P, size_t K2,
+            const uint32_t* start, const uint32_t* js, size_t n_rare, int S, tch_cb cb, void* ctx,
+            double* gpu_secs, int* rare_on_gpu, char* err, int errlen) {
+    Err e{err, errlen};
+    tch_solver* s = nullptr;
+    if (S <= 0) return e.set("stripe rows must be positive (got %d)", S);
+    if (solver_from_bits(device, n, n_pad, O, K1, P, K2, start, js, n_rare, default_kernel(), S, true, &s, e))
+        return 1;
+    if (rare_on_gpu) *rare_on_gpu = s->rare_on_host ? 0 : 1;
+    const int rc = solver_run(s, S, cb, ctx, gpu_secs, e);
+    solver_free(s);
+    return rc;
+}
+
+int tch_version(void) { return TCH_VERSION; }
+
+const char* tch_kernel_name(int kernel) {
+    return kernel >= 0 && kernel < TCH_KERNEL_COUNT ? kKernelNames[kernel] : "?";
+}
+
+int tch_kernel_available(int kernel) { return kernel == TCH_KERNEL_AUTO || kernel_compiled(kernel) ? 1 : 0; }
+
+int tch_set_kernel(int kernel) {
+    if (kernel < 0 || kernel >= TCH_KERNEL_COUNT || !tch_kernel_available(kernel)) return 1;
+    g_kernel = kernel;
+    return 0;
+}
+
+int tch_get_kernel(void) { return default_kernel(); }
+
+int tch_solver_from_bits(int device, int n, size_t n_pad, const uint8_t* O, size_t K1, const uint8_t* P,
+                         size_t K2, const uint32_t* start, const uint32_t* js, size_t n_rare, int kernel,
+                         tch_solver** out, char* err, int errlen) {
+    Err e{err, errlen};
+    if (!out) return e.set("null output handle");
+    return solver_from_bits(device, n, n_pad, O, K1, P, K2, start, js, n_rare, kernel, 0, false, out, e);
+}
+
+int tch_solver_info(const tch_solver* s, tch_info* info) {
+    if (!s || !info) return 1;
+    memset(info, 0, sizeof(*info));
+    info->n = s->n;
+    info->L = s->L;
+    info->tau = s->tau;
+    info->kernel = s->kernel;
+    info->n_pad = s->n_pad;
+    info->k_presence = s->K2;
+    info->k_onehot = s->K1;
+    info->d_onehot = s->D;
+    info->n_rare = s->n_rare;
+    info->rare_sorted = s->sorted ? 1 : 0;
+    info->device_bytes = s->bytes;
+    return 0;
+}
+
+int tch_solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, void* stream, char* err,
+                      int errlen) {
+    Err e{err, errlen};
+    if (!s) return e.set("null solver");
+    if (!d_out && rows > 0) return e.set("null output");
+    if (cudaSetDevice(s->device) != cudaSuccess) return e.set("cudaSetDevice(%d) failed", s->device);
+    return solver_stripe(s, r0, rows, d_out, ldo, (cudaStream_t)stream, e);
+}
+
+int tch_solver_check(tch_solver* s, char* err, int errlen) {
+    Err e{err, errlen};
+    if (!s) return e.set("null solver");
+    return solver_check(s, e);
+}
+
+int tch_solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_secs, char* err, int errlen) {
+    Err e{err, errlen};
+    if (!s) return e.set("null solver");
+    return solver_run(s, S, cb, ctx, gpu_secs, e);
+}
+
+void tch_solver_destroy(tch_solver* s) { solver_free(s); }
+
+}  // extern "C"

@@ -1,0 +1,187 @@
+/*
+ * libtch — exact cgMLST Hamming distance matrix on the NVIDIA GB300 (sm_103a).
+ *
+ *   H = P Pt - (O Ot + R)
+ *
+ *   P  n x L presence bits (allele called at a locus)
+ *   O  n x D one-hot bits of the frequent alleles (seen >= tau times)
+ *   R  equal pairs of the rare alleles, as CSR by row (partners j > i)
+ *
+ * H[i][j] is the number of loci where profiles i and j are both called and
+ * differ.  Every value is an exact integer (u16, at most L <= 65535).
+ *
+ * The first block is the reference project's C ABI, kept bit-compatible so
+ * that its Rust host (tensorcore/rs/src/main.rs:84-93) links against this
+ * library unchanged.  Everything after it is an extension with no counterpart
+ * in the reference.  No declaration uses CUDA or PyTorch types: device
+ * pointers and streams are passed as plain pointers.
+ *
+ * Return convention of every int function (reference tch.cu:52-53, 155-169):
+ * 0 on success; non-zero on failure, with a NUL-terminated message written to
+ * err[errlen] when err is not NULL.
+ */
+#ifndef TCH_H
+#define TCH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------------------------
+ * Reference ABI (tensorcore/rs/cuda/tch.cu:68-86)
+ * ------------------------------------------------------------------------- */
+
+/* Stripe callback (tch.cu:79).  Called once per stripe, in increasing r0
+ * order, on the thread that called tch_run, after the stripe's copy to host
+ * memory completed.  `stripe` is rows x w u16, row-major, w = n - r0; column c
+ * holds H[r0 + r][r0 + c].  Only c > r is meaningful (the callers read the
+ * strict upper triangle, main.rs:204-211).  The pointer is valid only during
+ * the call. */
+typedef void (*tch_cb)(void* ctx, int r0, int rows, size_t w, const uint16_t* stripe);
+
+/* Number of CUDA devices; 0 on error.  Replaces tch.cu:68-71. */
+int tch_device_count(void);
+
+/* Free device memory in bytes after making `device` current; 0 on error.
+ * Replaces tch.cu:73-77. */
+size_t tch_free_vram(int device);
+
+/* The whole distance matrix, upper triangle, in stripes of S rows.
+ * Replaces tch.cu:81-170 (declared on the Rust side at main.rs:88-92).
+ *
+ *   O      n_pad x K1 bits, row-major, bit k of a row at byte k>>3, bit k&7
+ *          (LSB first).  K1 a multiple of 1024, n_pad of 256, padding zero.
+ *   P      n_pad x K2 bits, same layout.
+ *   start  n+1 offsets into js; js[start[i] .. start[i+1]) are the partners
+ *          j > i of row i (any order, repeats allowed: one entry per locus
+ *          where i and j share a rare allele).  n_rare = start[n].
+ *   S      rows per stripe (a multiple of 8 in the reference's host).
+ *   gpu_secs     (may be NULL) device time of the whole pipeline.
+ *   rare_on_gpu  1 if the rare pairs were applied on the GPU, 0 if on the
+ *                host because they did not fit in device memory (tch.cu:105).
+ */
+int tch_run(int device, int n, size_t n_pad, const uint8_t* O, size_t K1, const uint8_t* P, size_t K2,
+            const uint32_t* start, const uint32_t* js, size_t n_rare, int S, tch_cb cb, void* ctx,
+            double* gpu_secs, int* rare_on_gpu, char* err, int errlen);
+
+/* ----------------------------------------------------------------------------
+ * Extensions (no counterpart in the reference)
+ * ------------------------------------------------------------------------- */
+
+#define TCH_VERSION 1
+
+/* Contraction kernels.  AUTO picks the fastest one measured on GB300 that is
+ * exact for the problem's size. */
+enum tch_kernel {
+    TCH_KERNEL_AUTO = 0,
+    TCH_KERNEL_POPC = 1, /* CUDA cores: LOP3 AND + popcount on the bit-packed rows */
+    TCH_KERNEL_MMA_B1 = 2, /* legacy warp MMA: mma.sync m16n8k256 b1 AND+popc   */
+    TCH_KERNEL_TC_F8 = 3, /* tcgen05.mma kind::f8f6f4, e4m3 0/+-1, TMEM fp32     */
+    TCH_KERNEL_TC_I8 = 4, /* tcgen05.mma kind::i8, s8 0/+-1, TMEM s32           */
+    TCH_KERNEL_TC_F16 = 5, /* tcgen05.mma kind::f16, bf16 0/+-1, TMEM fp32       */
+    TCH_KERNEL_COUNT = 6
+};
+
+int tch_version(void);
+/* Name of a kernel id ("popc", "tc_f8", ...), or "?" */
+const char* tch_kernel_name(int kernel);
+/* 1 if `kernel` was compiled into this library. */
+int tch_kernel_available(int kernel);
+/* Process-wide default kernel used by tch_run (TCH_KERNEL_AUTO initially;
+ * the TCH_KERNEL environment variable, a kernel name, overrides it at load). */
+int tch_set_kernel(int kernel);
+int tch_get_kernel(void);
+
+/* Sizes and choices of a solver, filled by tch_solver_info. */
+typedef struct tch_info {
+    int n;             /* profiles */
+    int L;             /* loci (0 when built from bit-packed operands) */
+    int tau;           /* frequency threshold (0 when unknown) */
+    int kernel;        /* enum tch_kernel actually used */
+    size_t n_pad;      /* padded row count of the device operands */
+    size_t k_presence; /* presence columns on the device (padded) */
+    size_t k_onehot;   /* one-hot columns on the device (padded) */
+    size_t d_onehot;   /* frequent one-hot columns before padding (0 if unknown) */
+    size_t n_rare;     /* rare equal pairs */
+    int rare_sorted;   /* 1 if every row's partner list is ascending */
+    size_t device_bytes; /* device memory held by the solver */
+} tch_info;
+
+/* A solver holds one profile set on one device: the operands of the two
+ * contractions and the rare-pair CSR, resident in device memory. */
+typedef struct tch_solver tch_solver;
+
+/* Build a solver from the reference's bit-packed host buffers (same meaning
+ * as tch_run's arguments).  `kernel` = enum tch_kernel. */
+int tch_solver_from_bits(int device, int n, size_t n_pad, const uint8_t* O, size_t K1, const uint8_t* P,
+                         size_t K2, const uint32_t* start, const uint32_t* js, size_t n_rare, int kernel,
+                         tch_solver** out, char* err, int errlen);
+
+/* Fill *info. */
+int tch_solver_info(const tch_solver* s, tch_info* info);
+
+/* One stripe into caller-owned DEVICE memory, asynchronously on `stream`
+ * (a cudaStream_t, NULL = the legacy default stream):
+ *   d_out[(i - r0) * ldo + (j - r0)] = H[i][j]   for r0 <= i < r0 + rows,
+ *                                                  max(i, r0) <= j < n
+ * Cells with j <= i are unspecified.  ldo >= n - r0.  Errors detected on the
+ * device (an invalid rare pair) are reported by the next tch_solver_check. */
+int tch_solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, void* stream, char* err,
+                      int errlen);
+
+/* Synchronise the device and report any error recorded by earlier stripes. */
+int tch_solver_check(tch_solver* s, char* err, int errlen);
+
+/* The whole upper triangle through host memory, with tch_run's stripe and
+ * callback contract (double-buffered: stripe s+1 is computed while the
+ * callback consumes stripe s). */
+int tch_solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_secs, char* err, int errlen);
+
+void tch_solver_destroy(tch_solver* s);
+
+/* ----------------------------------------------------------------------------
+ * Host encoder (restates the reference host, main.rs:134-198 and 366-444).
+ * Multi-threaded C++; `threads` <= 0 uses every hardware thread.
+ * ------------------------------------------------------------------------- */
+
+/* Dense per-locus ranks (main.rs:134-165): for each locus, the sorted unique
+ * non-zero ids get ranks 1..k (0 stays missing).  calls and x are n x L
+ * row-major; n_distinct[L] receives k per locus.  Fails when a locus has
+ * more than 65535 distinct ids. */
+int tch_dense_ranks(const uint64_t* calls, int n, int L, uint16_t* x, uint32_t* n_distinct, int threads,
+                    char* err, int errlen);
+
+/* Analytic tau (main.rs:167-198): tau in {2, 4, ..., 4096} minimising
+ * n^2/2 * K1 / gemm_rate + R / rare_rate such that the one-hot bits, the
+ * rare CSR and the stripe buffers fit in free_bytes and R < 4e9.  With
+ * gemm_rate = 5.9e14 and rare_rate = 3.5e9 this is the reference's choice.
+ * verbose != 0 prints the reference's per-tau table on stderr. */
+int tch_choose_tau(const uint16_t* x, const uint32_t* n_distinct, int n, int L, int stripe, size_t free_bytes,
+                   double gemm_rate, double rare_rate, int verbose, int* tau, char* err, int errlen);
+
+/* The reference's operands for a given tau (main.rs:366-444): O, P bit-packed
+ * in tch_run's layout, and the rare-pair CSR with each row's partners in
+ * ascending order (the reference's order is unspecified). */
+typedef struct tch_host_encoding {
+    int n, L, tau;
+    size_t D;     /* frequent one-hot columns */
+    size_t n_pad, K1, K2;
+    size_t n_rare;
+    uint8_t* O;   /* n_pad * K1 / 8 bytes */
+    uint8_t* P;   /* n_pad * K2 / 8 bytes */
+    uint32_t* start; /* n + 1 */
+    uint32_t* js;    /* n_rare */
+} tch_host_encoding;
+
+int tch_encode_host(const uint16_t* x, const uint32_t* n_distinct, int n, int L, int tau, int threads,
+                    tch_host_encoding* out, char* err, int errlen);
+void tch_host_encoding_free(tch_host_encoding* e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TCH_H */
