@@ -1,12 +1,511 @@
-// Tensor-core contraction (tcgen05) — not compiled in yet.
+// Tensor-core contraction for sm_103a: tcgen05.mma with TMEM accumulators,
+// operands staged by TMA, one fused epilogue writing u16 distances.
+//
+// Operands: X is n_rows x kb bytes, row = [presence part (kp bytes) |
+// one-hot part (kb - kp bytes)], one byte per element, 0 or +1 in e4m3
+// (0x38).  One output tile (128 rows i x 256 columns j) is
+//
+//   D = X_i[:, :kp] X_j[:, :kp]^T  -  X_i[:, kp:] X_j[:, kp:]^T  =  P Pt - O Ot
+//
+// with the minus taken by the instruction descriptor's negate-B bit on the
+// one-hot stages.  Every partial sum is an integer with |value| <= number of
+// loci < 2^24, so fp32 accumulation is exact; the epilogue re-checks the
+// integrality of every value anyway and reports a device error if it ever
+// fails.  This replaces the reference's two CUTLASS b1 GEMMs
+// (tensorcore/rs/cuda/tch.cu:22-32, 128-129): on GB300 the b1 and s8 warp
+// MMAs issue at ~150 TOPS, and tcgen05 kind::i8 does not exist on sm_103a.
+//
+// CTA = 6 warps, persistent over the stripe's tiles (upper triangle only):
+//   warp 0   TMA producer     4-stage ring of (A 128x128 B, B 256x128 B) tiles
+//   warp 1   MMA issuer       4 x tcgen05.mma (K = 32 bytes) per stage into one
+//                             of two 256-column TMEM accumulators
+//   warps 2-5 epilogue        tcgen05.ld 32 columns at a time -> int -> u16
+//                             in shared memory -> rare pairs of the row
+//                             subtracted (ascending CSR walk) -> coalesced
+//                             stores of the valid cells
+// Tiles are visited in groups of 8 row blocks (column-major inside a group) so
+// that concurrently running CTAs share A and B tiles in L2.
+//
+// Every mbarrier wait is bounded (about 2 s of %globaltimer); on a timeout the
+// CTA records DEVERR_TIMEOUT, stops issuing work, drains what it issued,
+// frees its TMEM and returns.
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "tch_internal.cuh"
 
 namespace tch {
+namespace {
 
-bool tc_kernel_compiled(int) { return false; }
+constexpr int BM = 128;            // tile rows (TMEM lanes)
+constexpr int BN = 256;            // tile columns (MMA N)
+constexpr int BK = 128;            // bytes of K per stage = one 128-byte swizzle row
+constexpr int STAGES = 4;
+constexpr int A_BYTES = BM * BK;   // 16 KB
+constexpr int B_BYTES = BN * BK;   // 32 KB
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int EPI_WARPS = 4;
+constexpr int THREADS = 64 + 32 * EPI_WARPS;
+constexpr int EPI_PITCH = 34;      // u16 per staged row: 32 + 2 keeps row writes conflict-free
+constexpr int EPI_BYTES = EPI_WARPS * 32 * EPI_PITCH * 2;
+constexpr int TMEM_COLS = 2 * BN;  // two accumulators
+constexpr int GROUP_M = 8;         // row blocks per raster group
+constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + EPI_BYTES + 256;
+constexpr unsigned long long WAIT_NS = 2000000000ull;  // bounded waits: 2 s
 
-cudaError_t launch_tc_stripe(int, const ByteOperands&, const uint8_t*, const RareCSR&, const StripeArgs&, int,
-                             cudaStream_t) {
+enum Kind { KIND_F8 = 0, KIND_I8 = 1 };
+
+// ---------------------------------------------------------------- PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase with `parity` to complete.  Returns false on a
+// timeout or when another role already aborted the CTA.
+__device__ __noinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag, int* err) {
+    if (mbar_test(b, parity)) return true;
+    const unsigned long long t0 = gtimer();
+    for (uint32_t it = 1;; it++) {
+        if (mbar_test(b, parity)) return true;
+        if ((it & 255) == 0) {
+            if (*abort_flag) return false;
+            if (gtimer() - t0 > WAIT_NS) {
+                *abort_flag = 1;
+                atomicOr(err, DEVERR_TIMEOUT);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(const CUtensorMap* map, uint64_t* bar, void* dst, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+template <int KIND>
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    static_assert(KIND == KIND_F8, "only kind::f8f6f4 is built for sm_103a");
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, rows of 128 B,
+// 8-row swizzle atoms 1024 B apart (SBO); LBO unused for this layout.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;             // LBO (ignored for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;   // SBO
+    d |= (uint64_t)1 << 46;             // descriptor version for tcgen05
+    d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor: D format, A/B formats, negate B, K-major A and B, N, M.
+__host__ __device__ constexpr uint32_t make_idesc(uint32_t dfmt, uint32_t abfmt, uint32_t negb) {
+    return (dfmt << 4) | (abfmt << 7) | (abfmt << 10) | (negb << 14) | ((uint32_t)(BN >> 3) << 17) |
+           ((uint32_t)(BM >> 4) << 24);
+}
+
+// ---------------------------------------------------------------- tile order
+struct TileSpace {
+    int nbi, nbj;  // row blocks of the stripe, column blocks of [r0, n)
+};
+
+// Tiles of row block bi: columns bj >= bi / 2 (128-row blocks against 256-wide
+// column blocks that both start at r0; earlier columns lie below the diagonal).
+__device__ __forceinline__ int cols_in_row(const TileSpace& ts, int bi) {
+    const int c = ts.nbj - bi / 2;
+    return c > 0 ? c : 0;
+}
+
+// t -> (bi, bj): groups of GROUP_M row blocks, column-major inside a group.
+__device__ bool tile_coords(const TileSpace& ts, int t, int* bi_out, int* bj_out) {
+    for (int g0 = 0; g0 < ts.nbi; g0 += GROUP_M) {
+        const int g1 = min(ts.nbi, g0 + GROUP_M);
+        int cnt = 0;
+        for (int bi = g0; bi < g1; bi++) cnt += cols_in_row(ts, bi);
+        if (t >= cnt) {
+            t -= cnt;
+            continue;
+        }
+        for (int bj = g0 / 2; bj < ts.nbj; bj++) {
+            // rows of the group present in column bj: bi <= 2 bj + 1
+            const int last = min(g1 - 1, 2 * bj + 1);
+            const int rows = last - g0 + 1;
+            if (rows <= 0) continue;
+            if (t < rows) {
+                *bi_out = g0 + t;
+                *bj_out = bj;
+                return true;
+            }
+            t -= rows;
+        }
+        return false;
+    }
+    return false;
+}
+
+struct TcParams {
+    int n, r0, rows;
+    int kblocks, kblocks_p;  // K stages in total and in the presence part
+    TileSpace ts;
+    int num_tiles;
+    const uint32_t* start;
+    const uint32_t* js;
+    int fuse_rare;
+    uint16_t* out;
+    size_t ldo;
+    int* err;
+};
+
+__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__ js, uint32_t lo, uint32_t hi,
+                                                    uint32_t key) {
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (__ldg(js + mid) < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(THREADS, 1)
+tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                 const TcParams p) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    // 1024-byte alignment of the swizzled stage buffers
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* stage_a = smem;
+    uint8_t* stage_b = smem + STAGES * A_BYTES;
+    uint16_t* epi = (uint16_t*)(smem + STAGES * STAGE_BYTES);
+    uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES + EPI_BYTES);
+    uint64_t* full = bars;                  // STAGES
+    uint64_t* empty = bars + STAGES;        // STAGES
+    uint64_t* tfull = bars + 2 * STAGES;    // 2
+    uint64_t* tempty = bars + 2 * STAGES + 2;  // 2
+    uint64_t* drain = bars + 2 * STAGES + 4;   // 1
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 5);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < 2; a++) {
+            mbar_init(&tfull[a], 1);
+            mbar_init(&tempty[a], EPI_WARPS);
+        }
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_a) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_b) : "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0) {
+        // ------------------------------------------------------------ producer
+        if (lane == 0) {
+            int s = 0;
+            uint32_t ph = 0;
+            bool ok = true;
+            int issued[STAGES];
+            uint32_t issued_ph[STAGES];
+            for (int q = 0; q < STAGES; q++) issued[q] = 0, issued_ph[q] = 0;
+            for (int t = blockIdx.x; ok && t < p.num_tiles; t += gridDim.x) {
+                int bi, bj;
+                if (!tile_coords(p.ts, t, &bi, &bj)) break;
+                const int y_a = p.r0 + bi * BM, y_b = p.r0 + bj * BN;
+                for (int kb = 0; kb < p.kblocks; kb++) {
+                    if (!mbar_wait(&empty[s], ph ^ 1, abort_flag, p.err)) { ok = false; break; }
+                    mbar_expect_tx(&full[s], STAGE_BYTES);
+                    tma_load_2d(&map_a, &full[s], stage_a + s * A_BYTES, kb * BK, y_a);
+                    tma_load_2d(&map_b, &full[s], stage_b + s * B_BYTES, kb * BK, y_b);
+                    issued[s] = 1;
+                    issued_ph[s] = ph;
+                    if (++s == STAGES) s = 0, ph ^= 1;
+                }
+            }
+            if (ok) {
+                // tail: every stage released by the MMA warp (all commits arrived)
+                for (int q = 0; q < STAGES; q++) {
+                    if (!mbar_wait(&empty[s], ph ^ 1, abort_flag, p.err)) break;
+                    if (++s == STAGES) s = 0, ph ^= 1;
+                }
+            } else {
+                // abort: let the loads already issued land before the CTA exits
+                for (int q = 0; q < STAGES; q++)
+                    if (issued[q]) {
+                        const unsigned long long t0 = gtimer();
+                        while (!mbar_test(&full[q], issued_ph[q]) && gtimer() - t0 < WAIT_NS) {}
+                    }
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ------------------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            const uint32_t id_pos = KIND == KIND_F8 ? make_idesc(1, 0, 0) : make_idesc(2, 1, 0);
+            const uint32_t id_neg = KIND == KIND_F8 ? make_idesc(1, 0, 1) : make_idesc(2, 1, 0);
+            int s = 0, acc = 0;
+            uint32_t ph = 0, aph = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < p.num_tiles; t += gridDim.x) {
+                if (!mbar_wait(&tempty[acc], aph ^ 1, abort_flag, p.err)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t d_tmem = tmem_base + (uint32_t)(acc * BN);
+                for (int kb = 0; kb < p.kblocks; kb++) {
+                    if (!mbar_wait(&full[s], ph, abort_flag, p.err)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(stage_a + s * A_BYTES), b0 = smem_u32(stage_b + s * B_BYTES);
+                    const uint32_t idesc = kb < p.kblocks_p ? id_pos : id_neg;
+#pragma unroll
+                    for (int k = 0; k < BK / 32; k++)
+                        tc_mma<KIND>(d_tmem, sw128_desc(a0 + 32 * k), sw128_desc(b0 + 32 * k), idesc,
+                                     (kb | k) ? 1u : 0u);
+                    tc_commit(&empty[s]);  // stage free once these MMAs have read it
+                    if (++s == STAGES) s = 0, ph ^= 1;
+                }
+                if (!ok) break;
+                tc_commit(&tfull[acc]);  // accumulator ready for the epilogue
+                if (++acc == 2) acc = 0, aph ^= 1;
+            }
+            // every MMA issued by this thread has completed before TMEM is freed
+            tc_commit(drain);
+            const unsigned long long t0 = gtimer();
+            while (!mbar_test(drain, 0) && gtimer() - t0 < WAIT_NS) {}
+        }
+        __syncwarp();
+    } else {
+        // ------------------------------------------------------------ epilogue
+        const int q = warp & 3;  // TMEM lanes [32 q, 32 q + 32) belong to this warp
+        uint16_t* stg = epi + (warp - 2) * 32 * EPI_PITCH;
+        const int iend = p.r0 + p.rows;
+        int acc = 0;
+        uint32_t aph = 0;
+        int bad = 0;
+        for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x) {
+            int bi, bj;
+            if (!tile_coords(p.ts, t, &bi, &bj)) break;
+            const int i0 = p.r0 + bi * BM, j0 = p.r0 + bj * BN;
+            const int my_i = i0 + q * 32 + lane;
+            // this row's rare partners inside the tile: an ascending run of js
+            uint32_t rp = 0, rhi = 0;
+            if (p.fuse_rare && my_i < iend) {
+                rhi = __ldg(p.start + my_i + 1);
+                rp = lower_bound_u32(p.js, __ldg(p.start + my_i), rhi, (uint32_t)j0);
+            }
+            if (!mbar_wait(&tfull[acc], aph, abort_flag, p.err)) break;
+            tc_fence_after();
+            const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
+#pragma unroll 1
+            for (int c = 0; c < BN / 32; c++) {
+                uint32_t v[32];
+                tmem_ld32(tbase + (uint32_t)(c * 32), v);
+                tmem_wait_ld();
+                if (c == BN / 32 - 1) {  // accumulator fully read: hand it back to the MMA warp
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&tempty[acc]);
+                }
+                // own row -> staging buffer (u16)
+                uint32_t* row32 = reinterpret_cast<uint32_t*>(stg + lane * EPI_PITCH);
+#pragma unroll
+                for (int w = 0; w < 16; w++) {
+                    int x0, x1;
+                    if (KIND == KIND_F8) {
+                        const float f0 = __uint_as_float(v[2 * w]), f1 = __uint_as_float(v[2 * w + 1]);
+                        x0 = __float2int_rn(f0);
+                        x1 = __float2int_rn(f1);
+                        bad |= (__int2float_rn(x0) != f0) | (__int2float_rn(x1) != f1);
+                    } else {
+                        x0 = (int)v[2 * w];
+                        x1 = (int)v[2 * w + 1];
+                    }
+                    row32[w] = (uint32_t)(x0 & 0xFFFF) | ((uint32_t)(x1 & 0xFFFF) << 16);
+                }
+                // rare pairs of this row in columns [cb, cb + 32)
+                const uint32_t cb = (uint32_t)(j0 + c * 32);
+                while (rp < rhi) {
+                    const uint32_t j = __ldg(p.js + rp);
+                    if (j >= cb + 32) break;
+                    stg[lane * EPI_PITCH + (int)(j - cb)] -= 1;
+                    rp++;
+                }
+                __syncwarp();
+                // coalesced store: 16 lanes x 4 bytes per row, 2 rows per step
+#pragma unroll 4
+                for (int st = 0; st < 16; st++) {
+                    const int rr = st * 2 + lane / 16, w = lane % 16;
+                    const int i = i0 + q * 32 + rr;
+                    const int j = (int)cb + 2 * w;
+                    if (i < iend && j < p.n) {
+                        const uint32_t val = reinterpret_cast<const uint32_t*>(stg + rr * EPI_PITCH)[w];
+                        uint16_t* dst = p.out + (size_t)(i - p.r0) * p.ldo + (size_t)(j - p.r0);
+                        if (j + 1 < p.n) *reinterpret_cast<uint32_t*>(dst) = val;
+                        else *dst = (uint16_t)(val & 0xFFFF);
+                    }
+                }
+                __syncwarp();
+            }
+            if (++acc == 2) acc = 0, aph ^= 1;
+        }
+        if (bad) atomicOr(p.err, DEVERR_OVERFLOW);
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
+                     : "memory");
+    }
+}
+
+// ---------------------------------------------------------------- host side
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+bool make_map(CUtensorMap* m, const uint8_t* X, size_t rows, int kb, int box_rows) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)kb, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)kb};
+    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)X, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int KIND>
+cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCSR& rare, const StripeArgs& a,
+                        int num_sms, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(tc_stripe_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    if ((ops.kb % BK) || (ops.kp % BK) || ops.kb <= 0) return cudaErrorInvalidValue;
+    if ((a.ldo & 1) || ((uintptr_t)a.out & 3)) return cudaErrorInvalidValue;
+    CUtensorMap ma, mb;
+    if (!make_map(&ma, ops.X, ops.n_rows, ops.kb, BM) || !make_map(&mb, xb, ops.n_rows, ops.kb, BN))
+        return cudaErrorInvalidValue;
+    TcParams p;
+    p.n = a.n;
+    p.r0 = a.r0;
+    p.rows = a.rows;
+    p.kblocks = ops.kb / BK;
+    p.kblocks_p = ops.kp / BK;
+    p.ts.nbi = (a.rows + BM - 1) / BM;
+    p.ts.nbj = (a.n - a.r0 + BN - 1) / BN;
+    long long tiles = 0;
+    for (int bi = 0; bi < p.ts.nbi; bi++) tiles += std::max(0, p.ts.nbj - bi / 2);
+    p.num_tiles = (int)tiles;
+    p.start = rare.start;
+    p.js = rare.js;
+    p.fuse_rare = (rare.n_rare > 0 && rare.sorted) ? 1 : 0;
+    p.out = a.out;
+    p.ldo = a.ldo;
+    p.err = a.err;
+    if (p.num_tiles == 0) return cudaSuccess;
+    const int grid = std::min(p.num_tiles, std::max(num_sms, 1));
+    tc_stripe_kernel<KIND><<<grid, THREADS, SMEM_BYTES, st>>>(ma, mb, p);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (rare.n_rare > 0 && !rare.sorted) return launch_rare_atomic(rare, a, st);
+    return cudaSuccess;
+}
+
+}  // namespace
+
+// kind::i8 does not exist on sm_103a (ptxas: "Feature '.kind::i8' not
+// supported on .target 'sm_103a'"), so TCH_KERNEL_TC_I8 is never compiled in.
+bool tc_kernel_compiled(int kernel) { return kernel == TCH_KERNEL_TC_F8; }
+
+cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t* Xneg, const RareCSR& rare,
+                             const StripeArgs& a, int num_sms, cudaStream_t st) {
+    (void)Xneg;
+    if (a.rows <= 0 || a.r0 >= a.n) return cudaSuccess;
+    if (kernel == TCH_KERNEL_TC_F8) return launch_kind<KIND_F8>(ops, ops.X, rare, a, num_sms, st);
     return cudaErrorNotSupported;
 }
 

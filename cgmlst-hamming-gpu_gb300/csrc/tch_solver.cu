@@ -259,6 +259,7 @@ static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_
     if (rows == 0) return 0;
     if (ldo < (size_t)(s->n - r0)) return e.set("ldo %zu < stripe width %d", ldo, s->n - r0);
     if (((uintptr_t)d_out & 15) != 0) return e.set("output pointer must be 16-byte aligned");
+    if (is_tc(s->kernel) && (ldo & 1)) return e.set("ldo must be even for the tensor-core kernels");
     StripeArgs a;
     a.n = s->n;
     a.r0 = r0;
