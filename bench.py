@@ -1,0 +1,358 @@
+#!/usr/bin/env python3
+"""Benchmark: exact cgMLST Hamming distances, pairs/s on one GB300.
+
+Workload: the long-tail outbreak shape, 63 005 profiles x 1 142 loci
+(synthetic, seeded: per-locus Zipf(1.2) alleles with lognormal distinct counts,
+median 60, tail to ~2 500; 1-5% missing per locus; 5% hashed 64-bit ids).  One
+step = the whole upper triangle of the u16 distance matrix,
+n (n - 1) / 2 = 1 984 783 510 exact pairs.
+
+    value  device-resident: operands and rare-pair CSR already in HBM, the
+           step is the tensor-core stripe kernel over all tiles of the upper
+           triangle (u16 output in HBM).  Inputs (X ~3 GB) exceed L2.
+    e2e    the reference-facing C ABI, tch_run, with host buffers: H2D of the
+           bit-packed operands and CSR, device expansion, stripes, D2H of every
+           stripe into pinned memory and the stripe callback, per step.
+    roofline   tensor-pipe bound: algorithmic MACs (unpadded K = L + D per
+           pair, 2 ops per MAC) per launch / CUDA-event duration of the
+           launch, against the measured fp8 tcgen05 peak of this GPU.
+    cpu_baseline   the brute-force count of the reference's exactness check
+           (the C restatement in oracle/), all host threads, bounded sample.
+
+--impl reference runs that CPU brute force alone (the reference's CPU path
+for the matrix) and prints its line.  Under torchrun each rank computes a
+balanced share of the rows (equal pair counts, no collective on the data
+path); value = all pairs / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "cgmlst-hamming-gpu_gb300"
+
+METRIC = "exact_pairs_per_s"
+UNIT = "pairs/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def row_shares(n: int, ws: int):
+    """Row ranges [a, b) with about equal upper-triangle pair counts."""
+    cum = np.cumsum(np.arange(n - 1, -1, -1, dtype=np.float64))
+    total = cum[-1]
+    bounds = [0]
+    for r in range(1, ws):
+        bounds.append(int(np.searchsorted(cum, total * r / ws)) // 128 * 128)
+    bounds.append(n)
+    return [(bounds[i], bounds[i + 1]) for i in range(ws)]
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+def tc_fp8_peak(tch):
+    """Measured tcgen05 kind::f8f6f4 MMA rate of this GPU (tch-peak probe)."""
+    exe = os.path.join(ROOT, PKG, "bin", "tch-peak")
+    try:
+        out = subprocess.run([exe], capture_output=True, text=True, timeout=120).stdout
+        return json.loads(out.strip().splitlines()[-1])
+    except Exception as e:  # noqa: BLE001
+        log("peak probe failed:", e)
+        return {}
+
+
+def cpu_sample(x: np.ndarray, target_s: float, threads: int = 0):
+    """The oracle's brute-force count on the first rows of the upper triangle,
+    sized to about target_s seconds.  Returns (pairs/s, pairs, rows, secs)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ctypes
+
+    import oracle
+
+    lib = oracle.lib()
+    n, L = x.shape
+    xp = x.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16))
+    s = ctypes.c_uint64(0)
+    rows = 16
+    t = time.perf_counter()
+    pairs = lib.orc_upper_rows(xp, n, L, 0, rows, ctypes.byref(s), threads)
+    dt = time.perf_counter() - t
+    rate = pairs / max(dt, 1e-9)
+    want_pairs = rate * target_s
+    # rows from the top of the triangle: row i has n - 1 - i pairs
+    r1 = rows
+    acc = 0
+    while r1 < n and acc < want_pairs:
+        acc += n - 1 - r1
+        r1 += 1
+    t = time.perf_counter()
+    pairs = lib.orc_upper_rows(xp, n, L, rows, r1, ctypes.byref(s), threads)
+    dt = time.perf_counter() - t
+    return pairs / dt, int(pairs), (rows, r1), dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--kernel", default="tc_f8")
+    ap.add_argument("--tau", type=int, default=128)
+    ap.add_argument("--stripe", type=int, default=4096, help="rows per stripe of the e2e tch_run call")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--n", type=int, default=63005)
+    ap.add_argument("--L", type=int, default=1142)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    ws, rank, local = dist_env()
+    tch = importlib.import_module(PKG)
+    synth = importlib.import_module(PKG + ".synth")
+
+    t0 = time.perf_counter()
+    A = synth.longtail(n=args.n, L=args.L)
+    x, nd = tch.dense_ranks(A)
+    del A
+    n, L = x.shape
+    pairs_total = n * (n - 1) // 2
+    workload = {"workload": f"long-tail outbreak profiles {n} x {L} (synthetic, seeded)", "n": n, "loci": L,
+                "pairs": pairs_total, "tau": args.tau, "l2": "inputs larger than L2 (operands ~3 GB)"}
+    log(f"generated + ranked {n}x{L} in {time.perf_counter() - t0:.1f}s")
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        threads = os.cpu_count() or 1
+        vals = []
+        for _ in range(args.warmup if args.warmup < 1 else 1):
+            cpu_sample(x, 1.0, 0)
+        for _ in range(args.steps):
+            rate, pairs, rows, dt = cpu_sample(x, args.cpu_seconds / max(args.steps, 1), 0)
+            vals.append(rate)
+        v = statistics.median(vals)
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": pairs_total / v * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
+                "data": "synthetic", "config": workload,
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"brute-force count (check.py:39-44 restated in C, OpenMP) over the "
+                                           f"first upper-triangle rows, ~{args.cpu_seconds / max(args.steps, 1):.0f} s "
+                                           f"per step; ms_per_step extrapolates to all {pairs_total} pairs"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    device = local
+    torch.cuda.set_device(device)
+    assert tch.device_count() > 0
+
+    t0 = time.perf_counter()
+    enc = tch.encode_host(x, nd, args.tau)
+    log(f"encoded tau={args.tau}: D={enc.D} n_rare={enc.n_rare} in {time.perf_counter() - t0:.1f}s")
+    solver = tch.Solver.from_encoding(enc, kernel=args.kernel, device=device)
+    info = solver.info()
+    log("solver", info)
+    shares = row_shares(n, ws)
+    a, b = shares[rank]
+    ldo = (n + 7) // 8 * 8
+    out = torch.empty(((b - a), ldo), dtype=torch.int16, device=f"cuda:{device}")
+    stream = torch.cuda.Stream(device=device)
+    sp = stream.cuda_stream
+
+    def step():
+        solver.stripe(a, b - a, out.data_ptr(), ldo, sp)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    solver.check()
+    torch.cuda.synchronize()
+    clocks = Clocks(device)
+    clocks.start()
+    time.sleep(0.3)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    launch_ms = []
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev0.record(stream)
+    for k in range(args.steps):
+        evs[k][0].record(stream)
+        step()
+        evs[k][1].record(stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ck = clocks.stop()
+    solver.check()
+    total_ms = ev0.elapsed_time(ev1)
+    launch_ms = [s.elapsed_time(e) for s, e in evs]
+    if ws > 1:
+        tt = torch.tensor([total_ms], device=f"cuda:{device}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    ms_per_step = total_ms / args.steps
+    value = pairs_total / (ms_per_step / 1e3)
+
+    # roofline of the stripe kernel (one launch per step)
+    k_alg = L + int(enc.D)
+    my_pairs = sum(n - 1 - i for i in range(a, b))
+    ops_per_launch = 2.0 * my_pairs * k_alg
+    achieved = ops_per_launch / (statistics.median(launch_ms) / 1e3) / 1e12
+    peak_info = tc_fp8_peak(tch) if rank == 0 else {}
+    mp = measured_peaks()
+    peak = peak_info.get("tc_f8_tflops")
+    peak_src = "tch-peak tcgen05 kind::f8f6f4 probe on this GPU"
+    if not peak:
+        peak = 2 * (mp or {}).get("bf16_tflops", 1900.0)
+        peak_src = "2 x measured bf16 (fp8 dense rate ratio)"
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": peak_src,
+                "algorithmic_ops_per_launch": ops_per_launch, "k_per_pair": k_alg,
+                "k_padded_bytes": info["k_presence"] + info["k_onehot"],
+                "bf16_measured_tflops": (mp or {}).get("bf16_tflops"), "traffic": None}
+    prof = os.path.join(ROOT, "profiles", "tc_stripe_longtail_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            roofline["traffic"] = json.load(f).get("bytes_per_launch")
+
+    # e2e through tch_run with host buffers
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        tch.set_kernel(args.kernel)
+        h2d = enc.O.nbytes + enc.P.nbytes + enc.start.nbytes + enc.js.nbytes
+        d2h = 0
+        for r0 in range(0, n, args.stripe):
+            d2h += min(args.stripe, n - r0) * (n - r0) * 2
+
+        class Nop:
+            calls = 0
+
+            def __call__(self, ctx, r0, rows, w, ptr):
+                Nop.calls += 1
+
+        times = []
+        for k in range(args.e2e_steps + 1):
+            sink = Nop()
+            cb = tch.CB(sink)
+            import ctypes
+
+            secs = ctypes.c_double(0)
+            rg = ctypes.c_int(0)
+            err = ctypes.create_string_buffer(512)
+            t = time.perf_counter()
+            rc = tch.lib().tch_run(device, enc.n, enc.n_pad, tch._ptr(enc.O), enc.K1, tch._ptr(enc.P), enc.K2,
+                                   tch._ptr(enc.start), tch._ptr(enc.js), enc.n_rare, args.stripe, cb, None,
+                                   ctypes.byref(secs), ctypes.byref(rg), err, len(err))
+            dt = time.perf_counter() - t
+            if rc:
+                raise RuntimeError(err.value.decode())
+            if k > 0:  # first call warms the context and the pinned allocator
+                times.append(dt)
+        e2e_s = statistics.median(times)
+        e2e = {"value": pairs_total / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_s,
+               "path": f"tch_run (reference C ABI), host O/P/CSR, stripe {args.stripe}, no-op callback"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, pairs, rows, dt = cpu_sample(x, args.cpu_seconds, 0)
+        cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"oracle brute force (check.py:39-44 in C, OpenMP) on rows {rows[0]}-{rows[1]} of the upper "
+                         f"triangle: {pairs} pairs in {dt:.1f} s"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+                "scaling": "strong", "vs_baseline": None, "dtype": "fp8(e4m3 0/1) -> fp32 exact ints -> u16",
+                "data": "synthetic", "config": dict(workload, kernel=info["kernel"], stripe_e2e=args.stripe,
+                                                    parallelism=f"row shares x{ws}"),
+                "gpu_launches": args.steps, "clocks": ck, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "peak_probe": peak_info}
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

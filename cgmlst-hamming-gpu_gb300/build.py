@@ -109,8 +109,8 @@ def build_peak(verbose: bool = False) -> str:
     src = os.path.join(CSRC, "peak.cu")
     os.makedirs(BIN, exist_ok=True)
     out = os.path.join(BIN, "tch-peak")
-    if not _newer(out, [src]):
-        _run([nvcc(), *ARCH, "-O3", "-std=c++17", "-lineinfo", src, "-o", out + ".tmp"])
+    if not _newer(out, [src] + _headers()):
+        _run([nvcc(), *ARCH, "-O3", "-std=c++17", "-lineinfo", "-I", INCLUDE, "-I", CSRC, src, "-o", out + ".tmp"])
         os.replace(out + ".tmp", out)
     if verbose:
         print("built", out)
