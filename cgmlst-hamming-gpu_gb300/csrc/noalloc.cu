@@ -1,0 +1,150 @@
+// tch_stripe_noalloc: one stripe of the distance matrix for callers that may
+// not allocate device memory.
+//
+// Who needs it: code that runs where cudaMalloc is off limits — a host that
+// hands this library memory it already owns and forbids further device
+// allocations (a fixed-budget service, a framework whose allocator must see
+// every byte), or code running while the caller holds a stream it must not
+// synchronise through an allocation.  tch_solver_* allocate their operand
+// expansion and error word with cudaMalloc; this entry point instead keeps
+// that scratch in one file-scope device array, so a call allocates nothing.
+//
+// The scratch (g_noalloc_scratch, TCH_NOALLOC_SCRATCH_BYTES) holds
+//   [0, 256)       the device error word of the call
+//   [256, ...)     the e4m3 operand rows [presence | one-hot] of all n profiles
+// It is a static device array: the module that holds it is loaded on the
+// first call of this entry point (or at library load when CUDA loads modules
+// eagerly), and a device that has loaded it keeps the memory until the
+// process exits.  Every call shares the array and leaves its contents behind;
+// the error word is cleared at the start of each call and the operand rows
+// are rewritten in full.  Calls whose work overlaps on the GPU race on the
+// array, so issue them one after another (this entry point synchronises the
+// stream before it returns).
+//
+// Set-up, once per device: the first call on a device, with that device
+// current, takes the array's device address with cudaGetSymbolAddress (in
+// host code the symbol is only a host-side stand-in).  Make that first call
+// before any stream capture.
+
+#include <mutex>
+
+#include "tch_internal.cuh"
+
+namespace tch {
+namespace {
+
+static __device__ __align__(256) uint8_t g_noalloc_scratch[TCH_NOALLOC_SCRATCH_BYTES];
+
+constexpr size_t kErrBytes = 256;
+constexpr int kMaxDevices = 64;
+
+std::mutex g_mu;
+uint8_t* g_addr[kMaxDevices];  // device address of g_noalloc_scratch, per device
+
+int scratch_address(int device, uint8_t** out, Err& e) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (device < 0 || device >= kMaxDevices) return e.set("device %d out of range", device);
+    if (!g_addr[device]) {
+        void* p = nullptr;
+        const cudaError_t ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (ce != cudaSuccess) return e.set("cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(ce));
+        g_addr[device] = static_cast<uint8_t*>(p);
+    }
+    *out = g_addr[device];
+    return 0;
+}
+
+// start[] must be ascending with start[n] <= n_rare before any kernel walks it.
+__global__ void check_offsets_kernel(const uint32_t* __restrict__ start, int n, size_t n_rare, int* err) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t a = start[i], b = start[i + 1];
+        if (a > b || (size_t)b > n_rare) atomicOr(err, DEVERR_RARE_PAIR);
+    }
+}
+
+int read_error(int* d_err, cudaStream_t st, Err& e) {
+    int h = 0;
+    cudaError_t ce = cudaMemcpyAsync(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return e.set("reading the device error word: %s", cudaGetErrorString(ce));
+    if (h & DEVERR_RARE_PAIR) return e.set("rare CSR: offsets not ascending or a partner j not in (i, n)");
+    if (h) return e.set("device reported error 0x%x", h);
+    return 0;
+}
+
+}  // namespace
+}  // namespace tch
+
+using namespace tch;
+
+extern "C" int tch_stripe_noalloc(int device, int n, const uint8_t* d_O, size_t K1, const uint8_t* d_P, size_t K2,
+                                  const uint32_t* d_start, const uint32_t* d_js, size_t n_rare, int r0, int rows,
+                                  uint16_t* d_out, size_t ldo, void* stream, char* err, int errlen) {
+    Err e{err, errlen};
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (n <= 0) return e.set("n must be positive (got %d)", n);
+    if (K1 == 0 || K2 == 0 || (K1 % 1024) || (K2 % 1024))
+        return e.set("K1 and K2 must be positive multiples of 1024 (got %zu, %zu)", K1, K2);
+    if (r0 < 0 || rows <= 0 || r0 >= n) return e.set("stripe out of range (r0=%d rows=%d n=%d)", r0, rows, n);
+    if (r0 + rows > n) rows = n - r0;
+    if (ldo < (size_t)(n - r0) || (ldo & 1)) return e.set("ldo must be even and >= n - r0 (got %zu)", ldo);
+    if (!d_O || !d_P || !d_out || (n_rare && (!d_start || !d_js)) || !d_start)
+        return e.set("null device buffer");
+    if (((uintptr_t)d_out & 15) != 0) return e.set("output pointer must be 16-byte aligned");
+    if (!tc_kernel_compiled(TCH_KERNEL_TC_F8)) return e.set("the tensor-core kernel is not compiled in");
+
+    const size_t kp = up(K2, 128), kb = kp + up(K1, 128);  // bytes per operand row
+    const size_t x_rows = up((size_t)n, 256);
+    const size_t need = kErrBytes + x_rows * kb;
+    if (need > (size_t)TCH_NOALLOC_SCRATCH_BYTES)
+        return e.set("needs %zu bytes of scratch (n=%d padded to %zu rows x %zu bytes); the limit is %zu bytes",
+                     need, n, x_rows, kb, (size_t)TCH_NOALLOC_SCRATCH_BYTES);
+    if (kb > (size_t)INT32_MAX) return e.set("rows too wide");
+
+    cudaError_t ce = cudaSetDevice(device);
+    if (ce != cudaSuccess) return e.set("cudaSetDevice(%d): %s", device, cudaGetErrorString(ce));
+    uint8_t* scratch = nullptr;
+    if (scratch_address(device, &scratch, e)) return 1;
+    int* d_err = reinterpret_cast<int*>(scratch);
+    uint8_t* X = scratch + kErrBytes;
+    int sms = 0;
+    ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (ce != cudaSuccess) return e.set("cudaDeviceGetAttribute: %s", cudaGetErrorString(ce));
+
+    // 1. clear the error word, check the CSR offsets before anything walks them
+    ce = cudaMemsetAsync(d_err, 0, sizeof(int), st);
+    if (ce != cudaSuccess) return e.set("cudaMemsetAsync: %s", cudaGetErrorString(ce));
+    check_offsets_kernel<<<(n + 255) / 256, 256, 0, st>>>(d_start, n, n_rare, d_err);
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) return e.set("offset check: %s", cudaGetErrorString(ce));
+    if (read_error(d_err, st, e)) return 1;
+
+    // 2. bits -> e4m3 operand rows in the scratch array, 3. the stripe
+    BitOperands bits;
+    bits.P = reinterpret_cast<const uint32_t*>(d_P);
+    bits.O = reinterpret_cast<const uint32_t*>(d_O);
+    bits.wP = (int)(K2 / 32);
+    bits.wO = (int)(K1 / 32);
+    ce = launch_expand_bits(bits, n, x_rows, X, (int)kb, (int)kp, (int)K2, (int)K1, 0x38, 0x38, st);
+    if (ce != cudaSuccess) return e.set("operand expansion: %s", cudaGetErrorString(ce));
+    ByteOperands ops;
+    ops.X = X;
+    ops.n_rows = x_rows;
+    ops.kb = (int)kb;
+    ops.kp = (int)kp;
+    RareCSR rare;  // partner lists in any order: subtracted after the tile pass
+    rare.start = d_start;
+    rare.js = d_js;
+    rare.n_rare = n_rare;
+    rare.sorted = false;
+    StripeArgs a;
+    a.n = n;
+    a.r0 = r0;
+    a.rows = rows;
+    a.out = d_out;
+    a.ldo = ldo;
+    a.err = d_err;
+    ce = launch_tc_stripe(TCH_KERNEL_TC_F8, ops, nullptr, rare, a, sms, st);
+    if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
+    return read_error(d_err, st, e);
+}

@@ -143,6 +143,38 @@ int tch_solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_secs,
 void tch_solver_destroy(tch_solver* s);
 
 /* ----------------------------------------------------------------------------
+ * Stripe without any device allocation.  No counterpart in the reference: it
+ * exists for callers that may not call cudaMalloc (a service with a fixed
+ * device-memory budget that it hands out itself, a framework whose allocator
+ * must own every byte), which therefore cannot use tch_run or tch_solver_*.
+ * ------------------------------------------------------------------------- */
+
+/* Size of the library's file-scope device scratch array (64 MiB). */
+#define TCH_NOALLOC_SCRATCH_BYTES (64u << 20)
+
+/* One stripe, like tch_solver_stripe, with every input already in the
+ * caller's DEVICE memory and no allocation by the library:
+ *
+ *   d_O     n x K1 bits, d_P n x K2 bits (tch_run's row layout; rows beyond
+ *           n are not read), K1 and K2 multiples of 1024
+ *   d_start n + 1 offsets, d_js n_rare partners (any order within a row)
+ *   d_out   receives H[i][j] at (i - r0) * ldo + (j - r0) for the stripe's
+ *           rows i and columns max(i, r0) <= j < n; ldo even, d_out 16-byte
+ *           aligned
+ *
+ * The e4m3 operand rows of all n profiles and the device error word live in
+ * one static device array of TCH_NOALLOC_SCRATCH_BYTES bytes, so the call
+ * fails with a clear message when 256 + up(n, 256) * (K2 + K1) bytes exceed
+ * it (one byte per bit column; e.g. n = 2 048 with K2 + K1 up to 32 768).
+ * The first call on a device takes the array's address (cudaGetSymbolAddress)
+ * and must come before any stream capture.  Every call reuses the array, so
+ * calls that overlap on the GPU race; the call synchronises `stream` before it
+ * returns.  A device that has loaded the array keeps it until process exit. */
+int tch_stripe_noalloc(int device, int n, const uint8_t* d_O, size_t K1, const uint8_t* d_P, size_t K2,
+                       const uint32_t* d_start, const uint32_t* d_js, size_t n_rare, int r0, int rows,
+                       uint16_t* d_out, size_t ldo, void* stream, char* err, int errlen);
+
+/* ----------------------------------------------------------------------------
  * Host encoder (restates the reference host, main.rs:134-198 and 366-444).
  * Multi-threaded C++; `threads` <= 0 uses every hardware thread.
  * ------------------------------------------------------------------------- */
