@@ -97,7 +97,10 @@ def build_cli(verbose: bool = False) -> str | None:
     if not _newer(out, deps):
         cmd = ["g++", "-O3", "-std=c++17", "-pthread", "-I", INCLUDE, "-I", HOST, src, "-o", out + ".tmp",
                "-L", LIB, "-ltch", "-Wl,-rpath,$ORIGIN/../lib", "-ldl"]
-        _run(cmd)
+        try:  # deflate through zlib when its header and library are present
+            _run(cmd + ["-DTCH_HAVE_ZLIB", "-lz"])
+        except RuntimeError:  # stored-block gzip (valid, uncompressed)
+            _run(cmd)
         os.replace(out + ".tmp", out)
     if verbose:
         print("built", out)

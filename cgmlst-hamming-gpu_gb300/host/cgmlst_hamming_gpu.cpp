@@ -1,0 +1,627 @@
+// cgmlst-hamming-gpu — the command-line host of libtch.
+//
+// Restates the reference's Rust host (tensorcore/rs/src/main.rs) in C++, with
+// the same flags, the same cell semantics, filters and limits, the same
+// stderr log lines and the same TSV output, over the same C ABI:
+//
+//   flags          main.rs:19-73        layouts        main.rs:75-82
+//   parse_allele   main.rs:95-113       read_input     main.rs:115-123
+//   load           main.rs:286-311      filters        main.rs:313-351
+//   encode         main.rs:353-445 (tch_dense_ranks / tch_choose_tau /
+//                  tch_encode_host in libtch)
+//   GPU            main.rs:447-465 (tch_run + on_stripe, main.rs:200-211)
+//   write          main.rs:213-265, 472-490 (gzip: level 3, also for *.gz)
+//
+// Differences that do not change any output byte: the automatic tau uses rates
+// measured on GB300 instead of the L4 constants of main.rs:170-171, and the
+// writer formats and writes with a thread pool instead of rayon.
+
+#include <dlfcn.h>
+#include <errno.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "tch.h"
+#include "gzip_writer.h"
+
+namespace {
+
+// GB300 rates for the analytic tau (pair-columns/s of the tcgen05 fp8 kernel
+// and rare pairs/s of the fused subtraction), measured with bench.py.
+constexpr double kGemmRateGB300 = 1.6e15;
+constexpr double kRareRateGB300 = 2.0e10;
+
+[[noreturn]] void die(const std::string& msg) {
+    fprintf(stderr, "error: %s\n", msg.c_str());
+    exit(1);
+}
+
+std::string fmt(const char* f, ...) {
+    char buf[4096];
+    va_list ap;
+    va_start(ap, f);
+    vsnprintf(buf, sizeof buf, f, ap);
+    va_end(ap);
+    return buf;
+}
+
+double now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+enum class Layout { Full, LowerTri, UpperTri };
+
+struct Args {
+    std::string input;
+    bool has_output = false;
+    std::string output;
+    size_t threads = 0;
+    Layout layout = Layout::Full;
+    std::string input_sep = "\t";
+    std::string output_sep = "\t";
+    std::string index_name = "cgmlst-hamming-gpu";
+    std::string missing = "-";
+    bool skip_repl = false;
+    bool has_locus = false, has_sample = false;
+    double locus_pct = 0, sample_pct = 0;
+    bool gzip = false;
+    int max_dist = 0;
+    size_t tau = 0;
+    size_t stripe = 512;
+    size_t device = 0;
+    bool silent = false;
+};
+
+const char* kUsage =
+    "Exact cgMLST Hamming distance matrix on GB300 tensor cores\n\n"
+    "Usage: cgmlst-hamming-gpu [OPTIONS] --input <INPUT>\n\n"
+    "Options:\n"
+    "  -i, --input <INPUT>                      Input allele-call TSV (chewBBACA format). Use '-' for stdin\n"
+    "  -o, --output <OUTPUT>                    Output file [default: stdout]\n"
+    "  -t, --threads <THREADS>                  Number of CPU threads [default: all cores] [default: 0]\n"
+    "  -m, --matrix-format <MATRIX_FORMAT>      Output matrix layout [default: full] [possible values: full, "
+    "lower-tri, upper-tri]\n"
+    "  -d, --input-sep <INPUT_SEP>              Input field separator [default: \"\\t\"]\n"
+    "  -D, --output-sep <OUTPUT_SEP>            Output field separator [default: \"\\t\"]\n"
+    "  -x, --index-name <INDEX_NAME>            Name for the top-left index cell [default: cgmlst-hamming-gpu]\n"
+    "  -n, --missing-char <MISSING_CHAR>        Character used for missing data [default: -]\n"
+    "  -r, --skip-input-replacements            Do not strip the chewBBACA `INF-` prefix\n"
+    "  -L, --locus-completeness <PCT>           Keep only loci with at least this % of non-missing calls (0-100)\n"
+    "  -S, --sample-completeness <PCT>          Keep only samples with at least this % of non-missing calls (0-100)\n"
+    "  -z, --gzip                               gzip-compress the output (also enabled when -o ends with .gz)\n"
+    "  -X, --max-dist <MAX_DIST>                Cap distances at this value (0 = no cap) [default: 0]\n"
+    "      --tau <TAU>                          Frequency threshold: alleles seen >= tau times go to the "
+    "tensor-core GEMM [0 = auto] [default: 0]\n"
+    "      --stripe <STRIPE>                    Rows per GPU stripe [default: 512]\n"
+    "      --device <DEVICE>                    CUDA device [default: 0]\n"
+    "  -s, --silent                             Suppress progress/log messages on stderr\n"
+    "  -h, --help                               Print help\n"
+    "  -V, --version                            Print version\n";
+
+[[noreturn]] void usage_error(const std::string& msg) {
+    fprintf(stderr, "error: %s\n\nUsage: cgmlst-hamming-gpu [OPTIONS] --input <INPUT>\n\nFor more information, try "
+            "'--help'.\n", msg.c_str());
+    exit(2);
+}
+
+template <class T>
+T parse_num(const std::string& flag, const std::string& v, bool allow_neg, bool is_float) {
+    errno = 0;
+    char* end = nullptr;
+    if (v.empty()) usage_error(fmt("invalid value '' for '%s'", flag.c_str()));
+    if (is_float) {
+        double d = strtod(v.c_str(), &end);
+        if (*end || errno) usage_error(fmt("invalid value '%s' for '%s': invalid float literal", v.c_str(), flag.c_str()));
+        return (T)d;
+    }
+    if (!allow_neg && v[0] == '-') usage_error(fmt("invalid value '%s' for '%s': invalid digit found in string",
+                                                   v.c_str(), flag.c_str()));
+    long long x = strtoll(v.c_str(), &end, 10);
+    if (*end || errno) usage_error(fmt("invalid value '%s' for '%s': invalid digit found in string", v.c_str(),
+                                       flag.c_str()));
+    return (T)x;
+}
+
+Args parse_args(int argc, char** argv) {
+    Args a;
+    bool have_input = false;
+    struct Opt {
+        const char* shrt;
+        const char* lng;
+        bool takes;
+    };
+    static const Opt opts[] = {{"i", "input", true},         {"o", "output", true},
+                               {"t", "threads", true},       {"m", "matrix-format", true},
+                               {"d", "input-sep", true},     {"D", "output-sep", true},
+                               {"x", "index-name", true},    {"n", "missing-char", true},
+                               {"r", "skip-input-replacements", false},
+                               {"L", "locus-completeness", true}, {"S", "sample-completeness", true},
+                               {"z", "gzip", false},         {"X", "max-dist", true},
+                               {nullptr, "tau", true},       {nullptr, "stripe", true},
+                               {nullptr, "device", true},    {"s", "silent", false},
+                               {"h", "help", false},         {"V", "version", false}};
+    for (int k = 1; k < argc; k++) {
+        std::string arg = argv[k];
+        const Opt* o = nullptr;
+        std::string val;
+        bool has_val = false;
+        if (arg.rfind("--", 0) == 0 && arg.size() > 2) {
+            std::string name = arg.substr(2);
+            size_t eq = name.find('=');
+            if (eq != std::string::npos) {
+                val = name.substr(eq + 1);
+                name = name.substr(0, eq);
+                has_val = true;
+            }
+            for (auto& c : opts)
+                if (name == c.lng) o = &c;
+            if (!o) usage_error(fmt("unexpected argument '%s' found", arg.c_str()));
+        } else if (arg.size() >= 2 && arg[0] == '-' && arg[1] != '-') {
+            std::string s(1, arg[1]);
+            for (auto& c : opts)
+                if (c.shrt && s == c.shrt) o = &c;
+            if (!o) usage_error(fmt("unexpected argument '%s' found", arg.c_str()));
+            if (arg.size() > 2) {
+                if (!o->takes) usage_error(fmt("unexpected argument '%s' found", arg.c_str()));
+                val = arg.substr(2);
+                has_val = true;
+            }
+        } else {
+            usage_error(fmt("unexpected argument '%s' found", arg.c_str()));
+        }
+        const std::string flag = o->lng ? std::string("--") + o->lng : arg;
+        if (o->takes && !has_val) {
+            if (k + 1 >= argc) usage_error(fmt("a value is required for '%s <VALUE>' but none was supplied",
+                                               flag.c_str()));
+            val = argv[++k];
+        }
+        const std::string name = o->lng;
+        if (name == "help") {
+            fputs(kUsage, stdout);
+            exit(0);
+        } else if (name == "version") {
+            printf("cgmlst-hamming-gpu %d.0.0 (GB300)\n", tch_version());
+            exit(0);
+        } else if (name == "input") {
+            a.input = val;
+            have_input = true;
+        } else if (name == "output") {
+            a.output = val;
+            a.has_output = true;
+        } else if (name == "threads") {
+            a.threads = parse_num<size_t>(flag, val, false, false);
+        } else if (name == "matrix-format") {
+            if (val == "full") a.layout = Layout::Full;
+            else if (val == "lower-tri") a.layout = Layout::LowerTri;
+            else if (val == "upper-tri") a.layout = Layout::UpperTri;
+            else usage_error(fmt("invalid value '%s' for '--matrix-format <MATRIX_FORMAT>'\n  [possible values: "
+                                 "full, lower-tri, upper-tri]", val.c_str()));
+        } else if (name == "input-sep") {
+            a.input_sep = val;
+        } else if (name == "output-sep") {
+            a.output_sep = val;
+        } else if (name == "index-name") {
+            a.index_name = val;
+        } else if (name == "missing-char") {
+            a.missing = val;
+        } else if (name == "skip-input-replacements") {
+            a.skip_repl = true;
+        } else if (name == "locus-completeness") {
+            a.locus_pct = parse_num<double>(flag, val, true, true);
+            a.has_locus = true;
+        } else if (name == "sample-completeness") {
+            a.sample_pct = parse_num<double>(flag, val, true, true);
+            a.has_sample = true;
+        } else if (name == "gzip") {
+            a.gzip = true;
+        } else if (name == "max-dist") {
+            a.max_dist = parse_num<int>(flag, val, true, false);
+        } else if (name == "tau") {
+            a.tau = parse_num<size_t>(flag, val, false, false);
+        } else if (name == "stripe") {
+            a.stripe = parse_num<size_t>(flag, val, false, false);
+        } else if (name == "device") {
+            a.device = parse_num<size_t>(flag, val, false, false);
+        } else if (name == "silent") {
+            a.silent = true;
+        }
+    }
+    if (!have_input) usage_error("the following required arguments were not provided:\n  --input <INPUT>");
+    return a;
+}
+
+template <class F>
+void parallel_for(size_t threads, size_t count, size_t chunk, F&& f) {
+    if (threads <= 1 || count <= chunk) {
+        for (size_t b = 0; b < count; b += chunk) f(b, std::min(count, b + chunk));
+        return;
+    }
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    for (size_t t = 0; t < threads; t++)
+        pool.emplace_back([&] {
+            for (;;) {
+                const size_t b = next.fetch_add(chunk);
+                if (b >= count) break;
+                f(b, std::min(count, b + chunk));
+            }
+        });
+    for (auto& th : pool) th.join();
+}
+
+// ---- text semantics ---------------------------------------------------------------
+
+// Decodes the UTF-8 code point starting at s[i] (input already validated).
+uint32_t cp_at(const std::string& s, size_t i, size_t* len) {
+    const unsigned char c = (unsigned char)s[i];
+    if (c < 0x80) { *len = 1; return c; }
+    if ((c >> 5) == 6) { *len = 2; return ((c & 0x1F) << 6) | (s[i + 1] & 0x3F); }
+    if ((c >> 4) == 14) { *len = 3; return ((c & 0x0F) << 12) | ((s[i + 1] & 0x3F) << 6) | (s[i + 2] & 0x3F); }
+    *len = 4;
+    return ((c & 0x07) << 18) | ((s[i + 1] & 0x3F) << 12) | ((s[i + 2] & 0x3F) << 6) | (s[i + 3] & 0x3F);
+}
+
+// Unicode White_Space, the set Rust's str::trim removes.
+bool is_ws(uint32_t c) {
+    return (c >= 0x09 && c <= 0x0D) || c == 0x20 || c == 0x85 || c == 0xA0 || c == 0x1680 ||
+           (c >= 0x2000 && c <= 0x200A) || c == 0x2028 || c == 0x2029 || c == 0x202F || c == 0x205F || c == 0x3000;
+}
+
+// [b, e) of the trimmed cell inside s.
+void trim(const std::string& s, size_t& b, size_t& e) {
+    while (b < e) {
+        size_t len;
+        const uint32_t c = cp_at(s, b, &len);
+        if (!is_ws(c)) break;
+        b += len;
+    }
+    while (e > b) {
+        size_t p = e - 1;
+        while (p > b && ((unsigned char)s[p] & 0xC0) == 0x80) p--;
+        size_t len;
+        const uint32_t c = cp_at(s, p, &len);
+        if (!is_ws(c)) break;
+        e = p;
+    }
+}
+
+// parse_allele (main.rs:98-113): 0 = missing; returns false on u64 overflow.
+bool parse_allele(const std::string& s, size_t b, size_t e, bool skip_repl, const std::string& missing,
+                  uint64_t* out) {
+    trim(s, b, e);
+    if (!skip_repl && e - b >= 4 && s.compare(b, 4, "INF-") == 0) b += 4;
+    if (b == e || (e - b == missing.size() && s.compare(b, e - b, missing) == 0)) {
+        *out = 0;
+        return true;
+    }
+    uint64_t v = 0;
+    for (size_t p = b; p < e; p++) {
+        const char c = s[p];
+        if (c < '0' || c > '9') {
+            *out = 0;
+            return true;
+        }
+    }
+    for (size_t p = b; p < e; p++) {
+        const uint64_t d = (uint64_t)(s[p] - '0');
+        if (v > (UINT64_MAX - d) / 10) return false;
+        v = v * 10 + d;
+    }
+    *out = v;
+    return true;
+}
+
+bool valid_utf8(const std::string& s) {
+    size_t i = 0, n = s.size();
+    while (i < n) {
+        const unsigned char c = (unsigned char)s[i];
+        size_t len;
+        uint32_t cp;
+        if (c < 0x80) { i++; continue; }
+        if ((c >> 5) == 6) { len = 2; cp = c & 0x1F; }
+        else if ((c >> 4) == 14) { len = 3; cp = c & 0x0F; }
+        else if ((c >> 3) == 30) { len = 4; cp = c & 0x07; }
+        else return false;
+        if (i + len > n) return false;
+        for (size_t k = 1; k < len; k++) {
+            const unsigned char d = (unsigned char)s[i + k];
+            if ((d & 0xC0) != 0x80) return false;
+            cp = (cp << 6) | (d & 0x3F);
+        }
+        if ((len == 2 && cp < 0x80) || (len == 3 && cp < 0x800) || (len == 4 && (cp < 0x10000 || cp > 0x10FFFF)) ||
+            (cp >= 0xD800 && cp <= 0xDFFF))
+            return false;
+        i += len;
+    }
+    return true;
+}
+
+bool read_all(const std::string& path, std::string& buf, std::string& err) {
+    FILE* f = path == "-" ? stdin : fopen(path.c_str(), "rb");
+    if (!f) {
+        err = strerror(errno);
+        return false;
+    }
+    char tmp[1 << 16];
+    size_t r;
+    while ((r = fread(tmp, 1, sizeof tmp, f)) > 0) buf.append(tmp, r);
+    const bool bad = ferror(f);
+    if (f != stdin) fclose(f);
+    if (bad) {
+        err = "read error";
+        return false;
+    }
+    if (!valid_utf8(buf)) {
+        err = "stream did not contain valid UTF-8";
+        return false;
+    }
+    return true;
+}
+
+// str::lines: (begin, end) of every line, '\n' and one '\r' before it removed.
+std::vector<std::pair<size_t, size_t>> rust_lines(const std::string& t) {
+    std::vector<std::pair<size_t, size_t>> out;
+    size_t b = 0;
+    while (b < t.size()) {
+        size_t nl = t.find('\n', b);
+        if (nl == std::string::npos) {
+            out.push_back({b, t.size()});
+            break;
+        }
+        size_t e = nl;
+        if (e > b && t[e - 1] == '\r') e--;
+        out.push_back({b, e});
+        b = nl + 1;
+    }
+    return out;
+}
+
+// ---- output ----------------------------------------------------------------------
+
+struct Sink {
+    std::vector<std::vector<uint16_t>>* upper;
+    size_t threads;
+};
+
+void on_stripe(void* ctx, int r0, int rows, size_t w, const uint16_t* stripe) {
+    Sink* s = (Sink*)ctx;
+    parallel_for(s->threads, (size_t)rows, 16, [&](size_t a, size_t b) {
+        for (size_t r = a; r < b; r++)
+            (*s->upper)[r0 + r].assign(stripe + r * w + r + 1, stripe + (r + 1) * w);
+    });
+}
+
+inline uint16_t at(const std::vector<std::vector<uint16_t>>& upper, size_t i, size_t j) {
+    if (i == j) return 0;
+    if (j > i) return upper[i][j - i - 1];
+    return upper[j][i - j - 1];
+}
+
+inline void put_int(std::string& b, int v) {
+    char tmp[16];
+    int k = 0;
+    bool neg = v < 0;
+    unsigned u = neg ? 0u - (unsigned)v : (unsigned)v;
+    do {
+        tmp[k++] = (char)('0' + u % 10);
+        u /= 10;
+    } while (u);
+    if (neg) tmp[k++] = '-';
+    while (k) b.push_back(tmp[--k]);
+}
+
+// write_matrix (main.rs:225-265): header, then rows formatted in parallel
+// chunks of 1024 and written in order.
+template <class W>
+void write_matrix(W& out, const std::vector<std::string>& ids, const std::vector<std::vector<uint16_t>>& upper,
+                  const std::string& osep, const std::string& index_name, Layout lay, int cap, size_t threads) {
+    const size_t n = ids.size();
+    std::string head = index_name;
+    for (auto& id : ids) {
+        head += osep;
+        head += id;
+    }
+    head += '\n';
+    out.write(head.data(), head.size());
+    const size_t CHUNK = 1024;
+    std::vector<std::string> bufs;
+    for (size_t start = 0; start < n; start += CHUNK) {
+        const size_t end = std::min(n, start + CHUNK);
+        bufs.assign(end - start, std::string());
+        parallel_for(threads, end - start, 8, [&](size_t a, size_t b) {
+            for (size_t q = a; q < b; q++) {
+                const size_t i = start + q;
+                std::string& buf = bufs[q];
+                buf.reserve((n + 1) * 7);
+                buf += ids[i];
+                for (size_t j = 0; j < n; j++) {
+                    buf += osep;
+                    const bool keep = lay == Layout::Full ? true : lay == Layout::LowerTri ? j <= i : j >= i;
+                    int v = keep ? (int)at(upper, i, j) : 0;
+                    if (cap > 0 && v > cap) v = cap;
+                    put_int(buf, v);
+                }
+                buf += '\n';
+            }
+        });
+        for (auto& b : bufs) out.write(b.data(), b.size());
+    }
+}
+
+struct FileOut {
+    FILE* f;
+    void write(const char* p, size_t n) {
+        if (n && fwrite(p, 1, n, f) != n) die(fmt("writing output: %s", strerror(errno)));
+    }
+};
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    Args args = parse_args(argc, argv);
+    const double t_start = now();
+    auto log = [&](const std::string& m) {
+        if (!args.silent) fprintf(stderr, "%s\n", m.c_str());
+    };
+    size_t threads = args.threads ? args.threads : std::max(1u, std::thread::hardware_concurrency());
+    if (args.input_sep.size() != 1) die("input separator must be a single character");
+    const char sep = args.input_sep[0];
+    if ((size_t)tch_device_count() <= args.device) die(fmt("CUDA device %zu not available", args.device));
+
+    // ---- load (main.rs:286-311)
+    double t = now();
+    std::string text, rerr;
+    if (!read_all(args.input, text, rerr)) die(fmt("reading %s: %s", args.input.c_str(), rerr.c_str()));
+    auto lines = rust_lines(text);
+    if (lines.empty()) die("empty input");
+    size_t L = 1;
+    for (size_t p = lines[0].first; p < lines[0].second; p++) L += text[p] == sep;
+    L -= 1;
+    std::vector<std::pair<size_t, size_t>> data;
+    for (size_t k = 1; k < lines.size(); k++)
+        if (lines[k].second > lines[k].first) data.push_back(lines[k]);
+    size_t n = data.size();
+    std::vector<std::string> ids(n);
+    std::vector<uint64_t> calls(n * L, 0);
+    std::atomic<long> bad_row{-1};
+    std::vector<std::string> bad_cell(1);
+    std::atomic<bool> bad_taken{false};
+    parallel_for(threads, n, 64, [&](size_t a, size_t b) {
+        for (size_t i = a; i < b; i++) {
+            size_t p = data[i].first, e = data[i].second;
+            size_t f = text.find(sep, p);
+            if (f == std::string::npos || f > e) f = e;
+            ids[i] = text.substr(p, f - p);
+            size_t k = 0;
+            while (f < e) {
+                const size_t cb = f + 1;
+                size_t ce = text.find(sep, cb);
+                if (ce == std::string::npos || ce > e) ce = e;
+                uint64_t v;
+                if (!parse_allele(text, cb, ce, args.skip_repl, args.missing, &v)) {
+                    bool expect = false;
+                    if (bad_taken.compare_exchange_strong(expect, true)) {
+                        size_t tb = cb, te = ce;
+                        trim(text, tb, te);
+                        bad_cell[0] = text.substr(tb, te - tb);
+                        bad_row = (long)i;
+                    }
+                    v = 0;
+                }
+                if (k < L) calls[i * L + k] = v;
+                k++;
+                f = ce;
+            }
+        }
+    });
+    if (bad_row >= 0) die(fmt("sample %s: allele '%s' too large", ids[bad_row].c_str(), bad_cell[0].c_str()));
+    std::string().swap(text);
+    log(fmt("Loaded %zu samples x %zu loci in %.2fs", n, L, now() - t));
+
+    // ---- completeness filters (main.rs:313-348)
+    if (args.has_locus) {
+        std::vector<size_t> keep;
+        for (size_t k = 0; k < L; k++) {
+            size_t c = 0;
+            for (size_t i = 0; i < n; i++) c += calls[i * L + k] != 0;
+            if (((double)c / (double)n) * 100.0 >= args.locus_pct) keep.push_back(k);
+        }
+        if (keep.size() != L) {
+            std::vector<uint64_t> nc(n * keep.size());
+            for (size_t i = 0; i < n; i++)
+                for (size_t d = 0; d < keep.size(); d++) nc[i * keep.size() + d] = calls[i * L + keep[d]];
+            calls.swap(nc);
+            L = keep.size();
+        }
+        log(fmt("Locus completeness >= %s%%: kept %zu loci", fmt("%g", args.locus_pct).c_str(), L));
+    }
+    if (args.has_sample) {
+        std::vector<size_t> keep;
+        for (size_t i = 0; i < n; i++) {
+            size_t c = 0;
+            for (size_t k = 0; k < L; k++) c += calls[i * L + k] != 0;
+            if (((double)c / (double)L) * 100.0 >= args.sample_pct) keep.push_back(i);
+        }
+        if (keep.size() != n) {
+            std::vector<uint64_t> nc(keep.size() * L);
+            std::vector<std::string> nids;
+            for (size_t d = 0; d < keep.size(); d++) {
+                std::copy(calls.begin() + keep[d] * L, calls.begin() + (keep[d] + 1) * L, nc.begin() + d * L);
+                nids.push_back(ids[keep[d]]);
+            }
+            calls.swap(nc);
+            ids.swap(nids);
+            n = keep.size();
+        }
+        log(fmt("Sample completeness >= %s%%: kept %zu samples", fmt("%g", args.sample_pct).c_str(), n));
+    }
+    if (L > 65535) die("more than 65535 loci (u16 distances)");
+
+    // ---- encode (main.rs:353-445)
+    t = now();
+    char err[512] = {0};
+    std::vector<uint16_t> x(n * L);
+    std::vector<uint32_t> nd(L);
+    if (tch_dense_ranks(calls.data(), (int)n, (int)L, x.data(), nd.data(), (int)threads, err, sizeof err)) die(err);
+    std::vector<uint64_t>().swap(calls);
+    std::vector<std::vector<uint16_t>> upper(n);
+    double gpu_secs = 0;
+    if (n >= 2 && L > 0) {
+        const size_t stripe = std::max<size_t>(args.stripe, 8) / 8 * 8;
+        int tau = (int)args.tau;
+        if (tau <= 0 &&
+            tch_choose_tau(x.data(), nd.data(), (int)n, (int)L, (int)stripe, tch_free_vram((int)args.device),
+                           kGemmRateGB300, kRareRateGB300, args.silent ? 0 : 1, &tau, err, sizeof err))
+            die(err);
+        tch_host_encoding enc;
+        if (tch_encode_host(x.data(), nd.data(), (int)n, (int)L, tau, (int)threads, &enc, err, sizeof err)) die(err);
+        log(fmt("Encoded in %.2fs: tau=%d, one-hot cols=%zu, rare equal pairs=%zu", now() - t, tau, enc.D,
+                enc.n_rare));
+        // ---- GPU (main.rs:447-465)
+        t = now();
+        Sink sink{&upper, threads};
+        int rare_gpu = 0;
+        const int rc = tch_run((int)args.device, (int)n, enc.n_pad, enc.O, enc.K1, enc.P, enc.K2, enc.start, enc.js,
+                               enc.n_rare, (int)stripe, on_stripe, &sink, &gpu_secs, &rare_gpu, err, sizeof err);
+        tch_host_encoding_free(&enc);
+        if (rc) die(fmt("CUDA: %s", err));
+        log(fmt("Computed %zu x %zu matrix on tensor cores in %.2fs (GPU pipeline %.2fs, rare pairs on %s)", n, n,
+                now() - t, gpu_secs, rare_gpu ? "GPU" : "host"));
+    } else {
+        for (size_t i = 0; i < n; i++) upper[i].assign(n - 1 - i, 0);
+    }
+
+    // ---- write (main.rs:472-490)
+    t = now();
+    const bool gz = args.gzip || (args.has_output && args.output.size() >= 3 &&
+                                  args.output.compare(args.output.size() - 3, 3, ".gz") == 0);
+    FILE* f = stdout;
+    if (args.has_output) {
+        f = fopen(args.output.c_str(), "wb");
+        if (!f) die(fmt("creating %s: %s", args.output.c_str(), strerror(errno)));
+    }
+    setvbuf(f, nullptr, _IOFBF, 16 << 20);
+    FileOut fo{f};
+    if (gz) {
+        tch_host::GzipWriter<FileOut> z(fo, 3);
+        write_matrix(z, ids, upper, args.output_sep, args.index_name, args.layout, args.max_dist, threads);
+        z.finish();
+    } else {
+        write_matrix(fo, ids, upper, args.output_sep, args.index_name, args.layout, args.max_dist, threads);
+    }
+    if (fflush(f) != 0) die(fmt("writing output: %s", strerror(errno)));
+    if (f != stdout) fclose(f);
+    log(fmt("Wrote output in %.2fs. Total %.2fs", now() - t, now() - t_start));
+    return 0;
+}

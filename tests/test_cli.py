@@ -1,0 +1,166 @@
+"""The command-line host, driven the way the reference's exactness check drives
+its binary (tensorcore/rs/check.py:47-83): same generator, same 3 cases x 8 flag
+sets, output parsed the same way and compared cell for cell — here against the
+golden digests of the matrices check.py expects, and against the oracle."""
+import gzip
+import hashlib
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+import refgen
+
+
+def cli(pkg):
+    assert os.path.exists(pkg.CLI_PATH), "CLI not built"
+    return pkg.CLI_PATH
+
+
+def run(pkg, args, stdin=None):
+    return subprocess.run([cli(pkg), *args], capture_output=True, text=True, input=stdin, timeout=600)
+
+
+def parse(stdout, sep="\t"):
+    """check.py:51-53."""
+    lines = stdout.rstrip("\n").split("\n")
+    return np.array([[int(x) for x in ln.split(sep)[1:]] for ln in lines[1:]])
+
+
+def mat_sha(M):
+    return hashlib.sha256(np.ascontiguousarray(M, dtype="<i8").tobytes()).hexdigest()
+
+
+# ------------------------------------------------------------------ CPU: host-side semantics
+
+def test_usage_errors(pkg):
+    r = run(pkg, [])
+    assert r.returncode == 2 and "--input <INPUT>" in r.stderr
+    r = run(pkg, ["-i", "x", "-m", "diagonal"])
+    assert r.returncode == 2 and "possible values: full, lower-tri, upper-tri" in r.stderr
+    r = run(pkg, ["-i", "x", "--tau", "-3"])
+    assert r.returncode == 2
+    r = run(pkg, ["--help"])
+    assert r.returncode == 0 and "--stripe" in r.stdout and "--matrix-format" in r.stdout
+
+
+def test_separator_checked_before_device(pkg):
+    r = run(pkg, ["-i", "x", "-d", "ab"])
+    assert r.returncode == 1 and r.stderr.strip() == "error: input separator must be a single character"
+
+
+def test_missing_device_is_fatal(pkg):
+    if pkg.device_count() > 0:
+        pytest.skip("a GPU is present")
+    r = run(pkg, ["-i", "x", "--device", "0"])
+    assert r.returncode == 1 and "CUDA device 0 not available" in r.stderr
+
+
+# ------------------------------------------------------------------ GPU: the check.py matrix
+
+@pytest.fixture(scope="module")
+def case_files(tmp_path_factory, golden):
+    d = tmp_path_factory.mktemp("checkpy")
+    out = []
+    for c in golden["cases"]:
+        A, cells = refgen.checkpy_make(c["n"], c["L"], c["seed"], c["hashed"])
+        p = d / f"c{c['seed']}.tsv"
+        p.write_text(refgen.checkpy_tsv(cells, c["L"]))
+        out.append((c, str(p), A))
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case_idx", [0, 1, 2])
+@pytest.mark.parametrize("flags_idx", range(len(refgen.CHECKPY_FLAGSETS)))
+def test_checkpy_matrix(pkg, case_files, case_idx, flags_idx):
+    c, path, A = case_files[case_idx]
+    args, kind = refgen.CHECKPY_FLAGSETS[flags_idx]
+    r = run(pkg, ["-s", "-i", path, *args])
+    assert r.returncode == 0, r.stderr
+    got = parse(r.stdout, "," if "-D" in args else "\t")
+    assert mat_sha(got) == c["expected"][kind]  # the matrix the reference's check.py expects
+
+
+@pytest.mark.gpu
+def test_full_text_equals_oracle(pkg, tmp_path):
+    text = ("FILE\tL0\tL1\tL2\tL3\n"
+            "a\t1\t2\tINF-3\t-\n"
+            "b\t 1\t5\t3\tLNF\r\n"
+            "\n"
+            "c\t1\t\t3\t4\textra\n"
+            "d\tINF-INF-1\t2\n"
+            "e\t7\t2\t3\t4\n")
+    p = tmp_path / "t.tsv"
+    p.write_text(text)
+    ids, x, cnt, H = oracle.distances_from_text(text)
+    for args, kw in [([], {}), (["-m", "lower-tri", "-D", ";"], dict(mode="lower-tri", osep=";")),
+                     (["-m", "upper-tri", "-X", "1", "-x", "ID"], dict(mode="upper-tri", cap=1, index_name="ID"))]:
+        r = run(pkg, ["-s", "-i", str(p), *args])
+        assert r.returncode == 0, r.stderr
+        assert r.stdout == oracle.write_matrix(ids, H, **kw)
+
+
+@pytest.mark.gpu
+def test_options_and_streams(pkg, tmp_path, case_files):
+    c, path, A = case_files[0]
+    with open(path) as f:
+        text = f.read()
+    ids, x, cnt, H = oracle.distances_from_text(text)
+    want = oracle.write_matrix(ids, H)
+    # stdin, output file, gzip by flag and by extension, threads, stripe
+    r = run(pkg, ["-s", "-i", "-", "-t", "3", "--stripe", "40"], stdin=text)
+    assert r.returncode == 0 and r.stdout == want
+    out = tmp_path / "o.tsv"
+    assert run(pkg, ["-s", "-i", path, "-o", str(out)]).returncode == 0
+    assert out.read_text() == want
+    gz = tmp_path / "o.tsv.gz"
+    assert run(pkg, ["-s", "-i", path, "-o", str(gz)]).returncode == 0
+    assert gzip.decompress(gz.read_bytes()).decode() == want
+    z = tmp_path / "o2"
+    assert run(pkg, ["-s", "-i", path, "-o", str(z), "-z"]).returncode == 0
+    assert gzip.decompress(z.read_bytes()).decode() == want
+    # logging on stderr without -s
+    r = run(pkg, ["-i", path, "--tau", "4"])
+    assert r.returncode == 0 and "Loaded 300 samples x 97 loci" in r.stderr and "tau=4" in r.stderr
+
+
+@pytest.mark.gpu
+def test_filters_and_cell_options(pkg, tmp_path):
+    text = ("F\ta\tb\tc\td\n"
+            "A\t1\tX\t1\tINF-2\n"
+            "B\t2\tX\t-\t2\n"
+            "C\t1\t3\tX\tINF-2\n"
+            "D\t-\t-\t-\t5\n")
+    p = tmp_path / "f.tsv"
+    p.write_text(text)
+    for args, kw in [(["-L", "70"], dict(locus_pct=70.0)), (["-S", "60"], dict(sample_pct=60.0)),
+                     (["-L", "50", "-S", "50"], dict(locus_pct=50.0, sample_pct=50.0)),
+                     (["-n", "X"], dict(missing="X")), (["-r"], dict(skip_repl=True))]:
+        ids, x, cnt, H = oracle.distances_from_text(text, **kw)
+        r = run(pkg, ["-s", "-i", str(p), *args])
+        assert r.returncode == 0, (args, r.stderr)
+        assert r.stdout == oracle.write_matrix(ids, H), args
+
+
+@pytest.mark.gpu
+def test_edge_inputs(pkg, tmp_path):
+    def go(text, *args):
+        p = tmp_path / "e.tsv"
+        p.write_bytes(text.encode() if isinstance(text, str) else text)
+        return run(pkg, ["-s", "-i", str(p), *args])
+
+    r = go("")
+    assert r.returncode == 1 and "empty input" in r.stderr
+    r = go("F\tL0\nA\t18446744073709551616\n")
+    assert r.returncode == 1 and "sample A: allele '18446744073709551616' too large" in r.stderr
+    r = go(b"F\tL0\nA\t\xff\n")
+    assert r.returncode == 1 and "valid UTF-8" in r.stderr
+    r = go("F\tL0\tL1\nA\t1\t2\n")  # one sample: no GPU work, 1x1 matrix
+    assert r.returncode == 0 and r.stdout == "cgmlst-hamming-gpu\tA\nA\t0\n"
+    r = go("F\nA\nB\n")  # no loci
+    assert r.returncode == 0 and r.stdout == "cgmlst-hamming-gpu\tA\tB\nA\t0\t0\nB\t0\t0\n"
+    r = go("F\tL0\n")  # header only
+    assert r.returncode == 0 and r.stdout == "cgmlst-hamming-gpu\n"
