@@ -102,6 +102,12 @@ def lib():
         L.tch_encode_host.argtypes = [c_void, c_void, c_int, c_int, c_int, c_int, P(HostEncoding), c_char_p, c_int]
         L.tch_encode_host.restype = c_int
         L.tch_host_encoding_free.argtypes, L.tch_host_encoding_free.restype = [P(HostEncoding)], None
+        L.tch_solver_from_calls.argtypes = [c_int, c_int, c_int, c_void, c_int, c_int, P(c_void), c_char_p, c_int]
+        L.tch_solver_from_calls.restype = c_int
+        L.tch_run_calls.argtypes = [c_int, c_int, c_int, c_void, c_int, c_int, CB, c_void, P(c_double), P(c_int),
+                                    c_char_p, c_int]
+        L.tch_run_calls.restype = c_int
+        L.tch_set_tau_model.argtypes, L.tch_set_tau_model.restype = [c_double, c_double], c_int
         _lib = L
     return _lib
 
@@ -238,6 +244,25 @@ def run(enc: Encoding, stripe: int = 512, device: int = 0, sink: StripeSink | No
     return sink.H, secs.value, rare_gpu.value, sink
 
 
+def run_calls(calls: np.ndarray, stripe: int = 512, tau: int = 0, device: int = 0, sink: StripeSink | None = None):
+    """tch_run_calls: device encoding + stripes; returns (H, gpu_secs, tau_used, sink)."""
+    calls = np.ascontiguousarray(calls, dtype=np.uint64)
+    n, L = calls.shape
+    sink = sink or StripeSink(n)
+    cb = CB(sink)
+    secs = ctypes.c_double(0)
+    tau_used = ctypes.c_int(0)
+    err = _errbuf()
+    _check(lib().tch_run_calls(device, n, L, _ptr(calls), tau, stripe, cb, None, ctypes.byref(secs),
+                               ctypes.byref(tau_used), err, len(err)), err)
+    return sink.H, secs.value, tau_used.value, sink
+
+
+def set_tau_model(gemm_rate: float, rare_rate: float) -> None:
+    if lib().tch_set_tau_model(gemm_rate, rare_rate):
+        raise TchError("rates must be positive")
+
+
 # ---------------------------------------------------------------------------------------
 # solver (device-resident operands)
 # ---------------------------------------------------------------------------------------
@@ -253,6 +278,17 @@ class Solver:
         _check(lib().tch_solver_from_bits(device, enc.n, enc.n_pad, _ptr(enc.O), enc.K1, _ptr(enc.P), enc.K2,
                                           _ptr(enc.start), _ptr(enc.js), enc.n_rare, kernel_id(kernel),
                                           ctypes.byref(h), err, len(err)), err)
+        return cls(h)
+
+    @classmethod
+    def from_calls(cls, calls: np.ndarray, tau: int = 0, kernel="auto", device: int = 0):
+        """Device encoding of allele calls (n x L u64, 0 = missing), tau <= 0 automatic."""
+        calls = np.ascontiguousarray(calls, dtype=np.uint64)
+        n, L = calls.shape
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        _check(lib().tch_solver_from_calls(device, n, L, _ptr(calls), tau, kernel_id(kernel), ctypes.byref(h), err,
+                                           len(err)), err)
         return cls(h)
 
     def info(self) -> dict:

@@ -27,7 +27,7 @@ OBJ = os.path.join(LIB, "obj")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["tch_solver.cu", "k_popc.cu", "k_expand.cu", "k_tc.cu", "encode_host.cpp", "noalloc.cu"]
+CU_SOURCES = ["tch_solver.cu", "k_popc.cu", "k_expand.cu", "k_tc.cu", "k_encode.cu", "encode_host.cpp", "noalloc.cu"]
 LIBNAME = "libtch.so"
 CLI_NAME = "cgmlst-hamming-gpu"
 

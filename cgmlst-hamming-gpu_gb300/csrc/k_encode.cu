@@ -1,0 +1,573 @@
+// Device encoder: allele calls (u64, 0 = missing) -> the tensor-core operand X
+// and the rare-pair CSR, without leaving the GPU except for small tables.
+//
+// It produces what the reference's host computes in main.rs:134-165 (dense
+// per-locus ranks), 366-403 (frequent one-hot columns, presence) and 404-444
+// (rare equal pairs), as device kernels:
+//
+//   1. insert_kernel      per-locus open-addressing hash tables (u64 keys,
+//                         atomicCAS) with a count per distinct id
+//   2. rank_kernel        one CTA per locus: compacts the distinct ids and
+//                         ranks each by counting the smaller ids (the
+//                         reference's sorted-unique rank, 1..k), and writes
+//                         the count of every rank
+//   3. cell_rank_kernel   every cell -> its rank (u16 matrix x, n x L)
+//      (host)             tau from the counts (analytic model), frequent
+//                         column map and per-locus offsets
+//   4. pack_x_kernel      x -> X rows [presence | one-hot] as e4m3 bytes
+//   5. group_fill_kernel  rows of each rare (locus, rank) group of size >= 2
+//      group_sort_kernel  ... sorted ascending inside the group
+//   6. rare_rows_kernel   one CTA per row: u16 counters over the columns
+//                         j > i (shared memory, 64 Ki columns per chunk), one
+//                         increment per shared rare group, then a block scan
+//                         emits the partners in ascending order with their
+//                         multiplicity.  Run twice: counts, then the CSR.
+//
+// The CSR rows come out ascending, so the stripe kernels subtract them in the
+// tile epilogue.  All ids are compared for equality only; any 64-bit values
+// work (hashed ids included).
+
+#include <vector>
+
+#include "tch_internal.cuh"
+
+namespace tch {
+namespace {
+
+constexpr uint32_t kMaxDistinct = 65535;
+constexpr int kJC = 65536;  // columns per counter chunk (u16 counters: 128 KB)
+
+__device__ __forceinline__ uint32_t hash_slot(uint64_t v, int logC) {
+    return (uint32_t)((v * 0x9E3779B97F4A7C15ull) >> (64 - logC));
+}
+
+__global__ void insert_kernel(const uint64_t* __restrict__ calls, int n, int L, int k0, int nk,
+                              unsigned long long* keys, uint32_t* cnts, int logC, uint32_t* nd, int* err) {
+    const size_t C = (size_t)1 << logC, total = (size_t)n * nk;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = t / nk;
+        const int kk = (int)(t % nk);
+        const unsigned long long v = calls[i * L + k0 + kk];
+        if (!v) continue;
+        unsigned long long* kt = keys + kk * C;
+        uint32_t s = hash_slot(v, logC);
+        bool placed = false;
+        for (size_t probe = 0; probe < C; probe++, s = (s + 1) & (uint32_t)(C - 1)) {
+            unsigned long long cur = kt[s];
+            if (cur == 0) cur = atomicCAS(kt + s, 0ull, v);
+            if (cur == 0) {  // new distinct id
+                atomicAdd(nd + k0 + kk, 1u);
+                atomicAdd(cnts + kk * C + s, 1u);
+                placed = true;
+                break;
+            }
+            if (cur == v) {
+                atomicAdd(cnts + kk * C + s, 1u);
+                placed = true;
+                break;
+            }
+        }
+        if (!placed) atomicOr(err, DEVERR_TOO_MANY_ALLELES);
+    }
+}
+
+// One CTA per locus of the batch.  rank = 1 + #(distinct ids smaller than it).
+__global__ void rank_kernel(int k0, const unsigned long long* keys, const uint32_t* cnts, int logC,
+                            const uint32_t* nd, const uint64_t* cnt_off, uint32_t* cnt_flat, uint16_t* rank_slot,
+                            unsigned long long* list_keys, uint32_t* list_slots, int* err) {
+    const int kk = blockIdx.x;
+    const size_t C = (size_t)1 << logC;
+    const unsigned long long* kt = keys + kk * C;
+    unsigned long long* lk = list_keys + (size_t)kk * kMaxDistinct;
+    uint32_t* ls = list_slots + (size_t)kk * kMaxDistinct;
+    __shared__ uint32_t m;
+    __shared__ unsigned long long tile[2048];
+    if (threadIdx.x == 0) m = 0;
+    __syncthreads();
+    for (uint32_t s = threadIdx.x; s < C; s += blockDim.x) {
+        const unsigned long long v = kt[s];
+        if (v) {
+            const uint32_t idx = atomicAdd(&m, 1u);
+            if (idx < kMaxDistinct) {
+                lk[idx] = v;
+                ls[idx] = s;
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t mm = m;
+    if (mm > kMaxDistinct || mm != nd[k0 + kk]) {
+        if (threadIdx.x == 0) atomicOr(err, DEVERR_TOO_MANY_ALLELES);
+        return;
+    }
+    const uint64_t off = cnt_off[k0 + kk];
+    // each thread ranks up to 8 ids per sweep of the id list through shared memory
+    for (uint32_t e0 = 0; e0 < mm; e0 += 8 * blockDim.x) {
+        unsigned long long mine[8];
+        uint32_t r[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const uint32_t e = e0 + q * blockDim.x + threadIdx.x;
+            mine[q] = e < mm ? lk[e] : ~0ull;
+            r[q] = 0;
+        }
+        for (uint32_t f0 = 0; f0 < mm; f0 += 2048) {
+            const uint32_t cntf = min(2048u, mm - f0);
+            __syncthreads();
+            for (uint32_t f = threadIdx.x; f < cntf; f += blockDim.x) tile[f] = lk[f0 + f];
+            __syncthreads();
+            for (uint32_t f = 0; f < cntf; f++) {
+                const unsigned long long w = tile[f];
+#pragma unroll
+                for (int q = 0; q < 8; q++) r[q] += w < mine[q];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const uint32_t e = e0 + q * blockDim.x + threadIdx.x;
+            if (e < mm) {
+                const uint32_t slot = ls[e];
+                rank_slot[kk * C + slot] = (uint16_t)(r[q] + 1);
+                cnt_flat[off + r[q] + 1] = cnts[kk * C + slot];
+            }
+        }
+    }
+}
+
+__global__ void cell_rank_kernel(const uint64_t* __restrict__ calls, int n, int L, int k0, int nk,
+                                 const unsigned long long* keys, const uint16_t* rank_slot, int logC,
+                                 uint16_t* x, int* err) {
+    const size_t C = (size_t)1 << logC, total = (size_t)n * nk;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = t / nk;
+        const int kk = (int)(t % nk);
+        const unsigned long long v = calls[i * L + k0 + kk];
+        uint16_t rk = 0;
+        if (v) {
+            const unsigned long long* kt = keys + kk * C;
+            uint32_t s = hash_slot(v, logC);
+            bool found = false;
+            for (size_t probe = 0; probe < C; probe++, s = (s + 1) & (uint32_t)(C - 1)) {
+                const unsigned long long cur = kt[s];
+                if (cur == v) {
+                    rk = rank_slot[kk * C + s];
+                    found = true;
+                    break;
+                }
+                if (cur == 0) break;
+            }
+            if (!found) atomicOr(err, DEVERR_TOO_MANY_ALLELES);
+        }
+        x[i * L + k0 + kk] = rk;
+    }
+}
+
+__global__ void pack_x_kernel(const uint16_t* __restrict__ x, int n, int L, const uint64_t* __restrict__ cnt_off,
+                              const int32_t* __restrict__ col_flat, const uint32_t* __restrict__ base, uint8_t* X,
+                              int kb, int kp, uint8_t one) {
+    const size_t total = (size_t)n * L;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = t / L;
+        const int k = (int)(t % L);
+        const int a = x[t];
+        if (!a) continue;
+        uint8_t* row = X + i * (size_t)kb;
+        row[k] = one;
+        const int32_t c = col_flat[cnt_off[k] + a];
+        if (c >= 0) row[kp + base[k] + c] = one;
+    }
+}
+
+__global__ void group_fill_kernel(const uint16_t* __restrict__ x, int n, int L, const uint64_t* __restrict__ cnt_off,
+                                  const uint64_t* __restrict__ goff, uint32_t* gfill, uint32_t* members) {
+    const size_t total = (size_t)n * L;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int a = x[t];
+        if (!a) continue;
+        const size_t i = t / L;
+        const int k = (int)(t % L);
+        const uint64_t q = cnt_off[k] + a;
+        const uint64_t g0 = goff[q], g1 = goff[q + 1];
+        if (g1 > g0) members[g0 + atomicAdd(gfill + q, 1u)] = (uint32_t)i;
+    }
+}
+
+// One CTA per rare group: rows are distinct, so a row's place is the number
+// of smaller rows in the group.
+__global__ void group_sort_kernel(const uint64_t* __restrict__ groups, const uint32_t* __restrict__ members,
+                                  uint32_t* sorted) {
+    const uint64_t g0 = groups[2 * blockIdx.x], g1 = groups[2 * blockIdx.x + 1];
+    const uint32_t g = (uint32_t)(g1 - g0);
+    __shared__ uint32_t tile[4096];
+    for (uint32_t e0 = 0; e0 < g; e0 += 4 * blockDim.x) {
+        uint32_t mine[4], r[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t e = e0 + q * blockDim.x + threadIdx.x;
+            mine[q] = e < g ? members[g0 + e] : 0xFFFFFFFFu;
+            r[q] = 0;
+        }
+        for (uint32_t f0 = 0; f0 < g; f0 += 4096) {
+            const uint32_t cntf = min(4096u, g - f0);
+            __syncthreads();
+            for (uint32_t f = threadIdx.x; f < cntf; f += blockDim.x) tile[f] = members[g0 + f0 + f];
+            __syncthreads();
+            for (uint32_t f = 0; f < cntf; f++) {
+                const uint32_t w = tile[f];
+#pragma unroll
+                for (int q = 0; q < 4; q++) r[q] += w < mine[q];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t e = e0 + q * blockDim.x + threadIdx.x;
+            if (e < g) sorted[g0 + r[q]] = mine[q];
+        }
+    }
+}
+
+__device__ __forceinline__ uint64_t lower_bound_rows(const uint32_t* __restrict__ a, uint64_t lo, uint64_t hi,
+                                                     uint32_t key) {
+    while (lo < hi) {
+        const uint64_t mid = lo + (hi - lo) / 2;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+constexpr int RR_THREADS = 512;
+
+// Rare partners of each row, ascending with multiplicity.  emit == 0: writes
+// the row's partner count to row_count[i]; emit == 1: writes the partners to
+// js[start[i] ...].
+__global__ void __launch_bounds__(RR_THREADS)
+rare_rows_kernel(const uint16_t* __restrict__ x, int n, int L, const uint64_t* __restrict__ cnt_off,
+                 const uint64_t* __restrict__ goff, const uint32_t* __restrict__ members, int emit,
+                 uint32_t* row_count, const uint64_t* __restrict__ start, uint32_t* js) {
+    extern __shared__ uint32_t cw[];  // kJC u16 counters as kJC / 2 words
+    __shared__ uint32_t warp_tot[RR_THREADS / 32];
+    __shared__ uint64_t chunk_base;
+    constexpr int PER = kJC / RR_THREADS;  // counters owned by a thread in the scan
+    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        if (threadIdx.x == 0) chunk_base = emit ? start[i] : 0;
+        uint64_t total = 0;
+        for (int c0 = i + 1; c0 < n; c0 += kJC) {
+            const int c1 = min(n, c0 + kJC);
+            for (int w = threadIdx.x; w < kJC / 2; w += RR_THREADS) cw[w] = 0;
+            __syncthreads();
+            for (int k = threadIdx.x; k < L; k += RR_THREADS) {
+                const int a = x[(size_t)i * L + k];
+                if (!a) continue;
+                const uint64_t q = cnt_off[k] + a;
+                const uint64_t g0 = goff[q], g1 = goff[q + 1];
+                if (g1 <= g0) continue;
+                for (uint64_t p = lower_bound_rows(members, g0, g1, (uint32_t)c0); p < g1; p++) {
+                    const uint32_t j = members[p];
+                    if (j >= (uint32_t)c1) break;
+                    const uint32_t o = j - (uint32_t)c0;
+                    atomicAdd(cw + (o >> 1), 1u << (16 * (o & 1)));
+                }
+            }
+            __syncthreads();
+            // exclusive scan of the counters in column order
+            const uint16_t* cc = reinterpret_cast<const uint16_t*>(cw);
+            uint32_t mine = 0;
+            const int b = threadIdx.x * PER;
+            for (int e = 0; e < PER; e++) mine += cc[b + e];
+            uint32_t incl = mine;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += y;
+            }
+            if (lane == 31) warp_tot[warp] = incl;
+            __syncthreads();
+            uint32_t before = 0, all = 0;
+            for (int w = 0; w < RR_THREADS / 32; w++) {
+                if (w < warp) before += warp_tot[w];
+                all += warp_tot[w];
+            }
+            if (emit) {
+                uint64_t pos = chunk_base + before + (incl - mine);
+                for (int e = 0; e < PER; e++) {
+                    const uint32_t c = cc[b + e];
+                    for (uint32_t r = 0; r < c; r++) js[pos++] = (uint32_t)(c0 + b + e);
+                }
+            }
+            total += all;
+            __syncthreads();
+            if (threadIdx.x == 0) chunk_base += all;
+            __syncthreads();
+        }
+        if (!emit && threadIdx.x == 0) row_count[i] = (uint32_t)(total < 0xFFFFFFFFull ? total : 0xFFFFFFFFull);
+        __syncthreads();
+    }
+}
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count, size_t* bytes) {
+    cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess && bytes) *bytes += count * sizeof(T);
+    return e;
+}
+
+int grid_for(size_t total, int sms) { return (int)std::min<size_t>((total + 255) / 256, (size_t)sms * 32); }
+
+}  // namespace
+
+// Analytic cost of tau on GB300: tensor-core time for the one-hot columns plus
+// the fused rare subtraction, subject to device memory.
+int choose_tau_gb300(const std::vector<uint32_t>& cnt_flat, const std::vector<uint64_t>& off, int n, int L,
+                     size_t free_bytes, const TauModel& m, bool verbose) {
+    std::vector<double> cs;
+    for (int k = 0; k < L; k++)
+        for (uint64_t q = off[k] + 1; q < off[k + 1]; q++)
+            if (cnt_flat[q]) cs.push_back((double)cnt_flat[q]);
+    const double pairs = (double)n * (double)(n - 1) / 2.0;
+    const size_t rows = up((size_t)std::max(n, 1), 256), kp = up((size_t)L, 128);
+    int best = 0;
+    double best_t = 1e300;
+    for (int tau = 2; tau <= 4096; tau *= 2) {
+        size_t d = 0;
+        double r = 0;
+        for (double v : cs) {
+            if (v >= tau) d++;
+            else r += v * (v - 1.0) / 2.0;
+        }
+        const double kb = (double)(kp + up(d, 128));
+        const double mem = (double)rows * kb + 4.0 * (r + n + 1.0) + 2.0 * (double)n * (double)up((size_t)n, 8) / 4;
+        const double t = pairs * kb / m.gemm_rate + r / m.rare_rate;
+        const bool fits = mem <= (double)free_bytes && r < 4.0e9;
+        if (verbose)
+            fprintf(stderr, "  tau=%5d  one-hot=%8zu  rare=%14.0f  est %.4fs  vram %.2f GB%s\n", tau, d, r, t,
+                    mem / 1e9, fits ? "" : "  (does not fit)");
+        if (fits && t < best_t) {
+            best = tau;
+            best_t = t;
+        }
+    }
+    return best;
+}
+
+int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_req, const TauModel& model,
+                     bool verbose, DeviceEncoding* out, Err& e) {
+    int sms = 0, hflag = 0;
+    size_t freeb = 0, totb = 0, tmp_bytes = 0;
+    int logC = 10;
+    while (((size_t)1 << logC) < 2 * (size_t)std::min<int>(std::max(n, 1), (int)kMaxDistinct)) logC++;
+    const size_t C = (size_t)1 << logC;
+    // loci per batch: hash tables + id lists within ~2 GB
+    const size_t per_locus = C * (8 + 4 + 2) + (size_t)kMaxDistinct * 12;
+    const int nk_max = (int)std::max<size_t>(1, std::min<size_t>((size_t)L, ((size_t)2 << 30) / per_locus));
+    unsigned long long* keys = nullptr;
+    uint32_t *cnts = nullptr, *nd = nullptr, *list_slots = nullptr, *cnt_flat = nullptr, *gfill = nullptr;
+    uint32_t *members = nullptr, *sorted = nullptr, *row_count = nullptr, *base_d = nullptr;
+    uint16_t* rank_slot = nullptr;
+    unsigned long long* list_keys = nullptr;
+    uint64_t *cnt_off_d = nullptr, *goff_d = nullptr, *groups_d = nullptr, *start64 = nullptr;
+    int32_t* col_d = nullptr;
+    int* err_d = nullptr;
+    std::vector<uint32_t> nd_h(L), cnt_h;
+    std::vector<uint64_t> off_h((size_t)L + 1, 0);
+    *out = DeviceEncoding();
+    out->n = n;
+    out->L = L;
+
+    TCH_CK(e, cudaSetDevice(device));
+    TCH_CK(e, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    TCH_CK(e, dalloc(&err_d, 1, nullptr));
+    TCH_CK(e, cudaMemset(err_d, 0, sizeof(int)));
+    TCH_CK(e, dalloc(&nd, (size_t)L, nullptr));
+    TCH_CK(e, cudaMemset(nd, 0, (size_t)L * 4));
+    TCH_CK(e, dalloc(&out->x, (size_t)n * L, &out->bytes));
+    TCH_CK(e, dalloc(&keys, C * nk_max, &tmp_bytes));
+    TCH_CK(e, dalloc(&cnts, C * nk_max, &tmp_bytes));
+    TCH_CK(e, dalloc(&rank_slot, C * nk_max, &tmp_bytes));
+    TCH_CK(e, dalloc(&list_keys, (size_t)kMaxDistinct * nk_max, &tmp_bytes));
+    TCH_CK(e, dalloc(&list_slots, (size_t)kMaxDistinct * nk_max, &tmp_bytes));
+    TCH_CK(e, dalloc(&cnt_off_d, (size_t)L + 1, nullptr));
+
+    // ---- 1-3: ranks and counts, batch by batch
+    {
+        std::vector<uint32_t> cnt_parts;
+        for (int k0 = 0; k0 < L; k0 += nk_max) {
+            const int nk = std::min(nk_max, L - k0);
+            TCH_CK(e, cudaMemset(keys, 0, C * nk * sizeof(unsigned long long)));
+            TCH_CK(e, cudaMemset(cnts, 0, C * nk * sizeof(uint32_t)));
+            insert_kernel<<<grid_for((size_t)n * nk, sms), 256>>>(d_calls, n, L, k0, nk, keys, cnts, logC, nd, err_d);
+            TCH_CK(e, cudaGetLastError());
+            TCH_CK(e, cudaMemcpy(nd_h.data() + k0, nd + k0, (size_t)nk * 4, cudaMemcpyDeviceToHost));
+            TCH_CK(e, cudaMemcpy(&hflag, err_d, sizeof(int), cudaMemcpyDeviceToHost));
+            if (hflag) { e.set("a locus has more than 65535 distinct alleles (limit 65535)"); goto fail; }
+            for (int kk = 0; kk < nk; kk++) {
+                if (nd_h[k0 + kk] > kMaxDistinct) {
+                    e.set("locus %d has %u distinct alleles (limit 65535)", k0 + kk, nd_h[k0 + kk]);
+                    goto fail;
+                }
+                off_h[k0 + kk + 1] = off_h[k0 + kk] + nd_h[k0 + kk] + 1;
+            }
+        }
+        // flat counts need every offset: a second sweep ranks the batches
+        TCH_CK(e, cudaMemcpy(cnt_off_d, off_h.data(), ((size_t)L + 1) * 8, cudaMemcpyHostToDevice));
+        TCH_CK(e, dalloc(&cnt_flat, off_h[L], &tmp_bytes));
+        TCH_CK(e, cudaMemset(cnt_flat, 0, std::max<uint64_t>(off_h[L], 1) * 4));
+        const bool one_batch = nk_max >= L;  // the first sweep's tables are still in place
+        if (!one_batch) TCH_CK(e, cudaMemset(nd, 0, (size_t)L * 4));
+        for (int k0 = 0; k0 < L; k0 += nk_max) {
+            const int nk = std::min(nk_max, L - k0);
+            if (!one_batch) {
+                TCH_CK(e, cudaMemset(keys, 0, C * nk * sizeof(unsigned long long)));
+                TCH_CK(e, cudaMemset(cnts, 0, C * nk * sizeof(uint32_t)));
+                insert_kernel<<<grid_for((size_t)n * nk, sms), 256>>>(d_calls, n, L, k0, nk, keys, cnts, logC, nd,
+                                                                       err_d);
+                TCH_CK(e, cudaGetLastError());
+            }
+            rank_kernel<<<nk, 512>>>(k0, keys, cnts, logC, nd, cnt_off_d, cnt_flat, rank_slot, list_keys, list_slots,
+                                     err_d);
+            TCH_CK(e, cudaGetLastError());
+            cell_rank_kernel<<<grid_for((size_t)n * nk, sms), 256>>>(d_calls, n, L, k0, nk, keys, rank_slot, logC,
+                                                                      out->x, err_d);
+            TCH_CK(e, cudaGetLastError());
+        }
+        TCH_CK(e, cudaMemcpy(&hflag, err_d, sizeof(int), cudaMemcpyDeviceToHost));
+        if (hflag) { e.set("device encoder: hash table error 0x%x", hflag); goto fail; }
+        cnt_h.resize(off_h[L]);
+        if (off_h[L]) TCH_CK(e, cudaMemcpy(cnt_h.data(), cnt_flat, off_h[L] * 4, cudaMemcpyDeviceToHost));
+    }
+    cudaFree(keys); keys = nullptr;
+    cudaFree(cnts); cnts = nullptr;
+    cudaFree(rank_slot); rank_slot = nullptr;
+    cudaFree(list_keys); list_keys = nullptr;
+    cudaFree(list_slots); list_slots = nullptr;
+
+    // ---- host: tau, frequent columns, rare groups
+    {
+        int tau = tau_req;
+        TCH_CK(e, cudaMemGetInfo(&freeb, &totb));
+        if (tau <= 0) {
+            tau = choose_tau_gb300(cnt_h, off_h, n, L, freeb, model, verbose);
+            if (!tau) { e.set("no tau fits in %.2f GB of free device memory", freeb / 1e9); goto fail; }
+        }
+        out->tau = tau;
+        std::vector<int32_t> col(off_h[L], -1);
+        std::vector<uint32_t> base((size_t)L + 1, 0);
+        std::vector<uint64_t> goff(off_h[L] + 1, 0);
+        std::vector<uint64_t> groups;
+        uint64_t D = 0;
+        for (int k = 0; k < L; k++) {
+            base[k] = (uint32_t)D;
+            uint32_t d = 0;
+            for (uint64_t q = off_h[k]; q < off_h[k + 1]; q++) {
+                const bool is_rank = q > off_h[k];
+                const uint32_t c = cnt_h[q];
+                const bool freq = is_rank && c >= (uint32_t)tau;
+                if (freq) col[q] = (int32_t)d++;
+                const bool rare = is_rank && !freq && c >= 2;
+                goff[q + 1] = goff[q] + (rare ? c : 0);
+                if (rare) {
+                    groups.push_back(goff[q]);
+                    groups.push_back(goff[q + 1]);
+                }
+            }
+            D += d;
+        }
+        base[L] = (uint32_t)D;
+        out->D = D;
+        out->kp = (int)up((size_t)L, 128);
+        out->kb = out->kp + (int)up(D, 128);
+        out->x_rows = up((size_t)std::max(n, 1), 256);
+        const uint64_t n_members = goff[off_h[L]];
+        TCH_CK(e, dalloc(&col_d, off_h[L], nullptr));
+        TCH_CK(e, dalloc(&base_d, (size_t)L + 1, nullptr));
+        TCH_CK(e, dalloc(&goff_d, off_h[L] + 1, nullptr));
+        if (off_h[L]) TCH_CK(e, cudaMemcpy(col_d, col.data(), off_h[L] * 4, cudaMemcpyHostToDevice));
+        TCH_CK(e, cudaMemcpy(base_d, base.data(), ((size_t)L + 1) * 4, cudaMemcpyHostToDevice));
+        TCH_CK(e, cudaMemcpy(goff_d, goff.data(), (off_h[L] + 1) * 8, cudaMemcpyHostToDevice));
+
+        // ---- 4: operand rows
+        TCH_CK(e, dalloc(&out->X, out->x_rows * (size_t)out->kb, &out->bytes));
+        TCH_CK(e, cudaMemset(out->X, 0, out->x_rows * (size_t)out->kb));
+        pack_x_kernel<<<grid_for((size_t)n * L, sms), 256>>>(out->x, n, L, cnt_off_d, col_d, base_d, out->X, out->kb,
+                                                             out->kp, 0x38);
+        TCH_CK(e, cudaGetLastError());
+
+        // ---- 5: rare groups, sorted
+        const size_t ngroups = groups.size() / 2;
+        TCH_CK(e, dalloc(&members, n_members, &tmp_bytes));
+        TCH_CK(e, dalloc(&sorted, n_members, &tmp_bytes));
+        TCH_CK(e, dalloc(&gfill, off_h[L], &tmp_bytes));
+        TCH_CK(e, cudaMemset(gfill, 0, std::max<uint64_t>(off_h[L], 1) * 4));
+        if (ngroups) {
+            TCH_CK(e, dalloc(&groups_d, groups.size(), &tmp_bytes));
+            TCH_CK(e, cudaMemcpy(groups_d, groups.data(), groups.size() * 8, cudaMemcpyHostToDevice));
+            group_fill_kernel<<<grid_for((size_t)n * L, sms), 256>>>(out->x, n, L, cnt_off_d, goff_d, gfill, members);
+            TCH_CK(e, cudaGetLastError());
+            for (size_t g0 = 0; g0 < ngroups; g0 += 65535) {
+                const unsigned gcount = (unsigned)std::min<size_t>(65535, ngroups - g0);
+                group_sort_kernel<<<gcount, 256>>>(groups_d + 2 * g0, members, sorted);
+                TCH_CK(e, cudaGetLastError());
+            }
+        }
+
+        // ---- 6: CSR of rare pairs, ascending per row
+        TCH_CK(e, dalloc(&row_count, (size_t)n, &tmp_bytes));
+        TCH_CK(e, dalloc(&start64, (size_t)n + 1, &tmp_bytes));
+        const int rr_smem = kJC * 2;
+        TCH_CK(e, cudaFuncSetAttribute(rare_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rr_smem));
+        const int rr_grid = std::max(1, std::min(n, sms * 1));
+        if (ngroups && n > 1) {
+            rare_rows_kernel<<<rr_grid, RR_THREADS, rr_smem>>>(out->x, n, L, cnt_off_d, goff_d, sorted, 0, row_count,
+                                                              nullptr, nullptr);
+            TCH_CK(e, cudaGetLastError());
+        } else {
+            TCH_CK(e, cudaMemset(row_count, 0, (size_t)std::max(n, 1) * 4));
+        }
+        std::vector<uint32_t> rc_h((size_t)n);
+        if (n) TCH_CK(e, cudaMemcpy(rc_h.data(), row_count, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        std::vector<uint32_t> start_h((size_t)n + 1);
+        std::vector<uint64_t> start64_h((size_t)n + 1);
+        uint64_t acc = 0;
+        for (int i = 0; i < n; i++) {
+            start_h[i] = (uint32_t)acc;
+            start64_h[i] = acc;
+            acc += rc_h[i];
+            if (acc >= (1ull << 32)) { e.set("too many rare pairs: raise --tau"); goto fail; }
+        }
+        start_h[n] = (uint32_t)acc;
+        start64_h[n] = acc;
+        out->n_rare = acc;
+        TCH_CK(e, dalloc(&out->start, (size_t)n + 1, &out->bytes));
+        TCH_CK(e, dalloc(&out->js, acc, &out->bytes));
+        TCH_CK(e, cudaMemcpy(out->start, start_h.data(), ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
+        TCH_CK(e, cudaMemcpy(start64, start64_h.data(), ((size_t)n + 1) * 8, cudaMemcpyHostToDevice));
+        if (acc) {
+            rare_rows_kernel<<<rr_grid, RR_THREADS, rr_smem>>>(out->x, n, L, cnt_off_d, goff_d, sorted, 1, nullptr,
+                                                              start64, out->js);
+            TCH_CK(e, cudaGetLastError());
+        }
+        TCH_CK(e, cudaDeviceSynchronize());
+    }
+    cudaFree(err_d); cudaFree(nd); cudaFree(cnt_off_d); cudaFree(cnt_flat); cudaFree(col_d); cudaFree(base_d);
+    cudaFree(goff_d); cudaFree(members); cudaFree(sorted); cudaFree(gfill); cudaFree(groups_d); cudaFree(row_count);
+    cudaFree(start64);
+    return 0;
+fail:
+    cudaFree(err_d); cudaFree(nd); cudaFree(cnt_off_d); cudaFree(cnt_flat); cudaFree(col_d); cudaFree(base_d);
+    cudaFree(goff_d); cudaFree(members); cudaFree(sorted); cudaFree(gfill); cudaFree(groups_d); cudaFree(row_count);
+    cudaFree(start64); cudaFree(keys); cudaFree(cnts); cudaFree(rank_slot); cudaFree(list_keys); cudaFree(list_slots);
+    free_device_encoding(out);
+    return 1;
+}
+
+void free_device_encoding(DeviceEncoding* d) {
+    cudaFree(d->x);
+    cudaFree(d->X);
+    cudaFree(d->start);
+    cudaFree(d->js);
+    d->x = nullptr;
+    d->X = nullptr;
+    d->start = d->js = nullptr;
+}
+
+}  // namespace tch

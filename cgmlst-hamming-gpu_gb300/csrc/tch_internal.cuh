@@ -36,6 +36,7 @@ enum DevErr : int {
     DEVERR_RARE_PAIR = 1,  // a rare partner j outside (i, n)
     DEVERR_OVERFLOW = 2,   // a distance outside [0, 65535]
     DEVERR_TIMEOUT = 4,    // a bounded wait gave up
+    DEVERR_TOO_MANY_ALLELES = 8,  // a locus has more distinct ids than the encoder's table holds
 };
 
 // Rare-pair CSR on the device.
@@ -90,5 +91,30 @@ cudaError_t launch_expand_bits(const BitOperands& bits, int n, size_t n_rows, ui
 bool tc_kernel_compiled(int kernel);
 cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t* Xneg, const RareCSR& rare,
                              const StripeArgs& a, int num_sms, cudaStream_t st);
+
+// ---- k_encode.cu ------------------------------------------------------------------
+// Rates of the analytic tau model on this GPU.
+struct TauModel {
+    double gemm_rate = 1.6e15;  // pair x one-byte-column MACs per second of the stripe kernel
+    double rare_rate = 2.0e10;  // rare pairs per second of the fused subtraction
+};
+
+// Operands built on the device from allele calls; device memory owned here.
+struct DeviceEncoding {
+    int n = 0, L = 0, tau = 0;
+    size_t D = 0;             // frequent one-hot columns
+    uint16_t* x = nullptr;    // n x L ranks
+    uint8_t* X = nullptr;     // x_rows x kb e4m3 operand rows
+    size_t x_rows = 0;
+    int kb = 0, kp = 0;
+    uint32_t* start = nullptr;  // n + 1
+    uint32_t* js = nullptr;     // n_rare, ascending per row
+    size_t n_rare = 0;
+    size_t bytes = 0;
+};
+
+int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_req, const TauModel& model,
+                     bool verbose, DeviceEncoding* out, Err& e);
+void free_device_encoding(DeviceEncoding* d);
 
 }  // namespace tch

@@ -253,6 +253,67 @@ fail:
     return 1;
 }
 
+static TauModel g_tau_model;
+
+// Operands on the device straight from allele calls (host buffer, n x L u64,
+// 0 = missing): the device encoder of k_encode.cu, then the tensor-core kernel.
+static int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, bool verbose,
+                             tch_solver** out, Err& e) {
+    tch_solver* s = nullptr;
+    uint64_t* d_calls = nullptr;
+    DeviceEncoding enc;
+    *out = nullptr;
+    if (n < 0 || L < 0) return e.set("negative size (n=%d, L=%d)", n, L);
+    if (L > 65535) return e.set("more than 65535 loci (u16 distances)");
+    if ((size_t)n * L && !calls) return e.set("null input buffer");
+    kernel = resolve_kernel(kernel);
+    if (kernel != TCH_KERNEL_TC_F8 || !kernel_compiled(kernel))
+        return e.set("the device encoder feeds the tensor-core kernel (tc_f8); kernel %s is not supported here",
+                     tch_kernel_name(kernel));
+    const int Le = std::max(L, 1);  // no loci: one all-zero column keeps every shape valid
+    s = new tch_solver();
+    s->device = device;
+    s->n = n;
+    s->L = L;
+    s->kernel = kernel;
+    TCH_CK(e, cudaSetDevice(device));
+    TCH_CK(e, cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, device));
+    TCH_CK(e, dmalloc(s, (void**)&s->dErr, sizeof(int)));
+    TCH_CK(e, cudaMemset(s->dErr, 0, sizeof(int)));
+    TCH_CK(e, cudaMalloc(&d_calls, std::max<size_t>((size_t)n * Le, 1) * 8));
+    if (L) {
+        if ((size_t)n * L) TCH_CK(e, cudaMemcpy(d_calls, calls, (size_t)n * L * 8, cudaMemcpyHostToDevice));
+    } else {
+        TCH_CK(e, cudaMemset(d_calls, 0, std::max<size_t>((size_t)n, 1) * 8));
+    }
+    if (encode_on_device(device, n, Le, d_calls, tau, g_tau_model, verbose, &enc, e)) goto fail;
+    cudaFree(d_calls);
+    d_calls = nullptr;
+    cudaFree(enc.x);
+    enc.bytes -= (size_t)n * Le * 2;
+    enc.x = nullptr;
+    s->dX = enc.X;
+    s->x_rows = enc.x_rows;
+    s->kb = enc.kb;
+    s->kp = enc.kp;
+    s->n_pad = enc.x_rows;
+    s->K2 = (size_t)enc.kp;
+    s->K1 = (size_t)(enc.kb - enc.kp);
+    s->D = enc.D;
+    s->tau = enc.tau;
+    s->dStart = enc.start;
+    s->dJs = enc.js;
+    s->n_rare = enc.n_rare;
+    s->sorted = true;
+    s->bytes += enc.bytes;
+    *out = s;
+    return 0;
+fail:
+    if (d_calls) cudaFree(d_calls);
+    solver_free(s);
+    return 1;
+}
+
 static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e) {
     if (r0 < 0 || rows < 0 || r0 > s->n) return e.set("stripe out of range (r0=%d rows=%d n=%d)", r0, rows, s->n);
     if (r0 + rows > s->n) rows = s->n - r0;
@@ -431,6 +492,33 @@ int tch_solver_from_bits(int device, int n, size_t n_pad, const uint8_t* O, size
     Err e{err, errlen};
     if (!out) return e.set("null output handle");
     return solver_from_bits(device, n, n_pad, O, K1, P, K2, start, js, n_rare, kernel, 0, false, out, e);
+}
+
+int tch_solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, tch_solver** out,
+                          char* err, int errlen) {
+    Err e{err, errlen};
+    if (!out) return e.set("null output handle");
+    return solver_from_calls(device, n, L, calls, tau, kernel, false, out, e);
+}
+
+int tch_run_calls(int device, int n, int L, const uint64_t* calls, int tau, int S, tch_cb cb, void* ctx,
+                  double* gpu_secs, int* tau_used, char* err, int errlen) {
+    Err e{err, errlen};
+    tch_solver* s = nullptr;
+    if (S <= 0) return e.set("stripe rows must be positive (got %d)", S);
+    const char* v = getenv("TCH_VERBOSE");
+    if (solver_from_calls(device, n, L, calls, tau, TCH_KERNEL_AUTO, v && v[0] == '1', &s, e)) return 1;
+    if (tau_used) *tau_used = s->tau;
+    const int rc = n > 0 ? solver_run(s, S, cb, ctx, gpu_secs, e) : 0;
+    solver_free(s);
+    return rc;
+}
+
+int tch_set_tau_model(double gemm_rate, double rare_rate) {
+    if (!(gemm_rate > 0) || !(rare_rate > 0)) return 1;
+    g_tau_model.gemm_rate = gemm_rate;
+    g_tau_model.rare_rate = rare_rate;
+    return 0;
 }
 
 int tch_solver_info(const tch_solver* s, tch_info* info) {

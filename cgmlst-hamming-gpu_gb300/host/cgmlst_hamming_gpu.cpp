@@ -81,6 +81,7 @@ struct Args {
     size_t stripe = 512;
     size_t device = 0;
     bool silent = false;
+    bool host_encode = false;
 };
 
 const char* kUsage =
@@ -106,6 +107,7 @@ const char* kUsage =
     "      --stripe <STRIPE>                    Rows per GPU stripe [default: 512]\n"
     "      --device <DEVICE>                    CUDA device [default: 0]\n"
     "  -s, --silent                             Suppress progress/log messages on stderr\n"
+    "      --host-encode                        Encode on the host and call tch_run (the reference's path)\n"
     "  -h, --help                               Print help\n"
     "  -V, --version                            Print version\n";
 
@@ -150,6 +152,7 @@ Args parse_args(int argc, char** argv) {
                                {"z", "gzip", false},         {"X", "max-dist", true},
                                {nullptr, "tau", true},       {nullptr, "stripe", true},
                                {nullptr, "device", true},    {"s", "silent", false},
+                               {nullptr, "host-encode", false},
                                {"h", "help", false},         {"V", "version", false}};
     for (int k = 1; k < argc; k++) {
         std::string arg = argv[k];
@@ -235,6 +238,8 @@ Args parse_args(int argc, char** argv) {
             a.device = parse_num<size_t>(flag, val, false, false);
         } else if (name == "silent") {
             a.silent = true;
+        } else if (name == "host-encode") {
+            a.host_encode = true;
         }
     }
     if (!have_input) usage_error("the following required arguments were not provided:\n  --input <INPUT>");
@@ -568,16 +573,38 @@ int main(int argc, char** argv) {
     }
     if (L > 65535) die("more than 65535 loci (u16 distances)");
 
-    // ---- encode (main.rs:353-445)
+    // ---- encode (main.rs:353-445) and GPU (main.rs:447-465)
     t = now();
     char err[512] = {0};
-    std::vector<uint16_t> x(n * L);
-    std::vector<uint32_t> nd(L);
-    if (tch_dense_ranks(calls.data(), (int)n, (int)L, x.data(), nd.data(), (int)threads, err, sizeof err)) die(err);
-    std::vector<uint64_t>().swap(calls);
     std::vector<std::vector<uint16_t>> upper(n);
     double gpu_secs = 0;
-    if (n >= 2 && L > 0) {
+    if (n >= 2 && L > 0 && !args.host_encode) {
+        // device encoder: ranks, one-hot, presence and rare pairs on the GPU
+        const size_t stripe = std::max<size_t>(args.stripe, 8) / 8 * 8;
+        if (!args.silent) setenv("TCH_VERBOSE", "1", 1);
+        tch_solver* solver = nullptr;
+        if (tch_solver_from_calls((int)args.device, (int)n, (int)L, calls.data(), (int)args.tau, TCH_KERNEL_AUTO,
+                                  &solver, err, sizeof err))
+            die(err);
+        std::vector<uint64_t>().swap(calls);
+        tch_info info;
+        tch_solver_info(solver, &info);
+        log(fmt("Encoded in %.2fs: tau=%d, one-hot cols=%zu, rare equal pairs=%zu", now() - t, info.tau,
+                info.d_onehot, info.n_rare));
+        t = now();
+        Sink sink{&upper, threads};
+        const int rc = tch_solver_run(solver, (int)stripe, on_stripe, &sink, &gpu_secs, err, sizeof err);
+        tch_solver_destroy(solver);
+        if (rc) die(fmt("CUDA: %s", err));
+        log(fmt("Computed %zu x %zu matrix on tensor cores in %.2fs (GPU pipeline %.2fs, rare pairs on GPU)", n, n,
+                now() - t, gpu_secs));
+    } else if (n >= 2 && L > 0) {
+        // the reference's path: host encoder + tch_run
+        std::vector<uint16_t> x(n * L);
+        std::vector<uint32_t> nd(L);
+        if (tch_dense_ranks(calls.data(), (int)n, (int)L, x.data(), nd.data(), (int)threads, err, sizeof err))
+            die(err);
+        std::vector<uint64_t>().swap(calls);
         const size_t stripe = std::max<size_t>(args.stripe, 8) / 8 * 8;
         int tau = (int)args.tau;
         if (tau <= 0 &&
@@ -588,7 +615,6 @@ int main(int argc, char** argv) {
         if (tch_encode_host(x.data(), nd.data(), (int)n, (int)L, tau, (int)threads, &enc, err, sizeof err)) die(err);
         log(fmt("Encoded in %.2fs: tau=%d, one-hot cols=%zu, rare equal pairs=%zu", now() - t, tau, enc.D,
                 enc.n_rare));
-        // ---- GPU (main.rs:447-465)
         t = now();
         Sink sink{&upper, threads};
         int rare_gpu = 0;
@@ -599,6 +625,12 @@ int main(int argc, char** argv) {
         log(fmt("Computed %zu x %zu matrix on tensor cores in %.2fs (GPU pipeline %.2fs, rare pairs on %s)", n, n,
                 now() - t, gpu_secs, rare_gpu ? "GPU" : "host"));
     } else {
+        // n < 2 or no loci: every distance is 0 and the GPU is not used (main.rs:466-470);
+        // the reference still ranks the calls, which enforces its 65535-allele limit
+        std::vector<uint16_t> x(n * L);
+        std::vector<uint32_t> nd(L);
+        if (tch_dense_ranks(calls.data(), (int)n, (int)L, x.data(), nd.data(), (int)threads, err, sizeof err))
+            die(err);
         for (size_t i = 0; i < n; i++) upper[i].assign(n - 1 - i, 0);
     }
 

@@ -120,6 +120,26 @@ int tch_solver_from_bits(int device, int n, size_t n_pad, const uint8_t* O, size
                          size_t K2, const uint32_t* start, const uint32_t* js, size_t n_rare, int kernel,
                          tch_solver** out, char* err, int errlen);
 
+/* Build a solver straight from allele calls (host buffer, n x L u64 row-major,
+ * 0 = missing; any other value is an allele id compared for equality only).
+ * The encoding the reference's host does (main.rs:134-165, 366-444: dense
+ * ranks, frequent one-hot columns, presence, rare equal pairs) runs on the
+ * device.  tau <= 0 picks tau with the analytic GB300 cost model.  Fails like
+ * the reference when a locus has more than 65535 distinct ids, L > 65535, or
+ * the rare pairs reach 2^32. */
+int tch_solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, tch_solver** out,
+                          char* err, int errlen);
+
+/* tch_run's stripe/callback contract on allele calls: device encoding, then
+ * the whole upper triangle through the callback.  *tau_used (may be NULL)
+ * receives the tau that was used.  TCH_VERBOSE=1 prints the tau table. */
+int tch_run_calls(int device, int n, int L, const uint64_t* calls, int tau, int S, tch_cb cb, void* ctx,
+                  double* gpu_secs, int* tau_used, char* err, int errlen);
+
+/* Rates of the analytic tau model (pair x column MACs per second of the
+ * stripe kernel, rare pairs per second); defaults are GB300 measurements. */
+int tch_set_tau_model(double gemm_rate, double rare_rate);
+
 /* Fill *info. */
 int tch_solver_info(const tch_solver* s, tch_info* info);
 

@@ -73,11 +73,14 @@ def case_files(tmp_path_factory, golden):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("encoder", ["device", "host"])
 @pytest.mark.parametrize("case_idx", [0, 1, 2])
 @pytest.mark.parametrize("flags_idx", range(len(refgen.CHECKPY_FLAGSETS)))
-def test_checkpy_matrix(pkg, case_files, case_idx, flags_idx):
+def test_checkpy_matrix(pkg, case_files, encoder, case_idx, flags_idx):
     c, path, A = case_files[case_idx]
     args, kind = refgen.CHECKPY_FLAGSETS[flags_idx]
+    if encoder == "host":
+        args = args + ["--host-encode"]
     r = run(pkg, ["-s", "-i", path, *args])
     assert r.returncode == 0, r.stderr
     got = parse(r.stdout, "," if "-D" in args else "\t")
@@ -123,8 +126,10 @@ def test_options_and_streams(pkg, tmp_path, case_files):
     assert run(pkg, ["-s", "-i", path, "-o", str(z), "-z"]).returncode == 0
     assert gzip.decompress(z.read_bytes()).decode() == want
     # logging on stderr without -s
-    r = run(pkg, ["-i", path, "--tau", "4"])
-    assert r.returncode == 0 and "Loaded 300 samples x 97 loci" in r.stderr and "tau=4" in r.stderr
+    for extra in ([], ["--host-encode"]):
+        r = run(pkg, ["-i", path, "--tau", "4", *extra])
+        assert r.returncode == 0 and "Loaded 300 samples x 97 loci" in r.stderr and "tau=4" in r.stderr
+        assert r.stdout == want
 
 
 @pytest.mark.gpu
