@@ -59,34 +59,43 @@ enum Kind { KIND_F8 = 0, KIND_I8 = 1 };
 using namespace ptx;
 
 // ---------------------------------------------------------------- tile order
+// A cluster of CM CTAs works on CM vertically adjacent 128-row blocks (a
+// "super-row" sr of CM * 128 rows) against one 256-column block bj; CTA rank r
+// owns row block bi = sr * CM + r.  With CM = 2 the two CTAs share the B tile:
+// each loads one 128-row half and multicasts it to both.
 struct TileSpace {
-    int nbi, nbj;  // row blocks of the stripe, column blocks of [r0, n)
+    int nsr, nbj;  // super-rows of the stripe, column blocks of [r0, n)
+    int cm;        // row blocks per super-row (cluster size)
 };
 
-// Tiles of row block bi: columns bj >= bi / 2 (128-row blocks against 256-wide
+// Columns of super-row sr: bj >= sr * cm / 2 (128-row blocks against 256-wide
 // column blocks that both start at r0; earlier columns lie below the diagonal).
-__device__ __forceinline__ int cols_in_row(const TileSpace& ts, int bi) {
-    const int c = ts.nbj - bi / 2;
-    return c > 0 ? c : 0;
+__host__ __device__ __forceinline__ int first_col(const TileSpace& ts, int sr) { return sr * ts.cm / 2; }
+
+__host__ __device__ __forceinline__ long long count_tiles(const TileSpace& ts) {
+    long long c = 0;
+    for (int sr = 0; sr < ts.nsr; sr++) c += ts.nbj > first_col(ts, sr) ? ts.nbj - first_col(ts, sr) : 0;
+    return c;
 }
 
-// t -> (bi, bj): groups of GROUP_M row blocks, column-major inside a group.
-__device__ bool tile_coords(const TileSpace& ts, int t, int* bi_out, int* bj_out) {
-    for (int g0 = 0; g0 < ts.nbi; g0 += GROUP_M) {
-        const int g1 = min(ts.nbi, g0 + GROUP_M);
+// t -> (sr, bj): groups of GROUP_M row blocks, column-major inside a group.
+__device__ bool tile_coords(const TileSpace& ts, int t, int* sr_out, int* bj_out) {
+    const int gs = GROUP_M / ts.cm;  // super-rows per group
+    for (int g0 = 0; g0 < ts.nsr; g0 += gs) {
+        const int g1 = min(ts.nsr, g0 + gs);
         int cnt = 0;
-        for (int bi = g0; bi < g1; bi++) cnt += cols_in_row(ts, bi);
+        for (int sr = g0; sr < g1; sr++) cnt += max(0, ts.nbj - first_col(ts, sr));
         if (t >= cnt) {
             t -= cnt;
             continue;
         }
-        for (int bj = g0 / 2; bj < ts.nbj; bj++) {
-            // rows of the group present in column bj: bi <= 2 bj + 1
-            const int last = min(g1 - 1, 2 * bj + 1);
+        for (int bj = first_col(ts, g0); bj < ts.nbj; bj++) {
+            // super-rows of the group present in column bj: sr * cm <= 2 bj + 1
+            const int last = min(g1 - 1, (2 * bj + 1) / ts.cm);
             const int rows = last - g0 + 1;
             if (rows <= 0) continue;
             if (t < rows) {
-                *bi_out = g0 + t;
+                *sr_out = g0 + t;
                 *bj_out = bj;
                 return true;
             }
@@ -119,10 +128,15 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__
     return lo;
 }
 
-template <int KIND>
+template <int KIND, int CM>
 __global__ void __launch_bounds__(THREADS, 1)
 tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                  const TcParams p) {
+    static_assert(CM == 1 || CM == 2, "cluster of 1 or 2 CTAs");
+    constexpr int B_PART = B_BYTES / CM;  // bytes of the B tile this CTA loads per stage
+    const uint32_t rank = CM == 1 ? 0u : cluster_ctarank();
+    const int cid = CM == 1 ? (int)blockIdx.x : (int)cluster_id_x();
+    const int ncl = CM == 1 ? (int)gridDim.x : (int)num_clusters_x();
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-byte alignment of the swizzled stage buffers
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -143,7 +157,7 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1);
+            mbar_init(&empty[s], CM);  // released by the MMA warp of every CTA that reads the stage
         }
         for (int a = 0; a < 2; a++) {
             mbar_init(&tfull[a], 1);
@@ -163,6 +177,7 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
     }
     tc_fence_before();
     __syncthreads();
+    if (CM > 1) cluster_sync();  // the peer's barriers exist before any multicast reaches them
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
 
@@ -175,15 +190,20 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
             int issued[STAGES];
             uint32_t issued_ph[STAGES];
             for (int q = 0; q < STAGES; q++) issued[q] = 0, issued_ph[q] = 0;
-            for (int t = blockIdx.x; ok && t < p.num_tiles; t += gridDim.x) {
-                int bi, bj;
-                if (!tile_coords(p.ts, t, &bi, &bj)) break;
-                const int y_a = p.r0 + bi * BM, y_b = p.r0 + bj * BN;
+            for (int t = cid; ok && t < p.num_tiles; t += ncl) {
+                int sr, bj;
+                if (!tile_coords(p.ts, t, &sr, &bj)) break;
+                const int bi = sr * CM + (int)rank;
+                const int y_a = p.r0 + bi * BM, y_b = p.r0 + bj * BN + (int)rank * (BN / CM);
                 for (int kb = 0; kb < p.kblocks; kb++) {
                     if (!mbar_wait(&empty[s], ph ^ 1, abort_flag, p.err)) { ok = false; break; }
-                    mbar_expect_tx(&full[s], STAGE_BYTES);
+                    mbar_expect_tx(&full[s], STAGE_BYTES);  // A + both halves of B land here
                     tma_load_2d(&map_a, &full[s], stage_a + s * A_BYTES, kb * BK, y_a);
-                    tma_load_2d(&map_b, &full[s], stage_b + s * B_BYTES, kb * BK, y_b);
+                    if (CM == 1)
+                        tma_load_2d(&map_b, &full[s], stage_b + s * B_BYTES, kb * BK, y_b);
+                    else
+                        tma_load_2d_multicast(&map_b, &full[s], stage_b + s * B_BYTES + rank * B_PART, kb * BK, y_b,
+                                              (uint16_t)((1u << CM) - 1));
                     issued[s] = 1;
                     issued_ph[s] = ph;
                     if (++s == STAGES) s = 0, ph ^= 1;
@@ -213,7 +233,7 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
             int s = 0, acc = 0;
             uint32_t ph = 0, aph = 0;
             bool ok = true;
-            for (int t = blockIdx.x; ok && t < p.num_tiles; t += gridDim.x) {
+            for (int t = cid; ok && t < p.num_tiles; t += ncl) {
                 if (!mbar_wait(&tempty[acc], aph ^ 1, abort_flag, p.err)) { ok = false; break; }
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + (uint32_t)(acc * BN);
@@ -226,7 +246,9 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
                     for (int k = 0; k < BK / 32; k++)
                         tc_mma_f8(d_tmem, sw128_desc(a0 + 32 * k), sw128_desc(b0 + 32 * k), idesc,
                                      (kb | k) ? 1u : 0u);
-                    tc_commit(&empty[s]);  // stage free once these MMAs have read it
+                    // stage free once these MMAs have read it (in every CTA whose B half it holds)
+                    if (CM == 1) tc_commit(&empty[s]);
+                    else tc_commit_multicast(&empty[s], (uint16_t)((1u << CM) - 1));
                     if (++s == STAGES) s = 0, ph ^= 1;
                 }
                 if (!ok) break;
@@ -247,9 +269,10 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
         int acc = 0;
         uint32_t aph = 0;
         int bad = 0;
-        for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x) {
-            int bi, bj;
-            if (!tile_coords(p.ts, t, &bi, &bj)) break;
+        for (int t = cid; t < p.num_tiles; t += ncl) {
+            int sr, bj;
+            if (!tile_coords(p.ts, t, &sr, &bj)) break;
+            const int bi = sr * CM + (int)rank;
             const int i0 = p.r0 + bi * BM, j0 = p.r0 + bj * BN;
             const int my_i = i0 + q * 32 + lane;
             // this row's rare partners inside the tile: an ascending run of js
@@ -318,6 +341,8 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
 
     tc_fence_before();
     __syncthreads();
+    // no CTA leaves while its peer may still multicast into it or arrive on its barriers
+    if (CM > 1) cluster_sync();
     if (warp == 1) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
@@ -351,20 +376,40 @@ bool make_map(CUtensorMap* m, const uint8_t* X, size_t rows, int kb, int box_row
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int KIND>
+template <int KIND, int CM>
 cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCSR& rare, const StripeArgs& a,
                         int num_sms, cudaStream_t st) {
     static bool attr = false;
+    static int max_clusters = 0;
+    auto kern = tc_stripe_kernel<KIND, CM>;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute lattr[1];
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = SMEM_BYTES;
+    cfg.stream = st;
+    if (CM > 1) {
+        lattr[0].id = cudaLaunchAttributeClusterDimension;
+        lattr[0].val.clusterDim.x = CM;
+        lattr[0].val.clusterDim.y = 1;
+        lattr[0].val.clusterDim.z = 1;
+        cfg.attrs = lattr;
+        cfg.numAttrs = 1;
+    }
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(tc_stripe_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             SMEM_BYTES);
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         if (e != cudaSuccess) return e;
+        if (CM > 1) {
+            cfg.gridDim = dim3(CM * std::max(num_sms / CM, 1));
+            e = cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg);
+            if (e != cudaSuccess) return e;
+            if (max_clusters < 1) return cudaErrorInvalidConfiguration;
+        }
         attr = true;
     }
     if ((ops.kb % BK) || (ops.kp % BK) || ops.kb <= 0) return cudaErrorInvalidValue;
     if ((a.ldo & 1) || ((uintptr_t)a.out & 3)) return cudaErrorInvalidValue;
     CUtensorMap ma, mb;
-    if (!make_map(&ma, ops.X, ops.n_rows, ops.kb, BM) || !make_map(&mb, xb, ops.n_rows, ops.kb, BN))
+    if (!make_map(&ma, ops.X, ops.n_rows, ops.kb, BM) || !make_map(&mb, xb, ops.n_rows, ops.kb, BN / CM))
         return cudaErrorInvalidValue;
     TcParams p;
     p.n = a.n;
@@ -372,11 +417,10 @@ cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCS
     p.rows = a.rows;
     p.kblocks = ops.kb / BK;
     p.kblocks_p = ops.kp / BK;
-    p.ts.nbi = (a.rows + BM - 1) / BM;
+    p.ts.cm = CM;
+    p.ts.nsr = ((a.rows + BM - 1) / BM + CM - 1) / CM;
     p.ts.nbj = (a.n - a.r0 + BN - 1) / BN;
-    long long tiles = 0;
-    for (int bi = 0; bi < p.ts.nbi; bi++) tiles += std::max(0, p.ts.nbj - bi / 2);
-    p.num_tiles = (int)tiles;
+    p.num_tiles = (int)count_tiles(p.ts);
     p.start = rare.start;
     p.js = rare.js;
     p.fuse_rare = (rare.n_rare > 0 && rare.sorted) ? 1 : 0;
@@ -384,12 +428,23 @@ cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCS
     p.ldo = a.ldo;
     p.err = a.err;
     if (p.num_tiles == 0) return cudaSuccess;
-    const int grid = std::min(p.num_tiles, std::max(num_sms, 1));
-    tc_stripe_kernel<KIND><<<grid, THREADS, SMEM_BYTES, st>>>(ma, mb, p);
-    cudaError_t e = cudaGetLastError();
+    const int clusters = std::min(p.num_tiles, CM > 1 ? max_clusters : std::max(num_sms, 1));
+    cfg.gridDim = dim3(CM * clusters);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, ma, mb, p);
     if (e != cudaSuccess) return e;
     if (rare.n_rare > 0 && !rare.sorted) return launch_rare_atomic(rare, a, st);
     return cudaSuccess;
+}
+
+// Cluster size of the stripe kernel: 2 (B tile shared by multicast) unless
+// TCH_TC_CLUSTER=1 asks for single CTAs.
+int cluster_size() {
+    static int cm = 0;
+    if (!cm) {
+        const char* v = getenv("TCH_TC_CLUSTER");
+        cm = (v && v[0] == '1') ? 1 : 2;
+    }
+    return cm;
 }
 
 }  // namespace
@@ -402,7 +457,9 @@ cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t*
                              const StripeArgs& a, int num_sms, cudaStream_t st) {
     (void)Xneg;
     if (a.rows <= 0 || a.r0 >= a.n) return cudaSuccess;
-    if (kernel == TCH_KERNEL_TC_F8) return launch_kind<KIND_F8>(ops, ops.X, rare, a, num_sms, st);
+    if (kernel == TCH_KERNEL_TC_F8)
+        return cluster_size() == 2 ? launch_kind<KIND_F8, 2>(ops, ops.X, rare, a, num_sms, st)
+                                   : launch_kind<KIND_F8, 1>(ops, ops.X, rare, a, num_sms, st);
     return cudaErrorNotSupported;
 }
 
