@@ -46,12 +46,13 @@ constexpr int STAGES = 4;
 constexpr int A_BYTES = BM * BK;   // 16 KB
 constexpr int B_BYTES = BN * BK;   // 32 KB
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int EPI_WARPS = 4;
+constexpr int EPI_WARPS = 8;      // two per TMEM lane quarter, one per column half
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int EPI_PITCH = 34;      // u16 per staged row: 32 + 2 keeps row writes conflict-free
 constexpr int EPI_BYTES = EPI_WARPS * 32 * EPI_PITCH * 2;
 constexpr int TMEM_COLS = 2 * BN;  // two accumulators
 constexpr int GROUP_M = 8;         // row blocks per raster group
+constexpr int RBUF = 16;           // rare partners fetched per batch in the epilogue
 constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + EPI_BYTES + 256;
 
 enum Kind { KIND_F8 = 0, KIND_I8 = 1 };
@@ -78,22 +79,39 @@ __host__ __device__ __forceinline__ long long count_tiles(const TileSpace& ts) {
     return c;
 }
 
-// t -> (sr, bj): groups of GROUP_M row blocks, column-major inside a group.
-__device__ bool tile_coords(const TileSpace& ts, int t, int* sr_out, int* bj_out) {
+constexpr int MAX_GROUPS = 1024;   // raster groups with a precomputed first tile
+
+// First tile index of every raster group (groups of GROUP_M row blocks,
+// column-major inside a group), so a tile's coordinates cost a binary search
+// over groups plus a few steps instead of a walk over the whole stripe.
+struct GroupTable {
+    int ngroups;
+    int first[MAX_GROUPS + 1];
+};
+
+__host__ __device__ __forceinline__ int group_tiles(const TileSpace& ts, int g0, int g1) {
+    int cnt = 0;
+    for (int sr = g0; sr < g1; sr++) cnt += ts.nbj > first_col(ts, sr) ? ts.nbj - first_col(ts, sr) : 0;
+    return cnt;
+}
+
+// t -> (sr, bj).
+__device__ bool tile_coords(const TileSpace& ts, const GroupTable& gt, int t, int* sr_out, int* bj_out) {
     const int gs = GROUP_M / ts.cm;  // super-rows per group
-    for (int g0 = 0; g0 < ts.nsr; g0 += gs) {
-        const int g1 = min(ts.nsr, g0 + gs);
-        int cnt = 0;
-        for (int sr = g0; sr < g1; sr++) cnt += max(0, ts.nbj - first_col(ts, sr));
-        if (t >= cnt) {
-            t -= cnt;
-            continue;
-        }
-        for (int bj = first_col(ts, g0); bj < ts.nbj; bj++) {
-            // super-rows of the group present in column bj: sr * cm <= 2 bj + 1
-            const int last = min(g1 - 1, (2 * bj + 1) / ts.cm);
-            const int rows = last - g0 + 1;
-            if (rows <= 0) continue;
+    int lo = 0, hi = gt.ngroups;     // last group whose first tile is <= t
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (gt.first[mid] <= t) lo = mid; else hi = mid;
+    }
+    t -= gt.first[lo];
+    const int g0 = lo * gs, g1 = min(ts.nsr, g0 + gs);
+    // columns where only part of the group lies on or above the diagonal
+    // (super-row sr is present in column bj iff sr * cm <= 2 bj + 1)
+    int bj = first_col(ts, g0);
+    for (; bj < ts.nbj; bj++) {
+        const int rows = min(g1 - 1, (2 * bj + 1) / ts.cm) - g0 + 1;
+        if (rows == g1 - g0) break;  // from here on every column holds the whole group
+        if (rows > 0) {
             if (t < rows) {
                 *sr_out = g0 + t;
                 *bj_out = bj;
@@ -101,15 +119,20 @@ __device__ bool tile_coords(const TileSpace& ts, int t, int* sr_out, int* bj_out
             }
             t -= rows;
         }
-        return false;
     }
-    return false;
+    const int full = g1 - g0;
+    bj += t / full;
+    if (bj >= ts.nbj) return false;
+    *sr_out = g0 + t % full;
+    *bj_out = bj;
+    return true;
 }
 
 struct TcParams {
     int n, r0, rows;
     int kblocks, kblocks_p;  // K stages in total and in the presence part
     TileSpace ts;
+    GroupTable gt;
     int num_tiles;
     const uint32_t* start;
     const uint32_t* js;
@@ -192,7 +215,7 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
             for (int q = 0; q < STAGES; q++) issued[q] = 0, issued_ph[q] = 0;
             for (int t = cid; ok && t < p.num_tiles; t += ncl) {
                 int sr, bj;
-                if (!tile_coords(p.ts, t, &sr, &bj)) break;
+                if (!tile_coords(p.ts, p.gt, t, &sr, &bj)) break;
                 const int bi = sr * CM + (int)rank;
                 const int y_a = p.r0 + bi * BM, y_b = p.r0 + bj * BN + (int)rank * (BN / CM);
                 for (int kb = 0; kb < p.kblocks; kb++) {
@@ -264,6 +287,8 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
     } else {
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3;  // TMEM lanes [32 q, 32 q + 32) belong to this warp
+        const int half = (warp - 2) / 4;  // columns [128 half, 128 half + 128) of the tile
+        constexpr int CHUNKS = BN / 32 / 2;
         uint16_t* stg = epi + (warp - 2) * 32 * EPI_PITCH;
         const int iend = p.r0 + p.rows;
         int acc = 0;
@@ -271,7 +296,7 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
         int bad = 0;
         for (int t = cid; t < p.num_tiles; t += ncl) {
             int sr, bj;
-            if (!tile_coords(p.ts, t, &sr, &bj)) break;
+            if (!tile_coords(p.ts, p.gt, t, &sr, &bj)) break;
             const int bi = sr * CM + (int)rank;
             const int i0 = p.r0 + bi * BM, j0 = p.r0 + bj * BN;
             const int my_i = i0 + q * 32 + lane;
@@ -279,17 +304,22 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
             uint32_t rp = 0, rhi = 0;
             if (p.fuse_rare && my_i < iend) {
                 rhi = __ldg(p.start + my_i + 1);
-                rp = lower_bound_u32(p.js, __ldg(p.start + my_i), rhi, (uint32_t)j0);
+                rp = lower_bound_u32(p.js, __ldg(p.start + my_i), rhi, (uint32_t)(j0 + half * (BN / 2)));
             }
+            // the next RBUF partners, fetched together (independent loads);
+            // entries [bpos, nbuf) are still to be applied
+            uint32_t rbuf[RBUF];
+            int bpos = 0, nbuf = 0;
             if (!mbar_wait(&tfull[acc], aph, abort_flag, p.err)) break;
             tc_fence_after();
             const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
 #pragma unroll 1
-            for (int c = 0; c < BN / 32; c++) {
+            for (int cc = 0; cc < CHUNKS; cc++) {
+                const int c = half * CHUNKS + cc;
                 uint32_t v[32];
                 tmem_ld32(tbase + (uint32_t)(c * 32), v);
                 tmem_wait_ld();
-                if (c == BN / 32 - 1) {  // accumulator fully read: hand it back to the MMA warp
+                if (cc == CHUNKS - 1) {  // this warp's part of the accumulator is read: hand it back
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&tempty[acc]);
@@ -312,11 +342,23 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
                 }
                 // rare pairs of this row in columns [cb, cb + 32)
                 const uint32_t cb = (uint32_t)(j0 + c * 32);
-                while (rp < rhi) {
-                    const uint32_t j = __ldg(p.js + rp);
-                    if (j >= cb + 32) break;
-                    stg[lane * EPI_PITCH + (int)(j - cb)] -= 1;
-                    rp++;
+                for (;;) {
+                    if (bpos == nbuf) {
+                        if (rp >= rhi) break;
+                        nbuf = rhi - rp < (uint32_t)RBUF ? (int)(rhi - rp) : RBUF;
+#pragma unroll
+                        for (int q = 0; q < RBUF; q++) rbuf[q] = q < nbuf ? __ldg(p.js + rp + q) : 0xFFFFFFFFu;
+                        rp += (uint32_t)nbuf;
+                        bpos = 0;
+                    }
+                    // ascending: the entries below cb + 32 form a prefix of what is left
+#pragma unroll
+                    for (int q = 0; q < RBUF; q++)
+                        if (q >= bpos && q < nbuf && rbuf[q] < cb + 32) {
+                            stg[lane * EPI_PITCH + (int)(rbuf[q] - cb)] -= 1;
+                            bpos = q + 1;
+                        }
+                    if (bpos < nbuf) break;  // the next partner lies beyond this chunk
                 }
                 __syncwarp();
                 // coalesced store: 16 lanes x 4 bytes per row, 2 rows per step
@@ -421,6 +463,17 @@ cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCS
     p.ts.nsr = ((a.rows + BM - 1) / BM + CM - 1) / CM;
     p.ts.nbj = (a.n - a.r0 + BN - 1) / BN;
     p.num_tiles = (int)count_tiles(p.ts);
+    {
+        const int gs = GROUP_M / CM;
+        p.gt.ngroups = (p.ts.nsr + gs - 1) / gs;
+        if (p.gt.ngroups > MAX_GROUPS) return cudaErrorInvalidValue;  // callers split taller stripes
+        int acc = 0;
+        for (int g = 0; g < p.gt.ngroups; g++) {
+            p.gt.first[g] = acc;
+            acc += group_tiles(p.ts, g * gs, std::min(p.ts.nsr, g * gs + gs));
+        }
+        p.gt.first[p.gt.ngroups] = acc;
+    }
     p.start = rare.start;
     p.js = rare.js;
     p.fuse_rare = (rare.n_rare > 0 && rare.sorted) ? 1 : 0;
@@ -457,10 +510,20 @@ cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t*
                              const StripeArgs& a, int num_sms, cudaStream_t st) {
     (void)Xneg;
     if (a.rows <= 0 || a.r0 >= a.n) return cudaSuccess;
-    if (kernel == TCH_KERNEL_TC_F8)
-        return cluster_size() == 2 ? launch_kind<KIND_F8, 2>(ops, ops.X, rare, a, num_sms, st)
-                                   : launch_kind<KIND_F8, 1>(ops, ops.X, rare, a, num_sms, st);
-    return cudaErrorNotSupported;
+    if (kernel != TCH_KERNEL_TC_F8) return cudaErrorNotSupported;
+    // one launch covers at most MAX_GROUPS raster groups of rows; a taller
+    // stripe runs as consecutive sub-stripes writing into the same output
+    const int max_rows = MAX_GROUPS * GROUP_M * BM;
+    for (int done = 0; done < a.rows; done += max_rows) {
+        StripeArgs s = a;
+        s.r0 = a.r0 + done;
+        s.rows = std::min(max_rows, a.rows - done);
+        s.out = a.out + (size_t)done * a.ldo + (size_t)done;
+        const cudaError_t e = cluster_size() == 2 ? launch_kind<KIND_F8, 2>(ops, ops.X, rare, s, num_sms, st)
+                                                  : launch_kind<KIND_F8, 1>(ops, ops.X, rare, s, num_sms, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace tch
