@@ -295,28 +295,27 @@ def main():
         with open(prof) as f:
             roofline["traffic"] = json.load(f).get("bytes_per_launch")
 
-    # e2e through tch_run with host buffers
+    # e2e through the C ABI with host buffers: tch_run (the reference's entry
+    # point, host-encoded operands) and tch_run_calls (allele calls, device encoder)
     e2e = None
+    e2e_calls = None
     if rank == 0 and args.e2e_steps > 0:
+        import ctypes
+
+        os.environ["TCH_VERBOSE"] = "1"  # phase breakdown on stderr
         tch.set_kernel(args.kernel)
-        enc = tch.encode_host(x, nd, tau)  # the reference host's encoding, outside the timed region
+        # the host path uploads every rare pair: its tau model charges the upload
+        tau_host = args.tau or tch.choose_tau(x, nd, args.stripe, tch.free_vram(device), 1.6e15, 1.0e11)
+        enc = tch.encode_host(x, nd, tau_host)  # the reference host's encoding, outside the timed region
         h2d = enc.O.nbytes + enc.P.nbytes + enc.start.nbytes + enc.js.nbytes
-        d2h = 0
-        for r0 in range(0, n, args.stripe):
-            d2h += min(args.stripe, n - r0) * (n - r0) * 2
+        d2h = sum(min(args.stripe, n - r0) * (n - r0) * 2 for r0 in range(0, n, args.stripe))
 
-        class Nop:
-            calls = 0
+        def nop(ctx, r0, rows, w, ptr):
+            pass
 
-            def __call__(self, ctx, r0, rows, w, ptr):
-                Nop.calls += 1
-
-        times = []
+        cb = tch.CB(nop)
+        times, times_calls = [], []
         for k in range(args.e2e_steps + 1):
-            sink = Nop()
-            cb = tch.CB(sink)
-            import ctypes
-
             secs = ctypes.c_double(0)
             rg = ctypes.c_int(0)
             err = ctypes.create_string_buffer(512)
@@ -327,12 +326,26 @@ def main():
             dt = time.perf_counter() - t
             if rc:
                 raise RuntimeError(err.value.decode())
-            if k > 0:  # first call warms the context and the pinned allocator
+            tu = ctypes.c_int(0)
+            t = time.perf_counter()
+            rc = tch.lib().tch_run_calls(device, n, L, tch._ptr(A), args.tau, args.stripe, cb, None,
+                                         ctypes.byref(secs), ctypes.byref(tu), err, len(err))
+            dt_calls = time.perf_counter() - t
+            if rc:
+                raise RuntimeError(err.value.decode())
+            if k > 0:  # the first round warms the context and the pinned stripe buffers
                 times.append(dt)
+                times_calls.append(dt_calls)
+        os.environ.pop("TCH_VERBOSE", None)
         e2e_s = statistics.median(times)
         e2e = {"value": pairs_total / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_s,
-               "path": f"tch_run (reference C ABI), host O/P/CSR, stripe {args.stripe}, no-op callback"}
+               "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_s, "tau": tau_host,
+               "path": f"tch_run (the reference's C ABI): host O/P bits + rare CSR uploaded, stripes of "
+                       f"{args.stripe} rows copied back, no-op callback"}
+        ec = statistics.median(times_calls)
+        e2e_calls = {"value": pairs_total / ec, "unit": UNIT, "h2d_bytes_per_step": int(A.nbytes),
+                     "d2h_bytes_per_step": int(d2h), "seconds_per_step": ec, "tau": int(tu.value),
+                     "path": "tch_run_calls: allele calls uploaded, device encoder, same stripes and copy-back"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -348,6 +361,7 @@ def main():
                 "data": "synthetic", "config": dict(workload, kernel=info["kernel"], stripe_e2e=args.stripe,
                                                     parallelism=f"row shares x{ws}"),
                 "gpu_launches": args.steps, "clocks": ck, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "e2e_device_encoder": e2e_calls,
                 "peak_probe": peak_info}
         print(json.dumps(line), flush=True)
     solver.close()

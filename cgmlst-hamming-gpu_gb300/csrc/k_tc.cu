@@ -355,7 +355,10 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
 #pragma unroll
                     for (int q = 0; q < RBUF; q++)
                         if (q >= bpos && q < nbuf && rbuf[q] < cb + 32) {
-                            stg[lane * EPI_PITCH + (int)(rbuf[q] - cb)] -= 1;
+                            // one shared-memory op per partner: subtract from the cell's half of
+                            // its 32-bit word (a cell never drops below zero, so nothing borrows)
+                            const int cidx = lane * EPI_PITCH + (int)(rbuf[q] - cb);
+                            atomicSub(reinterpret_cast<unsigned int*>(stg) + (cidx >> 1), 1u << (16 * (cidx & 1)));
                             bpos = q + 1;
                         }
                     if (bpos < nbuf) break;  // the next partner lies beyond this chunk

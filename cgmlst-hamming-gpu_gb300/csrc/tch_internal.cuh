@@ -96,7 +96,7 @@ cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t*
 // Rates of the analytic tau model on this GPU.
 struct TauModel {
     double gemm_rate = 1.6e15;  // pair x one-byte-column MACs per second of the stripe kernel
-    double rare_rate = 2.0e10;  // rare pairs per second of the fused subtraction
+    double rare_rate = 6.0e11;  // rare pairs per second of the fused subtraction
 };
 
 // Operands built on the device from allele calls; device memory owned here.

@@ -21,6 +21,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
+#include <mutex>
 #include <vector>
 
 #include "tch_internal.cuh"
@@ -371,25 +373,89 @@ fail:
 }
 
 // Stripe pipeline through pinned host memory, two streams (tch.cu:113-149).
+// Page-locked stripe buffers cost far more to allocate than to use, so the
+// pair of the previous run is kept for the next one (one pair per process;
+// a run that finds it in use allocates its own).
+struct PinnedPool {
+    std::mutex mu;
+    void* buf[2] = {nullptr, nullptr};
+    size_t bytes = 0;
+    bool busy = false;
+};
+static PinnedPool g_pinned;
+
+static cudaError_t pinned_acquire(size_t bytes, uint16_t* out[2], bool* pooled) {
+    {
+        std::lock_guard<std::mutex> lk(g_pinned.mu);
+        if (!g_pinned.busy) {
+            if (g_pinned.bytes < bytes) {
+                for (int b = 0; b < 2; b++) {
+                    if (g_pinned.buf[b]) cudaFreeHost(g_pinned.buf[b]);
+                    g_pinned.buf[b] = nullptr;
+                }
+                g_pinned.bytes = 0;
+                for (int b = 0; b < 2; b++) {
+                    const cudaError_t ce = cudaMallocHost(&g_pinned.buf[b], bytes);
+                    if (ce != cudaSuccess) return ce;
+                }
+                g_pinned.bytes = bytes;
+            }
+            g_pinned.busy = true;
+            out[0] = (uint16_t*)g_pinned.buf[0];
+            out[1] = (uint16_t*)g_pinned.buf[1];
+            *pooled = true;
+            return cudaSuccess;
+        }
+    }
+    *pooled = false;
+    for (int b = 0; b < 2; b++) {
+        const cudaError_t ce = cudaMallocHost((void**)&out[b], bytes);
+        if (ce != cudaSuccess) return ce;
+    }
+    return cudaSuccess;
+}
+
+static void pinned_release(uint16_t* p[2], bool pooled) {
+    if (pooled) {
+        std::lock_guard<std::mutex> lk(g_pinned.mu);
+        g_pinned.busy = false;
+        return;
+    }
+    for (int b = 0; b < 2; b++)
+        if (p[b]) cudaFreeHost(p[b]);
+}
+
+static double wall() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+static bool verbose() {
+    const char* v = getenv("TCH_VERBOSE");
+    return v && v[0] == '1';
+}
+
 static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_secs, Err& e) {
     const int n = s->n;
     const size_t ldo = up((size_t)std::max(n, 1), 8);
     uint16_t* dU[2] = {nullptr, nullptr};
     uint16_t* hU[2] = {nullptr, nullptr};
+    bool pooled = false;
     cudaStream_t st[2] = {nullptr, nullptr};
     cudaEvent_t done[2] = {nullptr, nullptr}, t0 = nullptr, t1 = nullptr;
     int rc = 1, prev = -1;
     float ms = 0.f;
+    double w0 = wall(), w_setup = 0, w_cb = 0;
     if (S <= 0) return e.set("stripe rows must be positive (got %d)", S);
     if (!cb) return e.set("null callback");
     S = std::min(S, std::max(n, 1));
     TCH_CK(e, cudaSetDevice(s->device));
+    TCH_CK(e, pinned_acquire((size_t)S * ldo * 2, hU, &pooled));
     for (int b = 0; b < 2; b++) {
         TCH_CK(e, cudaMalloc(&dU[b], (size_t)S * ldo * 2));
-        TCH_CK(e, cudaMallocHost(&hU[b], (size_t)S * ldo * 2));
         TCH_CK(e, cudaStreamCreateWithFlags(&st[b], cudaStreamNonBlocking));
         TCH_CK(e, cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming));
     }
+    w_setup = wall() - w0;
     TCH_CK(e, cudaEventCreate(&t0));
     TCH_CK(e, cudaEventCreate(&t1));
     TCH_CK(e, cudaEventRecord(t0, st[0]));
@@ -412,7 +478,9 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
                     for (uint32_t p = s->hStart[i]; p < s->hStart[i + 1]; p++)
                         hU[b][(size_t)r * w + (s->hJs[p] - prev)] -= 1;
                 }
+            const double wc = wall();
             cb(ctx, prev, rows, w, hU[b]);
+            w_cb += wall() - wc;
         }
         if (r0 >= n) break;
         prev = r0;
@@ -423,15 +491,18 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
     TCH_CK(e, cudaEventElapsedTime(&ms, t0, t1));
     if (gpu_secs) *gpu_secs = ms / 1e3;
     if (solver_check(s, e)) goto fail;
+    if (verbose())
+        fprintf(stderr, "tch: stripes %d rows: setup %.1f ms, pipeline %.1f ms (device %.1f ms, callbacks %.1f ms)\n",
+                S, w_setup * 1e3, (wall() - w0 - w_setup) * 1e3, ms, w_cb * 1e3);
     rc = 0;
 fail:
     for (int b = 0; b < 2; b++) {
         if (st[b]) cudaStreamSynchronize(st[b]);
         if (dU[b]) cudaFree(dU[b]);
-        if (hU[b]) cudaFreeHost(hU[b]);
         if (st[b]) cudaStreamDestroy(st[b]);
         if (done[b]) cudaEventDestroy(done[b]);
     }
+    pinned_release(hU, pooled);
     if (t0) cudaEventDestroy(t0);
     if (t1) cudaEventDestroy(t1);
     return rc;
@@ -462,8 +533,12 @@ int tch_run(int device, int n, size_t n_pad, const uint8_t* O, size_t K1, const 
     Err e{err, errlen};
     tch_solver* s = nullptr;
     if (S <= 0) return e.set("stripe rows must be positive (got %d)", S);
+    const double w0 = wall();
     if (solver_from_bits(device, n, n_pad, O, K1, P, K2, start, js, n_rare, default_kernel(), S, true, &s, e))
         return 1;
+    if (verbose())
+        fprintf(stderr, "tch: operands on the device in %.1f ms (%.2f GB uploaded)\n", (wall() - w0) * 1e3,
+                (double)(n_pad * (K1 + K2) / 8 + (n_rare + (size_t)n + 1) * 4) / 1e9);
     if (rare_on_gpu) *rare_on_gpu = s->rare_on_host ? 0 : 1;
     const int rc = solver_run(s, S, cb, ctx, gpu_secs, e);
     solver_free(s);
