@@ -27,6 +27,7 @@
 // tile epilogue.  All ids are compared for equality only; any 64-bit values
 // work (hashed ids included).
 
+#include <chrono>
 #include <vector>
 
 #include "tch_internal.cuh"
@@ -373,6 +374,16 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
     *out = DeviceEncoding();
     out->n = n;
     out->L = L;
+    // phase times (with a device sync at each mark) when verbose
+    double t_mark = 0;
+    auto mark = [&](const char* phase) {
+        if (!verbose) return;
+        cudaDeviceSynchronize();
+        const double t = std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+        if (t_mark > 0) fprintf(stderr, "tch encoder: %-26s %8.1f ms\n", phase, (t - t_mark) * 1e3);
+        t_mark = t;
+    };
+    mark("start");
 
     TCH_CK(e, cudaSetDevice(device));
     TCH_CK(e, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
@@ -441,6 +452,7 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
     cudaFree(list_keys); list_keys = nullptr;
     cudaFree(list_slots); list_slots = nullptr;
 
+    mark("ranks and counts");
     // ---- host: tau, frequent columns, rare groups
     {
         int tau = tau_req;
@@ -485,6 +497,7 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
         TCH_CK(e, cudaMemcpy(base_d, base.data(), ((size_t)L + 1) * 4, cudaMemcpyHostToDevice));
         TCH_CK(e, cudaMemcpy(goff_d, goff.data(), (off_h[L] + 1) * 8, cudaMemcpyHostToDevice));
 
+        mark("tau and column maps");
         // ---- 4: operand rows
         TCH_CK(e, dalloc(&out->X, out->x_rows * (size_t)out->kb, &out->bytes));
         TCH_CK(e, cudaMemset(out->X, 0, out->x_rows * (size_t)out->kb));
@@ -492,6 +505,7 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
                                                              out->kp, 0x38);
         TCH_CK(e, cudaGetLastError());
 
+        mark("operand rows");
         // ---- 5: rare groups, sorted
         const size_t ngroups = groups.size() / 2;
         TCH_CK(e, dalloc(&members, n_members, &tmp_bytes));
@@ -510,6 +524,7 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
             }
         }
 
+        mark("rare groups");
         // ---- 6: CSR of rare pairs, ascending per row
         TCH_CK(e, dalloc(&row_count, (size_t)n, &tmp_bytes));
         TCH_CK(e, dalloc(&start64, (size_t)n + 1, &tmp_bytes));
@@ -547,6 +562,7 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
             TCH_CK(e, cudaGetLastError());
         }
         TCH_CK(e, cudaDeviceSynchronize());
+        mark("rare CSR (2 passes)");
     }
     cudaFree(err_d); cudaFree(nd); cudaFree(cnt_off_d); cudaFree(cnt_flat); cudaFree(col_d); cudaFree(base_d);
     cudaFree(goff_d); cudaFree(members); cudaFree(sorted); cudaFree(gfill); cudaFree(groups_d); cudaFree(row_count);

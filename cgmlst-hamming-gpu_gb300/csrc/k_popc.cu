@@ -122,7 +122,9 @@ popc_stripe_kernel(const uint32_t* __restrict__ P, int wP, const uint32_t* __res
 // cell (the cell never goes below zero, so no borrow reaches its neighbour).
 __global__ void rare_atomic_kernel(uint16_t* __restrict__ out, size_t ldo, int n, int r0, int rows,
                                    const uint32_t* __restrict__ start, const uint32_t* __restrict__ js,
-                                   int* err) {
+                                   int* err, const int* only_if_unsorted) {
+    // with a check flag: the stripe kernel already subtracted ascending lists
+    if (only_if_unsorted && *only_if_unsorted == 0) return;
     const int r = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x % 32;
     if (r >= rows) return;
     const int i = r0 + r;
@@ -141,9 +143,9 @@ __global__ void rare_atomic_kernel(uint16_t* __restrict__ out, size_t ldo, int n
 
 // flag stays 0 iff every row is ascending and every partner is in (i, n)
 __global__ void rare_check_kernel(const uint32_t* __restrict__ start, const uint32_t* __restrict__ js, int n,
-                                  int* bad) {
-    const int i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x % 32;
-    if (i >= n) return;
+                                  int r_begin, int r_end, int* bad) {
+    const int i = r_begin + blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x % 32;
+    if (i >= r_end) return;
     const uint32_t lo = __ldg(start + i), hi = __ldg(start + i + 1);
     int flag = 0;
     for (uint32_t p = lo + lane; p < hi; p += 32) {
@@ -176,13 +178,16 @@ cudaError_t launch_popc_stripe(const BitOperands& ops, const RareCSR& rare, cons
 cudaError_t launch_rare_atomic(const RareCSR& rare, const StripeArgs& a, cudaStream_t st) {
     if (rare.n_rare == 0 || a.rows <= 0) return cudaSuccess;
     rare_atomic_kernel<<<(a.rows + 7) / 8, 256, 0, st>>>(a.out, a.ldo, a.n, a.r0, a.rows, rare.start, rare.js,
-                                                         a.err);
+                                                         a.err, rare.unsorted_flag);
     return cudaGetLastError();
 }
 
-cudaError_t launch_rare_check_sorted(const RareCSR& rare, int n, int* d_flag, cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
-    rare_check_kernel<<<(n + 7) / 8, 256, 0, st>>>(rare.start, rare.js, n, d_flag);
+cudaError_t launch_rare_check_sorted(const RareCSR& rare, int n, int* d_flag, cudaStream_t st, int r_begin,
+                                     int r_end) {
+    if (r_end < 0 || r_end > n) r_end = n;
+    if (r_begin < 0) r_begin = 0;
+    if (r_end <= r_begin) return cudaSuccess;
+    rare_check_kernel<<<(r_end - r_begin + 7) / 8, 256, 0, st>>>(rare.start, rare.js, n, r_begin, r_end, d_flag);
     return cudaGetLastError();
 }
 

@@ -137,6 +137,7 @@ struct TcParams {
     const uint32_t* start;
     const uint32_t* js;
     int fuse_rare;
+    const int* unsorted;  // optional device flag: non-zero turns the fused subtraction off
     uint16_t* out;
     size_t ldo;
     int* err;
@@ -291,6 +292,7 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
         constexpr int CHUNKS = BN / 32 / 2;
         uint16_t* stg = epi + (warp - 2) * 32 * EPI_PITCH;
         const int iend = p.r0 + p.rows;
+        const bool fuse = p.fuse_rare && !(p.unsorted && *p.unsorted);
         int acc = 0;
         uint32_t aph = 0;
         int bad = 0;
@@ -302,7 +304,7 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
             const int my_i = i0 + q * 32 + lane;
             // this row's rare partners inside the tile: an ascending run of js
             uint32_t rp = 0, rhi = 0;
-            if (p.fuse_rare && my_i < iend) {
+            if (fuse && my_i < iend) {
                 rhi = __ldg(p.start + my_i + 1);
                 rp = lower_bound_u32(p.js, __ldg(p.start + my_i), rhi, (uint32_t)(j0 + half * (BN / 2)));
             }
@@ -355,10 +357,9 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
 #pragma unroll
                     for (int q = 0; q < RBUF; q++)
                         if (q >= bpos && q < nbuf && rbuf[q] < cb + 32) {
-                            // one shared-memory op per partner: subtract from the cell's half of
-                            // its 32-bit word (a cell never drops below zero, so nothing borrows)
-                            const int cidx = lane * EPI_PITCH + (int)(rbuf[q] - cb);
-                            atomicSub(reinterpret_cast<unsigned int*>(stg) + (cidx >> 1), 1u << (16 * (cidx & 1)));
+                            // (a shared atomicSub on the 32-bit word measured slower than this
+                            // plain read-modify-write of the lane's own row)
+                            stg[lane * EPI_PITCH + (int)(rbuf[q] - cb)] -= 1;
                             bpos = q + 1;
                         }
                     if (bpos < nbuf) break;  // the next partner lies beyond this chunk
@@ -479,7 +480,8 @@ cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCS
     }
     p.start = rare.start;
     p.js = rare.js;
-    p.fuse_rare = (rare.n_rare > 0 && rare.sorted) ? 1 : 0;
+    p.fuse_rare = (rare.n_rare > 0 && (rare.sorted || rare.unsorted_flag)) ? 1 : 0;
+    p.unsorted = rare.unsorted_flag;
     p.out = a.out;
     p.ldo = a.ldo;
     p.err = a.err;

@@ -45,6 +45,11 @@ struct RareCSR {
     const uint32_t* js = nullptr;     // n_rare
     size_t n_rare = 0;
     bool sorted = false;              // every row ascending -> fused subtraction
+    // Optional device flag set by a check of this stripe's rows that ran
+    // earlier on the same stream: 0 = ascending (fused subtraction), non-zero =
+    // not (the separate atomic pass).  Lets the host launch both without
+    // waiting for the check.
+    const int* unsorted_flag = nullptr;
 };
 
 // Bit-packed operands in the reference layout, u32 words, LSB first.
@@ -76,8 +81,10 @@ cudaError_t launch_popc_stripe(const BitOperands& ops, const RareCSR& rare, cons
                                cudaStream_t st);
 // Unsorted CSR: separate pass with 32-bit atomics on the u16 stripe.
 cudaError_t launch_rare_atomic(const RareCSR& rare, const StripeArgs& a, cudaStream_t st);
-// Sets *flag to 0 if every CSR row is ascending (and stays 1 otherwise).
-cudaError_t launch_rare_check_sorted(const RareCSR& rare, int n, int* d_unsorted, cudaStream_t st);
+// ORs into *d_flag: 1 if a row in [r_begin, r_end) is not ascending, 2 if a
+// partner is outside (i, n).  r_end < 0 means n.
+cudaError_t launch_rare_check_sorted(const RareCSR& rare, int n, int* d_flag, cudaStream_t st, int r_begin = 0,
+                                     int r_end = -1);
 
 // ---- k_expand.cu ------------------------------------------------------------------
 // Bit rows -> byte operand rows for the tensor-core kernels.

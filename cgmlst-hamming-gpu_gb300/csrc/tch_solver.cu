@@ -97,6 +97,10 @@ struct tch_solver {
     size_t n_rare = 0;
     bool sorted = false;
     bool rare_on_host = false;              // reference fallback (tch.cu:140-144)
+    // tch_run uploads the partner list stripe by stripe, overlapped with the
+    // previous stripe's work (borrowed host arrays, valid during tch_run)
+    const uint32_t* defer_start = nullptr;
+    const uint32_t* defer_js = nullptr;
     const uint32_t* hStart = nullptr;       // borrowed for the host fallback
     const uint32_t* hJs = nullptr;
     int* dErr = nullptr;
@@ -140,7 +144,8 @@ static void tc_encoding(int kernel, uint8_t* one, uint8_t* neg) {
 // Operands on the device from the reference's bit layout (host buffers).
 static int solver_from_bits(int device, int n, size_t n_pad, const uint8_t* O, size_t K1, const uint8_t* P,
                             size_t K2, const uint32_t* start, const uint32_t* js, size_t n_rare, int kernel,
-                            int stripe_for_fit, bool allow_host_rare, tch_solver** out, Err& e) {
+                            int stripe_for_fit, bool allow_host_rare, tch_solver** out, Err& e,
+                            bool defer_js = false) {
     tch_solver* s = nullptr;
     int* dflag = nullptr;
     int hflag = 0;
@@ -220,6 +225,13 @@ static int solver_from_bits(int device, int n, size_t n_pad, const uint8_t* O, s
         TCH_CK(e, dmalloc(s, (void**)&s->dJs, std::max<size_t>(n_rare, 1) * 4));
         if (start) TCH_CK(e, cudaMemcpy(s->dStart, start, ((size_t)n + 1) * 4, cudaMemcpyHostToDevice));
         else TCH_CK(e, cudaMemset(s->dStart, 0, ((size_t)n + 1) * 4));
+        if (defer_js && n_rare && is_tc(kernel)) {  // uploaded and checked per stripe by solver_run
+            s->defer_start = start;
+            s->defer_js = js;
+            s->sorted = false;
+            *out = s;
+            return 0;
+        }
         if (n_rare) TCH_CK(e, cudaMemcpy(s->dJs, js, n_rare * 4, cudaMemcpyHostToDevice));
         // ascending rows -> subtraction fused into the contraction's epilogue
         TCH_CK(e, cudaMalloc(&dflag, sizeof(int)));
@@ -316,8 +328,10 @@ fail:
     return 1;
 }
 
-static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e) {
+static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e,
+                         const int* unsorted_flag = nullptr) {
     if (r0 < 0 || rows < 0 || r0 > s->n) return e.set("stripe out of range (r0=%d rows=%d n=%d)", r0, rows, s->n);
+    if (s->defer_js && !unsorted_flag) return e.set("partner lists not uploaded (run the whole pipeline)");
     if (r0 + rows > s->n) rows = s->n - r0;
     if (rows == 0) return 0;
     if (ldo < (size_t)(s->n - r0)) return e.set("ldo %zu < stripe width %d", ldo, s->n - r0);
@@ -336,6 +350,7 @@ static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_
         rare.js = s->dJs;
         rare.n_rare = s->n_rare;
         rare.sorted = s->sorted;
+        rare.unsorted_flag = unsorted_flag;
     }
     cudaError_t ce;
     if (s->kernel == TCH_KERNEL_POPC) {
@@ -440,6 +455,8 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
     uint16_t* dU[2] = {nullptr, nullptr};
     uint16_t* hU[2] = {nullptr, nullptr};
     bool pooled = false;
+    int* dflags = nullptr;  // per stripe: its partner lists are not ascending (1) / invalid (2)
+    std::vector<int> hflags;
     cudaStream_t st[2] = {nullptr, nullptr};
     cudaEvent_t done[2] = {nullptr, nullptr}, t0 = nullptr, t1 = nullptr;
     int rc = 1, prev = -1;
@@ -455,6 +472,11 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
         TCH_CK(e, cudaStreamCreateWithFlags(&st[b], cudaStreamNonBlocking));
         TCH_CK(e, cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming));
     }
+    if (s->defer_js) {
+        hflags.assign((size_t)(n + S - 1) / S, 0);
+        TCH_CK(e, cudaMalloc(&dflags, hflags.size() * sizeof(int)));
+        TCH_CK(e, cudaMemset(dflags, 0, hflags.size() * sizeof(int)));
+    }
     w_setup = wall() - w0;
     TCH_CK(e, cudaEventCreate(&t0));
     TCH_CK(e, cudaEventCreate(&t1));
@@ -464,7 +486,23 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
         if (r0 < n) {
             const int rows = std::min(S, n - r0), b = (r0 / S) & 1;
             const size_t w = (size_t)(n - r0);
-            if (solver_stripe(s, r0, rows, dU[b], ldo, st[b], e)) goto fail;
+            const int* flag = nullptr;
+            if (s->defer_js) {
+                // this stripe's partner lists: uploaded while the previous stripe
+                // computes, then checked on the device; the stripe kernel and the
+                // atomic pass read the verdict from the flag
+                const size_t pa = s->defer_start[r0], pb = s->defer_start[r0 + rows];
+                if (pb > pa)
+                    TCH_CK(e, cudaMemcpyAsync(s->dJs + pa, s->defer_js + pa, (pb - pa) * 4, cudaMemcpyHostToDevice,
+                                              st[b]));
+                RareCSR rc;
+                rc.start = s->dStart;
+                rc.js = s->dJs;
+                rc.n_rare = s->n_rare;
+                TCH_CK(e, launch_rare_check_sorted(rc, n, dflags + r0 / S, st[b], r0, r0 + rows));
+                flag = dflags + r0 / S;
+            }
+            if (solver_stripe(s, r0, rows, dU[b], ldo, st[b], e, flag)) goto fail;
             TCH_CK(e, cudaMemcpy2DAsync(hU[b], w * 2, dU[b], ldo * 2, w * 2, rows, cudaMemcpyDeviceToHost, st[b]));
             TCH_CK(e, cudaEventRecord(done[b], st[b]));
         }
@@ -491,6 +529,14 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
     TCH_CK(e, cudaEventElapsedTime(&ms, t0, t1));
     if (gpu_secs) *gpu_secs = ms / 1e3;
     if (solver_check(s, e)) goto fail;
+    if (dflags) {
+        TCH_CK(e, cudaMemcpy(hflags.data(), dflags, hflags.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int f : hflags)
+            if (f & 2) {
+                e.set("rare CSR: a partner j is not in (i, n)");
+                goto fail;
+            }
+    }
     if (verbose())
         fprintf(stderr, "tch: stripes %d rows: setup %.1f ms, pipeline %.1f ms (device %.1f ms, callbacks %.1f ms)\n",
                 S, w_setup * 1e3, (wall() - w0 - w_setup) * 1e3, ms, w_cb * 1e3);
@@ -503,6 +549,7 @@ fail:
         if (done[b]) cudaEventDestroy(done[b]);
     }
     pinned_release(hU, pooled);
+    if (dflags) cudaFree(dflags);
     if (t0) cudaEventDestroy(t0);
     if (t1) cudaEventDestroy(t1);
     return rc;
@@ -534,7 +581,7 @@ int tch_run(int device, int n, size_t n_pad, const uint8_t* O, size_t K1, const 
     tch_solver* s = nullptr;
     if (S <= 0) return e.set("stripe rows must be positive (got %d)", S);
     const double w0 = wall();
-    if (solver_from_bits(device, n, n_pad, O, K1, P, K2, start, js, n_rare, default_kernel(), S, true, &s, e))
+    if (solver_from_bits(device, n, n_pad, O, K1, P, K2, start, js, n_rare, default_kernel(), S, true, &s, e, true))
         return 1;
     if (verbose())
         fprintf(stderr, "tch: operands on the device in %.1f ms (%.2f GB uploaded)\n", (wall() - w0) * 1e3,
