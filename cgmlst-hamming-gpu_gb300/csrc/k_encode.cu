@@ -263,11 +263,28 @@ rare_rows_kernel(const uint16_t* __restrict__ x, int n, int L, const uint64_t* _
                 const uint64_t q = cnt_off[k] + a;
                 const uint64_t g0 = goff[q], g1 = goff[q + 1];
                 if (g1 <= g0) continue;
-                for (uint64_t p = lower_bound_rows(members, g0, g1, (uint32_t)c0); p < g1; p++) {
-                    const uint32_t j = members[p];
-                    if (j >= (uint32_t)c1) break;
-                    const uint32_t o = j - (uint32_t)c0;
-                    atomicAdd(cw + (o >> 1), 1u << (16 * (o & 1)));
+                // members in batches of 16 independent loads (a dependent load per
+                // member leaves the walk latency-bound)
+                uint64_t p = lower_bound_rows(members, g0, g1, (uint32_t)c0);
+                while (p < g1) {
+                    const int m = g1 - p < 16 ? (int)(g1 - p) : 16;
+                    uint32_t buf[16];
+#pragma unroll
+                    for (int q = 0; q < 16; q++) buf[q] = q < m ? members[p + q] : 0xFFFFFFFFu;
+                    bool stop = false;
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        if (q < m && !stop) {
+                            if (buf[q] >= (uint32_t)c1) {
+                                stop = true;
+                            } else {
+                                const uint32_t o = buf[q] - (uint32_t)c0;
+                                atomicAdd(cw + (o >> 1), 1u << (16 * (o & 1)));
+                            }
+                        }
+                    }
+                    if (stop) break;
+                    p += (uint64_t)m;
                 }
             }
             __syncthreads();

@@ -440,6 +440,33 @@ static void pinned_release(uint16_t* p[2], bool pooled) {
         if (p[b]) cudaFreeHost(p[b]);
 }
 
+// Device-side copy from the caller's (pageable) host memory, for GPUs that
+// reach host memory through the host's page tables (Grace-Blackwell: the
+// NVLink-C2C link is coherent).  Runs asynchronously on the stripe's stream,
+// unlike a cudaMemcpyAsync from pageable memory, which the host stages.
+__global__ void pull_from_host_kernel(uint32_t* __restrict__ dst, const uint32_t* __restrict__ src, size_t count) {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < count; k += (size_t)gridDim.x * blockDim.x)
+        dst[k] = src[k];
+}
+
+static bool host_pages_visible(int device) {
+    int a = 0, b = 0;
+    if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess)
+        return false;
+    const char* off = getenv("TCH_NO_HOST_PULL");  // force the staged copy
+    return a == 1 && b == 1 && !(off && off[0] == '1');
+}
+
+static cudaError_t upload_u32(uint32_t* dst, const uint32_t* src, size_t count, bool pull, int sms,
+                              cudaStream_t st) {
+    if (!count) return cudaSuccess;
+    if (!pull) return cudaMemcpyAsync(dst, src, count * 4, cudaMemcpyHostToDevice, st);
+    const int blocks = (int)std::min<size_t>((count + 255) / 256, (size_t)sms * 2);
+    pull_from_host_kernel<<<blocks, 256, 0, st>>>(dst, src, count);
+    return cudaGetLastError();
+}
+
 static double wall() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -457,6 +484,7 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
     bool pooled = false;
     int* dflags = nullptr;  // per stripe: its partner lists are not ascending (1) / invalid (2)
     std::vector<int> hflags;
+    const bool pull = s->defer_js && host_pages_visible(s->device);
     cudaStream_t st[2] = {nullptr, nullptr};
     cudaEvent_t done[2] = {nullptr, nullptr}, t0 = nullptr, t1 = nullptr;
     int rc = 1, prev = -1;
@@ -492,9 +520,7 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
                 // computes, then checked on the device; the stripe kernel and the
                 // atomic pass read the verdict from the flag
                 const size_t pa = s->defer_start[r0], pb = s->defer_start[r0 + rows];
-                if (pb > pa)
-                    TCH_CK(e, cudaMemcpyAsync(s->dJs + pa, s->defer_js + pa, (pb - pa) * 4, cudaMemcpyHostToDevice,
-                                              st[b]));
+                TCH_CK(e, upload_u32(s->dJs + pa, s->defer_js + pa, pb - pa, pull, s->num_sms, st[b]));
                 RareCSR rc;
                 rc.start = s->dStart;
                 rc.js = s->dJs;

@@ -91,6 +91,27 @@ def test_host_rare_fallback(tch, checkpy_inputs):
     upper_equal(H, ref)
 
 
+@pytest.mark.parametrize("pull", ["1", "0"])
+def test_tch_run_partner_upload_paths(tch, checkpy_inputs, pull):
+    """tch_run uploads each stripe's partner lists while the previous stripe
+    computes: read by the GPU from host memory where the platform allows it,
+    else staged by cudaMemcpyAsync (TCH_NO_HOST_PULL=1).  Both in any order."""
+    c, A, x, ref = checkpy_inputs[2]
+    xr, nd = tch.dense_ranks(A.astype(np.uint64))
+    enc = tch.encode_host(xr, nd, 64)
+    rng = np.random.default_rng(5)
+    for i in range(0, enc.n, 3):  # every third row unsorted
+        seg = enc.js[enc.start[i]:enc.start[i + 1]]
+        rng.shuffle(seg)
+    os.environ["TCH_NO_HOST_PULL"] = "0" if pull == "1" else "1"
+    try:
+        H, _, rare_gpu, _ = tch.run(enc, stripe=136)
+    finally:
+        del os.environ["TCH_NO_HOST_PULL"]
+    assert rare_gpu == 1
+    upper_equal(H, ref)
+
+
 def test_unsorted_partner_lists(tch, checkpy_inputs):
     """The reference host fills partner lists in any order (main.rs:436-442)."""
     c, A, x, ref = checkpy_inputs[1]
