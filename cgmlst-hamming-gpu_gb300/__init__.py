@@ -40,7 +40,7 @@ class Info(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int), ("L", ctypes.c_int), ("tau", ctypes.c_int), ("kernel", ctypes.c_int),
                 ("n_pad", ctypes.c_size_t), ("k_presence", ctypes.c_size_t), ("k_onehot", ctypes.c_size_t),
                 ("d_onehot", ctypes.c_size_t), ("n_rare", ctypes.c_size_t), ("rare_sorted", ctypes.c_int),
-                ("device_bytes", ctypes.c_size_t)]
+                ("device_bytes", ctypes.c_size_t), ("k_chunks", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -108,6 +108,7 @@ def lib():
                                     c_char_p, c_int]
         L.tch_run_calls.restype = c_int
         L.tch_set_tau_model.argtypes, L.tch_set_tau_model.restype = [c_double, c_double], c_int
+        L.tch_set_max_chunk_bytes.argtypes, L.tch_set_max_chunk_bytes.restype = [c_size], c_int
         _lib = L
     return _lib
 
@@ -256,6 +257,11 @@ def run_calls(calls: np.ndarray, stripe: int = 512, tau: int = 0, device: int = 
     _check(lib().tch_run_calls(device, n, L, _ptr(calls), tau, stripe, cb, None, ctypes.byref(secs),
                                ctypes.byref(tau_used), err, len(err)), err)
     return sink.H, secs.value, tau_used.value, sink
+
+
+def set_max_chunk_bytes(nbytes: int) -> None:
+    """Split solver operands along K into allocations of at most nbytes (0 = one)."""
+    lib().tch_set_max_chunk_bytes(int(nbytes))
 
 
 def set_tau_model(gemm_rate: float, rare_rate: float) -> None:

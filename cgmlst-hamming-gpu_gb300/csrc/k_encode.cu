@@ -164,18 +164,17 @@ __global__ void cell_rank_kernel(const uint64_t* __restrict__ calls, int n, int 
 }
 
 __global__ void pack_x_kernel(const uint16_t* __restrict__ x, int n, int L, const uint64_t* __restrict__ cnt_off,
-                              const int32_t* __restrict__ col_flat, const uint32_t* __restrict__ base, uint8_t* X,
-                              int kb, int kp, uint8_t one) {
+                              const int32_t* __restrict__ col_flat, const uint32_t* __restrict__ base, KChunks X,
+                              int kp, uint8_t one) {
     const size_t total = (size_t)n * L;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
         const size_t i = t / L;
         const int k = (int)(t % L);
         const int a = x[t];
         if (!a) continue;
-        uint8_t* row = X + i * (size_t)kb;
-        row[k] = one;
+        *X.at(i, k) = one;
         const int32_t c = col_flat[cnt_off[k] + a];
-        if (c >= 0) row[kp + base[k] + c] = one;
+        if (c >= 0) *X.at(i, kp + (int)base[k] + c) = one;
     }
 }
 
@@ -369,7 +368,7 @@ int choose_tau_gb300(const std::vector<uint32_t>& cnt_flat, const std::vector<ui
 }
 
 int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_req, const TauModel& model,
-                     bool verbose, DeviceEncoding* out, Err& e) {
+                     bool verbose, size_t max_chunk_bytes, DeviceEncoding* out, Err& e) {
     int sms = 0, hflag = 0;
     size_t freeb = 0, totb = 0, tmp_bytes = 0;
     int logC = 10;
@@ -516,10 +515,20 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
 
         mark("tau and column maps");
         // ---- 4: operand rows
-        TCH_CK(e, dalloc(&out->X, out->x_rows * (size_t)out->kb, &out->bytes));
-        TCH_CK(e, cudaMemset(out->X, 0, out->x_rows * (size_t)out->kb));
-        pack_x_kernel<<<grid_for((size_t)n * L, sms), 256>>>(out->x, n, L, cnt_off_d, col_d, base_d, out->X, out->kb,
-                                                             out->kp, 0x38);
+        {
+            const int w = chunk_width_for(out->kb, out->x_rows, max_chunk_bytes);
+            if (!w) { e.set("the operand needs more than %d K chunks of %zu bytes", kMaxKChunks, max_chunk_bytes); goto fail; }
+            out->X.kb = out->kb;
+            out->X.width = w;
+            out->X.n = (out->kb + w - 1) / w;
+            for (int c = 0; c < out->X.n; c++) {
+                const size_t bytes = out->x_rows * (size_t)out->X.width_of(c);
+                TCH_CK(e, dalloc(&out->X.p[c], bytes, &out->bytes));
+                TCH_CK(e, cudaMemset(out->X.p[c], 0, bytes));
+            }
+        }
+        pack_x_kernel<<<grid_for((size_t)n * L, sms), 256>>>(out->x, n, L, cnt_off_d, col_d, base_d, out->X, out->kp,
+                                                             0x38);
         TCH_CK(e, cudaGetLastError());
 
         mark("operand rows");
@@ -595,11 +604,11 @@ fail:
 
 void free_device_encoding(DeviceEncoding* d) {
     cudaFree(d->x);
-    cudaFree(d->X);
+    for (int c = 0; c < d->X.n; c++) cudaFree(d->X.p[c]);
     cudaFree(d->start);
     cudaFree(d->js);
     d->x = nullptr;
-    d->X = nullptr;
+    d->X = KChunks();
     d->start = d->js = nullptr;
 }
 

@@ -128,6 +128,15 @@ __device__ bool tile_coords(const TileSpace& ts, const GroupTable& gt, int t, in
     return true;
 }
 
+// Tensor maps of every K chunk of the operand: A boxes (128 rows) and B boxes
+// (256 / CM rows), and the 128-byte K blocks of each chunk.
+struct TcMaps {
+    CUtensorMap a[kMaxKChunks];
+    CUtensorMap b[kMaxKChunks];
+    int kblocks[kMaxKChunks];
+    int n;
+};
+
 struct TcParams {
     int n, r0, rows;
     int kblocks, kblocks_p;  // K stages in total and in the presence part
@@ -154,7 +163,7 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__
 
 template <int KIND, int CM>
 __global__ void __launch_bounds__(THREADS, 1)
-tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+tc_stripe_kernel(const __grid_constant__ TcMaps maps,
                  const TcParams p) {
     static_assert(CM == 1 || CM == 2, "cluster of 1 or 2 CTAs");
     constexpr int B_PART = B_BYTES / CM;  // bytes of the B tile this CTA loads per stage
@@ -190,8 +199,10 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
         mbar_init(drain, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_a) : "memory");
-        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&map_b) : "memory");
+        for (int c = 0; c < maps.n; c++) {
+            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&maps.a[c]) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&maps.b[c]) : "memory");
+        }
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -219,15 +230,17 @@ tc_stripe_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constan
                 if (!tile_coords(p.ts, p.gt, t, &sr, &bj)) break;
                 const int bi = sr * CM + (int)rank;
                 const int y_a = p.r0 + bi * BM, y_b = p.r0 + bj * BN + (int)rank * (BN / CM);
+                int ch = 0, kbl = 0;  // K chunk and block inside it
                 for (int kb = 0; kb < p.kblocks; kb++) {
                     if (!mbar_wait(&empty[s], ph ^ 1, abort_flag, p.err)) { ok = false; break; }
                     mbar_expect_tx(&full[s], STAGE_BYTES);  // A + both halves of B land here
-                    tma_load_2d(&map_a, &full[s], stage_a + s * A_BYTES, kb * BK, y_a);
+                    tma_load_2d(&maps.a[ch], &full[s], stage_a + s * A_BYTES, kbl * BK, y_a);
                     if (CM == 1)
-                        tma_load_2d(&map_b, &full[s], stage_b + s * B_BYTES, kb * BK, y_b);
+                        tma_load_2d(&maps.b[ch], &full[s], stage_b + s * B_BYTES, kbl * BK, y_b);
                     else
-                        tma_load_2d_multicast(&map_b, &full[s], stage_b + s * B_BYTES + rank * B_PART, kb * BK, y_b,
-                                              (uint16_t)((1u << CM) - 1));
+                        tma_load_2d_multicast(&maps.b[ch], &full[s], stage_b + s * B_BYTES + rank * B_PART, kbl * BK,
+                                              y_b, (uint16_t)((1u << CM) - 1));
+                    if (++kbl == maps.kblocks[ch]) kbl = 0, ch++;
                     issued[s] = 1;
                     issued_ph[s] = ph;
                     if (++s == STAGES) s = 0, ph ^= 1;
@@ -454,9 +467,24 @@ cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCS
     }
     if ((ops.kb % BK) || (ops.kp % BK) || ops.kb <= 0) return cudaErrorInvalidValue;
     if ((a.ldo & 1) || ((uintptr_t)a.out & 3)) return cudaErrorInvalidValue;
-    CUtensorMap ma, mb;
-    if (!make_map(&ma, ops.X, ops.n_rows, ops.kb, BM) || !make_map(&mb, xb, ops.n_rows, ops.kb, BN / CM))
-        return cudaErrorInvalidValue;
+    (void)xb;
+    KChunks ch = ops.chunks;
+    if (ch.n == 0) {  // one allocation
+        ch.p[0] = const_cast<uint8_t*>(ops.X);
+        ch.n = 1;
+        ch.width = ops.kb;
+        ch.kb = ops.kb;
+    }
+    if (ch.kb != ops.kb || (ch.width % BK)) return cudaErrorInvalidValue;
+    TcMaps maps;
+    maps.n = ch.n;
+    for (int c = 0; c < ch.n; c++) {
+        const int wc = ch.width_of(c);
+        if (wc <= 0 || (wc % BK)) return cudaErrorInvalidValue;
+        if (!make_map(&maps.a[c], ch.p[c], ops.n_rows, wc, BM) || !make_map(&maps.b[c], ch.p[c], ops.n_rows, wc, BN / CM))
+            return cudaErrorInvalidValue;
+        maps.kblocks[c] = wc / BK;
+    }
     TcParams p;
     p.n = a.n;
     p.r0 = a.r0;
@@ -488,7 +516,7 @@ cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCS
     if (p.num_tiles == 0) return cudaSuccess;
     const int clusters = std::min(p.num_tiles, CM > 1 ? max_clusters : std::max(num_sms, 1));
     cfg.gridDim = dim3(CM * clusters);
-    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, ma, mb, p);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, maps, p);
     if (e != cudaSuccess) return e;
     if (rare.n_rare > 0 && !rare.sorted) return launch_rare_atomic(rare, a, st);
     return cudaSuccess;

@@ -59,15 +59,44 @@ struct BitOperands {
     int wP = 0, wO = 0;
 };
 
+// The operand rows can be split along K into up to kMaxKChunks separate
+// allocations: chunk c holds columns [c * width, c * width + width_c) of every
+// row (width a multiple of 128 bytes; the last chunk may be narrower).  The
+// one-hot part then never has to fit in one allocation.
+constexpr int kMaxKChunks = 8;
+struct KChunks {
+    uint8_t* p[kMaxKChunks] = {};
+    int n = 0;      // chunks in use
+    int width = 0;  // bytes of K per chunk row
+    int kb = 0;     // bytes per full row
+    __host__ __device__ int width_of(int c) const { return c < n - 1 ? width : kb - width * (n - 1); }
+    __host__ __device__ uint8_t* at(size_t row, int col) const {
+        const int c = col / width;
+        return p[c] + row * (size_t)width_of(c) + (col - c * width);
+    }
+};
+
 // Byte operands of the tensor-core kernels: one row = [presence | one-hot],
-// each part padded to a multiple of 128 bytes, row stride kb bytes.
+// each part padded to a multiple of 128 bytes, row length kb bytes.
 struct ByteOperands {
-    const uint8_t* X = nullptr;  // n_rows x kb bytes (element encoding per kernel)
+    const uint8_t* X = nullptr;  // single-chunk operand (used when chunks.n == 0)
     size_t n_rows = 0;           // multiple of 256
     int kb = 0;                  // bytes per row
     int kp = 0;                  // presence bytes (prefix of the row)
     int elem_shift = 0;          // log2(elements per byte) for the kernel's type (0 here)
+    KChunks chunks;              // K-split operand (chunks.n > 0)
 };
+
+// Splits kb bytes of K into chunks of at most max_bytes per chunk for `rows`
+// rows (0 = one chunk); returns the chunk width, or 0 if more than
+// kMaxKChunks chunks would be needed.
+inline int chunk_width_for(int kb, size_t rows, size_t max_bytes) {
+    if (!max_bytes || (size_t)kb * rows <= max_bytes) return kb;
+    size_t w = max_bytes / std::max<size_t>(rows, 1) / 128 * 128;
+    if (w < 128) w = 128;
+    const size_t n = ((size_t)kb + w - 1) / w;
+    return n > (size_t)kMaxKChunks ? 0 : (int)w;
+}
 
 struct StripeArgs {
     int n = 0, r0 = 0, rows = 0;
@@ -93,6 +122,10 @@ cudaError_t launch_rare_check_sorted(const RareCSR& rare, int n, int* d_flag, cu
 cudaError_t launch_expand_bits(const BitOperands& bits, int n, size_t n_rows, uint8_t* X, int kb, int kp,
                                int k_presence_bits, int k_onehot_bits, uint8_t one, uint8_t one_neg,
                                cudaStream_t st);
+// The same into a K-chunked operand.
+cudaError_t launch_expand_bits_chunked(const BitOperands& bits, int n, size_t n_rows, const KChunks& X, int kp,
+                                       int k_presence_bits, int k_onehot_bits, uint8_t one, uint8_t one_neg,
+                                       cudaStream_t st);
 
 // ---- k_tc.cu ----------------------------------------------------------------------
 bool tc_kernel_compiled(int kernel);
@@ -111,7 +144,7 @@ struct DeviceEncoding {
     int n = 0, L = 0, tau = 0;
     size_t D = 0;             // frequent one-hot columns
     uint16_t* x = nullptr;    // n x L ranks
-    uint8_t* X = nullptr;     // x_rows x kb e4m3 operand rows
+    KChunks X;                // x_rows x kb e4m3 operand rows, split along K
     size_t x_rows = 0;
     int kb = 0, kp = 0;
     uint32_t* start = nullptr;  // n + 1
@@ -121,7 +154,7 @@ struct DeviceEncoding {
 };
 
 int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_req, const TauModel& model,
-                     bool verbose, DeviceEncoding* out, Err& e);
+                     bool verbose, size_t max_chunk_bytes, DeviceEncoding* out, Err& e);
 void free_device_encoding(DeviceEncoding* d);
 
 }  // namespace tch

@@ -41,6 +41,19 @@ int Err::set(const char* fmt, ...) {
 
 static int g_kernel = -1;  // process default, resolved lazily
 
+// Largest single allocation of the operand rows (bytes); 0 = one allocation.
+// Set by tch_set_max_chunk_bytes or TCH_MAX_CHUNK_BYTES.
+static long long g_max_chunk = -1;
+
+static size_t max_chunk_bytes() {
+    if (g_max_chunk < 0) {
+        const char* v = getenv("TCH_MAX_CHUNK_BYTES");
+        g_max_chunk = v ? atoll(v) : 0;
+        if (g_max_chunk < 0) g_max_chunk = 0;
+    }
+    return (size_t)g_max_chunk;
+}
+
 static const char* kKernelNames[TCH_KERNEL_COUNT] = {"auto", "popc", "mma_b1", "tc_f8", "tc_i8", "tc_f16"};
 
 static bool kernel_compiled(int k) {
@@ -88,8 +101,7 @@ struct tch_solver {
     size_t n_pad = 0, K1 = 0, K2 = 0, D = 0;
     uint32_t* dP = nullptr;  // bit operands (popc kernel)
     uint32_t* dO = nullptr;
-    uint8_t* dX = nullptr;   // byte operands (tensor-core kernels)
-    uint8_t* dXneg = nullptr;
+    KChunks xc;              // byte operands of the tensor-core kernels, split along K
     size_t x_rows = 0;
     int kb = 0, kp = 0;
     uint32_t* dStart = nullptr;
@@ -123,8 +135,7 @@ static void solver_free(tch_solver* s) {
     cudaSetDevice(s->device);
     cudaFree(s->dP);
     cudaFree(s->dO);
-    cudaFree(s->dX);
-    cudaFree(s->dXneg);
+    for (int c = 0; c < s->xc.n; c++) cudaFree(s->xc.p[c]);
     cudaFree(s->dStart);
     cudaFree(s->dJs);
     cudaFree(s->dErr);
@@ -193,16 +204,20 @@ static int solver_from_bits(int device, int n, size_t n_pad, const uint8_t* O, s
         bits.wO = (int)(K1 / 32);
         uint8_t one, neg;
         tc_encoding(kernel, &one, &neg);
+        (void)neg;  // the one-hot part is subtracted by the MMA's negate-B bit
         s->kp = (int)up(K2, 128);
         s->kb = s->kp + (int)up(K1, 128);
         s->x_rows = up((size_t)std::max(n, 1), 256);
-        TCH_CK(e, dmalloc(s, (void**)&s->dX, s->x_rows * (size_t)s->kb));
-        TCH_CK(e, launch_expand_bits(bits, n, s->x_rows, s->dX, s->kb, s->kp, (int)K2, (int)K1, one, one, 0));
-        if (kernel == TCH_KERNEL_TC_I8) {  // no negate bit for integer MMA: subtract through B
-            TCH_CK(e, dmalloc(s, (void**)&s->dXneg, s->x_rows * (size_t)s->kb));
-            TCH_CK(e, launch_expand_bits(bits, n, s->x_rows, s->dXneg, s->kb, s->kp, (int)K2, (int)K1, one, neg,
-                                         0));
+        {
+            const int w = chunk_width_for(s->kb, s->x_rows, max_chunk_bytes());
+            if (!w) { e.set("the operand needs more than %d K chunks", kMaxKChunks); goto fail; }
+            s->xc.kb = s->kb;
+            s->xc.width = w;
+            s->xc.n = (s->kb + w - 1) / w;
+            for (int c = 0; c < s->xc.n; c++)
+                TCH_CK(e, dmalloc(s, (void**)&s->xc.p[c], s->x_rows * (size_t)s->xc.width_of(c)));
         }
+        TCH_CK(e, launch_expand_bits_chunked(bits, n, s->x_rows, s->xc, s->kp, (int)K2, (int)K1, one, one, 0));
         TCH_CK(e, cudaDeviceSynchronize());
         cudaFree(s->dP);
         cudaFree(s->dO);
@@ -300,13 +315,13 @@ static int solver_from_calls(int device, int n, int L, const uint64_t* calls, in
     } else {
         TCH_CK(e, cudaMemset(d_calls, 0, std::max<size_t>((size_t)n, 1) * 8));
     }
-    if (encode_on_device(device, n, Le, d_calls, tau, g_tau_model, verbose, &enc, e)) goto fail;
+    if (encode_on_device(device, n, Le, d_calls, tau, g_tau_model, verbose, max_chunk_bytes(), &enc, e)) goto fail;
     cudaFree(d_calls);
     d_calls = nullptr;
     cudaFree(enc.x);
     enc.bytes -= (size_t)n * Le * 2;
     enc.x = nullptr;
-    s->dX = enc.X;
+    s->xc = enc.X;
     s->x_rows = enc.x_rows;
     s->kb = enc.kb;
     s->kp = enc.kp;
@@ -362,11 +377,12 @@ static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_
         ce = launch_popc_stripe(ops, rare, a, st);
     } else {
         ByteOperands ops;
-        ops.X = s->dX;
+        ops.X = s->xc.p[0];
+        ops.chunks = s->xc;
         ops.n_rows = s->x_rows;
         ops.kb = s->kb;
         ops.kp = s->kp;
-        ce = launch_tc_stripe(s->kernel, ops, s->dXneg, rare, a, s->num_sms, st);
+        ce = launch_tc_stripe(s->kernel, ops, nullptr, rare, a, s->num_sms, st);
     }
     if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
     return 0;
@@ -454,8 +470,10 @@ static bool host_pages_visible(int device) {
     if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) return false;
     if (cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess)
         return false;
-    const char* off = getenv("TCH_NO_HOST_PULL");  // force the staged copy
-    return a == 1 && b == 1 && !(off && off[0] == '1');
+    // opt-in: measured on GB300 the pull competes with the stripe kernel and
+    // ends slower than the staged copy overlapped with it
+    const char* on = getenv("TCH_HOST_PULL");
+    return a == 1 && b == 1 && on && on[0] == '1';
 }
 
 static cudaError_t upload_u32(uint32_t* dst, const uint32_t* src, size_t count, bool pull, int sms,
@@ -662,6 +680,11 @@ int tch_run_calls(int device, int n, int L, const uint64_t* calls, int tau, int 
     return rc;
 }
 
+int tch_set_max_chunk_bytes(size_t bytes) {
+    g_max_chunk = (long long)bytes;
+    return 0;
+}
+
 int tch_set_tau_model(double gemm_rate, double rare_rate) {
     if (!(gemm_rate > 0) || !(rare_rate > 0)) return 1;
     g_tau_model.gemm_rate = gemm_rate;
@@ -683,6 +706,7 @@ int tch_solver_info(const tch_solver* s, tch_info* info) {
     info->n_rare = s->n_rare;
     info->rare_sorted = s->sorted ? 1 : 0;
     info->device_bytes = s->bytes;
+    info->k_chunks = s->xc.n;
     return 0;
 }
 

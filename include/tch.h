@@ -108,7 +108,15 @@ typedef struct tch_info {
     size_t n_rare;     /* rare equal pairs */
     int rare_sorted;   /* 1 if every row's partner list is ascending */
     size_t device_bytes; /* device memory held by the solver */
+    int k_chunks;        /* separate allocations the operand rows are split into along K */
 } tch_info;
+
+/* Largest single device allocation of a solver's operand rows, in bytes
+ * (0 = no limit, the default; also TCH_MAX_CHUNK_BYTES).  Above it the rows
+ * are split along K into up to 8 allocations that the contraction kernel
+ * streams in turn, so the one-hot matrix never has to fit in one buffer.
+ * Applies to solvers created afterwards. */
+int tch_set_max_chunk_bytes(size_t bytes);
 
 /* A solver holds one profile set on one device: the operands of the two
  * contractions and the rare-pair CSR, resident in device memory. */

@@ -94,8 +94,8 @@ def test_host_rare_fallback(tch, checkpy_inputs):
 @pytest.mark.parametrize("pull", ["1", "0"])
 def test_tch_run_partner_upload_paths(tch, checkpy_inputs, pull):
     """tch_run uploads each stripe's partner lists while the previous stripe
-    computes: read by the GPU from host memory where the platform allows it,
-    else staged by cudaMemcpyAsync (TCH_NO_HOST_PULL=1).  Both in any order."""
+    computes: staged by cudaMemcpyAsync, or read by the GPU from host memory
+    (TCH_HOST_PULL=1, where the platform allows it).  Both in any order."""
     c, A, x, ref = checkpy_inputs[2]
     xr, nd = tch.dense_ranks(A.astype(np.uint64))
     enc = tch.encode_host(xr, nd, 64)
@@ -103,11 +103,11 @@ def test_tch_run_partner_upload_paths(tch, checkpy_inputs, pull):
     for i in range(0, enc.n, 3):  # every third row unsorted
         seg = enc.js[enc.start[i]:enc.start[i + 1]]
         rng.shuffle(seg)
-    os.environ["TCH_NO_HOST_PULL"] = "0" if pull == "1" else "1"
+    os.environ["TCH_HOST_PULL"] = pull
     try:
         H, _, rare_gpu, _ = tch.run(enc, stripe=136)
     finally:
-        del os.environ["TCH_NO_HOST_PULL"]
+        del os.environ["TCH_HOST_PULL"]
     assert rare_gpu == 1
     upper_equal(H, ref)
 
@@ -214,3 +214,34 @@ def test_device_stripe_api(tch):
             for r in range(rows):
                 i = r0 + r
                 np.testing.assert_array_equal(got[r, i - r0 + 1: n - r0], ref[i, i + 1:])
+
+
+def test_k_chunked_operand(tch):
+    """The operand rows split along K into several allocations (spec K
+    tiling): same distances as one allocation, for both solver builds."""
+    rng = np.random.default_rng(17)
+    n, L = 900, 300
+    A = rng.integers(1, 60, size=(n, L)).astype(np.uint64)
+    A[rng.random((n, L)) < 0.03] = 0
+    x, nd = tch.dense_ranks(A)
+    ref = oracle.hamming(x)
+    enc = tch.encode_host(x, nd, 4)
+    try:
+        # rows are ~18.4 KB long and padded to 1024 rows: chunks of 2.5 KB / 8 KB of K
+        for limit in (1024 * 2560, 1024 * 8192):
+            tch.set_max_chunk_bytes(limit)
+            with tch.Solver.from_encoding(enc, kernel="tc_f8") as s:
+                info = s.info()
+                H, _ = s.run(256)
+            assert 1 < info["k_chunks"] <= 8
+            upper_equal(H, ref)
+            with tch.Solver.from_calls(A, tau=4) as s:
+                info = s.info()
+                H, _ = s.run(300)
+            assert 1 < info["k_chunks"] <= 8
+            upper_equal(H, ref)
+        tch.set_max_chunk_bytes(1024)  # would need far more than 8 chunks
+        with pytest.raises(tch.TchError, match="chunks"):
+            tch.Solver.from_encoding(enc, kernel="tc_f8")
+    finally:
+        tch.set_max_chunk_bytes(0)
