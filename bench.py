@@ -7,15 +7,19 @@ median 60, tail to ~2 500; 1-5% missing per locus; 5% hashed 64-bit ids).  One
 step = the whole upper triangle of the u16 distance matrix,
 n (n - 1) / 2 = 1 984 783 510 exact pairs.
 
-    value  device-resident: operands and rare-pair CSR already in HBM, the
-           step is the tensor-core stripe kernel over all tiles of the upper
-           triangle (u16 output in HBM).  Inputs (X ~3 GB) exceed L2.
+    value  device-resident: operands and rare groups already in HBM (device
+           encoder), the step is one tch_solver_stripe over the whole upper
+           triangle: the dense rare-count kernel (u16 block of the stripe),
+           then the tensor-core tile pass that subtracts it (u16 output in
+           HBM).  Inputs (operands ~1 GB, rare counts 8 GB) exceed L2.
     e2e    the reference-facing C ABI, tch_run, with host buffers: H2D of the
            bit-packed operands and CSR, device expansion, stripes, D2H of every
            stripe into pinned memory and the stripe callback, per step.
-    roofline   tensor-pipe bound: algorithmic MACs (unpadded K = L + D per
-           pair, 2 ops per MAC) per launch / CUDA-event duration of the
-           launch, against the measured fp8 tcgen05 peak of this GPU.
+    roofline   the tile-pass kernel (tc_stripe_kernel), tensor-pipe bound:
+           algorithmic MACs (unpadded K = L + D per pair, 2 ops per MAC) per
+           launch / CUDA-event duration of that launch alone (the two passes
+           are timed apart through tch_solver_rare_counts and
+           tch_solver_stripe_counts), against the measured fp8 tcgen05 peak.
     cpu_baseline   the brute-force count of the reference's exactness check
            (the C restatement in oracle/), all host threads, bounded sample.
 
@@ -185,7 +189,7 @@ def main():
     n, L = x.shape
     pairs_total = n * (n - 1) // 2
     workload = {"workload": f"long-tail outbreak profiles {n} x {L} (synthetic, seeded)", "n": n, "loci": L,
-                "pairs": pairs_total, "tau": args.tau, "l2": "inputs larger than L2 (operands ~3 GB)"}
+                "pairs": pairs_total, "tau": args.tau, "l2": "inputs larger than L2 (operands ~1 GB + 8 GB rare counts per step)"}
     log(f"generated + ranked {n}x{L} in {time.perf_counter() - t0:.1f}s")
 
     if args.impl == "reference":
@@ -273,11 +277,36 @@ def main():
     ms_per_step = total_ms / args.steps
     value = pairs_total / (ms_per_step / 1e3)
 
-    # roofline of the stripe kernel (one launch per step)
+    # a dense-rare solver's step is two launches: the stripe's rare counts,
+    # then the tile pass that subtracts them; time them apart for the roofline
+    dense = bool(info.get("rare_dense"))
+    launches_per_step = 2 if dense else 1
+    split = None
+    tc_ms = statistics.median(launch_ms)
+    if dense:
+        ldr = (n - a + 255) // 256 * 256
+        rbuf = torch.empty(((b - a), ldr), dtype=torch.int16, device=f"cuda:{device}")
+        trip = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(max(args.steps, 3))]
+        for e0, e1, e2 in trip:
+            e0.record(stream)
+            solver.rare_counts(a, b - a, rbuf.data_ptr(), ldr, sp)
+            e1.record(stream)
+            solver.stripe_counts(a, b - a, out.data_ptr(), ldo, rbuf.data_ptr(), ldr, sp)
+            e2.record(stream)
+        torch.cuda.synchronize()
+        solver.check()
+        rare_ms = statistics.median(e0.elapsed_time(e1) for e0, e1, _ in trip)
+        tc_ms = statistics.median(e1.elapsed_time(e2) for _, e1, e2 in trip)
+        split = {"rare_counts_ms": rare_ms, "tile_pass_ms": tc_ms, "rare_pairs": int(info["n_rare"]),
+                 "rare_pairs_per_s": info["n_rare"] * (b - a) / max(n, 1) / (rare_ms / 1e3)}
+        del rbuf
+        log("split:", split)
+
+    # roofline of the tile-pass kernel (tc_stripe_kernel)
     k_alg = L + int(info["d_onehot"])
     my_pairs = sum(n - 1 - i for i in range(a, b))
     ops_per_launch = 2.0 * my_pairs * k_alg
-    achieved = ops_per_launch / (statistics.median(launch_ms) / 1e3) / 1e12
+    achieved = ops_per_launch / (tc_ms / 1e3) / 1e12
     peak_info = tc_fp8_peak(tch) if rank == 0 else {}
     mp = measured_peaks()
     peak = peak_info.get("tc_f8_tflops")
@@ -360,7 +389,8 @@ def main():
                 "scaling": "strong", "vs_baseline": None, "dtype": "fp8(e4m3 0/1) -> fp32 exact ints -> u16",
                 "data": "synthetic", "config": dict(workload, kernel=info["kernel"], stripe_e2e=args.stripe,
                                                     parallelism=f"row shares x{ws}"),
-                "gpu_launches": args.steps, "clocks": ck, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": args.steps * launches_per_step, "step_split": split,
+                "clocks": ck, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "e2e_device_encoder": e2e_calls,
                 "peak_probe": peak_info}
         print(json.dumps(line), flush=True)

@@ -40,7 +40,8 @@ class Info(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int), ("L", ctypes.c_int), ("tau", ctypes.c_int), ("kernel", ctypes.c_int),
                 ("n_pad", ctypes.c_size_t), ("k_presence", ctypes.c_size_t), ("k_onehot", ctypes.c_size_t),
                 ("d_onehot", ctypes.c_size_t), ("n_rare", ctypes.c_size_t), ("rare_sorted", ctypes.c_int),
-                ("device_bytes", ctypes.c_size_t), ("k_chunks", ctypes.c_int)]
+                ("device_bytes", ctypes.c_size_t), ("k_chunks", ctypes.c_int),
+                ("rare_dense", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -91,6 +92,11 @@ def lib():
         L.tch_solver_stripe.argtypes = [c_void, c_int, c_int, c_void, c_size, c_void, c_char_p, c_int]
         L.tch_solver_stripe.restype = c_int
         L.tch_solver_check.argtypes, L.tch_solver_check.restype = [c_void, c_char_p, c_int], c_int
+        L.tch_solver_rare_counts.argtypes = [c_void, c_int, c_int, c_void, c_size, c_void, c_char_p, c_int]
+        L.tch_solver_rare_counts.restype = c_int
+        L.tch_solver_stripe_counts.argtypes = [c_void, c_int, c_int, c_void, c_size, c_void, c_size, c_void,
+                                               c_char_p, c_int]
+        L.tch_solver_stripe_counts.restype = c_int
         L.tch_solver_run.argtypes = [c_void, c_int, CB, c_void, P(c_double), c_char_p, c_int]
         L.tch_solver_run.restype = c_int
         L.tch_solver_destroy.argtypes, L.tch_solver_destroy.restype = [c_void], None
@@ -109,6 +115,8 @@ def lib():
         L.tch_run_calls.restype = c_int
         L.tch_set_tau_model.argtypes, L.tch_set_tau_model.restype = [c_double, c_double], c_int
         L.tch_set_max_chunk_bytes.argtypes, L.tch_set_max_chunk_bytes.restype = [c_size], c_int
+        L.tch_set_dense_rare_rate.argtypes, L.tch_set_dense_rare_rate.restype = [c_double], c_int
+        L.tch_set_rare_term.argtypes, L.tch_set_rare_term.restype = [c_int], c_int
         _lib = L
     return _lib
 
@@ -264,9 +272,17 @@ def set_max_chunk_bytes(nbytes: int) -> None:
     lib().tch_set_max_chunk_bytes(int(nbytes))
 
 
-def set_tau_model(gemm_rate: float, rare_rate: float) -> None:
+def set_tau_model(gemm_rate: float, rare_rate: float, dense_rare_rate: float | None = None) -> None:
     if lib().tch_set_tau_model(gemm_rate, rare_rate):
         raise TchError("rates must be positive")
+    if dense_rare_rate is not None and lib().tch_set_dense_rare_rate(dense_rare_rate):
+        raise TchError("rates must be positive")
+
+
+def set_rare_term(dense: bool) -> None:
+    """Rare term of solvers built from calls: dense per-stripe counts from the
+    rare groups (True, default) or per-row pair lists (False)."""
+    lib().tch_set_rare_term(1 if dense else 0)
 
 
 # ---------------------------------------------------------------------------------------
@@ -307,6 +323,19 @@ class Solver:
         err = _errbuf()
         _check(lib().tch_solver_stripe(self._h, r0, rows, ctypes.c_void_p(d_out), ldo,
                                        ctypes.c_void_p(stream) if stream else None, err, len(err)), err)
+
+    def rare_counts(self, r0: int, rows: int, d_R: int, ldr: int, stream: int = 0):
+        """Dense rare counts of a stripe into device memory at d_R (row stride
+        ldr u16, ldr >= up(n - r0, 256)); dense-rare solvers only."""
+        err = _errbuf()
+        _check(lib().tch_solver_rare_counts(self._h, r0, rows, ctypes.c_void_p(d_R), ldr,
+                                            ctypes.c_void_p(stream) if stream else None, err, len(err)), err)
+
+    def stripe_counts(self, r0: int, rows: int, d_out: int, ldo: int, d_R: int, ldr: int, stream: int = 0):
+        """The stripe's tile pass with the rare term read from d_R."""
+        err = _errbuf()
+        _check(lib().tch_solver_stripe_counts(self._h, r0, rows, ctypes.c_void_p(d_out), ldo, ctypes.c_void_p(d_R),
+                                              ldr, ctypes.c_void_p(stream) if stream else None, err, len(err)), err)
 
     def check(self):
         err = _errbuf()

@@ -193,10 +193,12 @@ __global__ void group_fill_kernel(const uint16_t* __restrict__ x, int n, int L, 
 }
 
 // One CTA per rare group: rows are distinct, so a row's place is the number
-// of smaller rows in the group.
+// of smaller rows in the group.  groups holds (first, end, locus) triples;
+// mpos (optional, n x L) receives every row's own index in `sorted`.
 __global__ void group_sort_kernel(const uint64_t* __restrict__ groups, const uint32_t* __restrict__ members,
-                                  uint32_t* sorted) {
-    const uint64_t g0 = groups[2 * blockIdx.x], g1 = groups[2 * blockIdx.x + 1];
+                                  uint32_t* sorted, uint32_t* mpos, int L) {
+    const uint64_t g0 = groups[3 * blockIdx.x], g1 = groups[3 * blockIdx.x + 1];
+    const int locus = (int)groups[3 * blockIdx.x + 2];
     const uint32_t g = (uint32_t)(g1 - g0);
     __shared__ uint32_t tile[4096];
     for (uint32_t e0 = 0; e0 < g; e0 += 4 * blockDim.x) {
@@ -221,7 +223,10 @@ __global__ void group_sort_kernel(const uint64_t* __restrict__ groups, const uin
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const uint32_t e = e0 + q * blockDim.x + threadIdx.x;
-            if (e < g) sorted[g0 + r[q]] = mine[q];
+            if (e < g) {
+                sorted[g0 + r[q]] = mine[q];
+                if (mpos) mpos[(size_t)mine[q] * L + locus] = (uint32_t)(g0 + r[q]);
+            }
         }
     }
 }
@@ -334,28 +339,41 @@ int grid_for(size_t total, int sms) { return (int)std::min<size_t>((total + 255)
 }  // namespace
 
 // Analytic cost of tau on GB300: tensor-core time for the one-hot columns plus
-// the fused rare subtraction, subject to device memory.
+// the rare term (fused pair-list walk, or the dense rare-count build), subject
+// to device memory.
 int choose_tau_gb300(const std::vector<uint32_t>& cnt_flat, const std::vector<uint64_t>& off, int n, int L,
-                     size_t free_bytes, const TauModel& m, bool verbose) {
+                     size_t free_bytes, const TauModel& m, bool dense, bool verbose) {
     std::vector<double> cs;
     for (int k = 0; k < L; k++)
         for (uint64_t q = off[k] + 1; q < off[k + 1]; q++)
             if (cnt_flat[q]) cs.push_back((double)cnt_flat[q]);
     const double pairs = (double)n * (double)(n - 1) / 2.0;
     const size_t rows = up((size_t)std::max(n, 1), 256), kp = up((size_t)L, 128);
+    const double nl = (double)n * (double)L;
     int best = 0;
     double best_t = 1e300;
-    for (int tau = 2; tau <= 4096; tau *= 2) {
+    for (int tau = 2; tau <= (dense ? 65536 : 4096); tau *= 2) {
         size_t d = 0;
-        double r = 0;
+        double r = 0, cells = 0;
         for (double v : cs) {
             if (v >= tau) d++;
-            else r += v * (v - 1.0) / 2.0;
+            else if (v >= 2) {
+                r += v * (v - 1.0) / 2.0;
+                cells += v;
+            }
         }
         const double kb = (double)(kp + up(d, 128));
-        const double mem = (double)rows * kb + 4.0 * (r + n + 1.0) + 2.0 * (double)n * (double)up((size_t)n, 8) / 4;
-        const double t = pairs * kb / m.gemm_rate + r / m.rare_rate;
-        const bool fits = mem <= (double)free_bytes && r < 4.0e9;
+        double mem, t;
+        bool fits;
+        if (dense) {  // ranks, own positions, group members (a stripe's counts come later)
+            mem = (double)rows * kb + nl * 6.0 + 4.0 * cells;
+            t = pairs * kb / m.gemm_rate + r / m.dense_rate;
+            fits = mem <= (double)free_bytes && cells < 4.0e9;
+        } else {
+            mem = (double)rows * kb + 4.0 * (r + n + 1.0) + 2.0 * (double)n * (double)up((size_t)n, 8) / 4;
+            t = pairs * kb / m.gemm_rate + r / m.rare_rate;
+            fits = mem <= (double)free_bytes && r < 4.0e9;
+        }
         if (verbose)
             fprintf(stderr, "  tau=%5d  one-hot=%8zu  rare=%14.0f  est %.4fs  vram %.2f GB%s\n", tau, d, r, t,
                     mem / 1e9, fits ? "" : "  (does not fit)");
@@ -368,7 +386,7 @@ int choose_tau_gb300(const std::vector<uint32_t>& cnt_flat, const std::vector<ui
 }
 
 int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_req, const TauModel& model,
-                     bool verbose, size_t max_chunk_bytes, DeviceEncoding* out, Err& e) {
+                     bool verbose, size_t max_chunk_bytes, bool dense_rare, DeviceEncoding* out, Err& e) {
     int sms = 0, hflag = 0;
     size_t freeb = 0, totb = 0, tmp_bytes = 0;
     int logC = 10;
@@ -379,7 +397,7 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
     const int nk_max = (int)std::max<size_t>(1, std::min<size_t>((size_t)L, ((size_t)2 << 30) / per_locus));
     unsigned long long* keys = nullptr;
     uint32_t *cnts = nullptr, *nd = nullptr, *list_slots = nullptr, *cnt_flat = nullptr, *gfill = nullptr;
-    uint32_t *members = nullptr, *sorted = nullptr, *row_count = nullptr, *base_d = nullptr;
+    uint32_t *members = nullptr, *sorted = nullptr, *row_count = nullptr, *base_d = nullptr, *mpos = nullptr;
     uint16_t* rank_slot = nullptr;
     unsigned long long* list_keys = nullptr;
     uint64_t *cnt_off_d = nullptr, *goff_d = nullptr, *groups_d = nullptr, *start64 = nullptr;
@@ -474,14 +492,15 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
         int tau = tau_req;
         TCH_CK(e, cudaMemGetInfo(&freeb, &totb));
         if (tau <= 0) {
-            tau = choose_tau_gb300(cnt_h, off_h, n, L, freeb, model, verbose);
+            tau = choose_tau_gb300(cnt_h, off_h, n, L, freeb, model, dense_rare, verbose);
             if (!tau) { e.set("no tau fits in %.2f GB of free device memory", freeb / 1e9); goto fail; }
         }
         out->tau = tau;
         std::vector<int32_t> col(off_h[L], -1);
         std::vector<uint32_t> base((size_t)L + 1, 0);
         std::vector<uint64_t> goff(off_h[L] + 1, 0);
-        std::vector<uint64_t> groups;
+        std::vector<uint64_t> groups;  // (first, end, locus) of every rare group
+        double n_rare_pairs = 0;
         uint64_t D = 0;
         for (int k = 0; k < L; k++) {
             base[k] = (uint32_t)D;
@@ -496,6 +515,8 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
                 if (rare) {
                     groups.push_back(goff[q]);
                     groups.push_back(goff[q + 1]);
+                    groups.push_back((uint64_t)k);
+                    n_rare_pairs += (double)c * (double)(c - 1) / 2.0;
                 }
             }
             D += d;
@@ -506,6 +527,10 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
         out->kb = out->kp + (int)up(D, 128);
         out->x_rows = up((size_t)std::max(n, 1), 256);
         const uint64_t n_members = goff[off_h[L]];
+        if (dense_rare && n_members >= (1ull << 32)) {
+            e.set("%llu rare cells: more than 2^32 (lower tau)", (unsigned long long)n_members);
+            goto fail;
+        }
         TCH_CK(e, dalloc(&col_d, off_h[L], nullptr));
         TCH_CK(e, dalloc(&base_d, (size_t)L + 1, nullptr));
         TCH_CK(e, dalloc(&goff_d, off_h[L] + 1, nullptr));
@@ -533,11 +558,12 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
 
         mark("operand rows");
         // ---- 5: rare groups, sorted
-        const size_t ngroups = groups.size() / 2;
+        const size_t ngroups = groups.size() / 3;
         TCH_CK(e, dalloc(&members, n_members, &tmp_bytes));
         TCH_CK(e, dalloc(&sorted, n_members, &tmp_bytes));
         TCH_CK(e, dalloc(&gfill, off_h[L], &tmp_bytes));
         TCH_CK(e, cudaMemset(gfill, 0, std::max<uint64_t>(off_h[L], 1) * 4));
+        if (dense_rare) TCH_CK(e, dalloc(&mpos, (size_t)n * L, &tmp_bytes));
         if (ngroups) {
             TCH_CK(e, dalloc(&groups_d, groups.size(), &tmp_bytes));
             TCH_CK(e, cudaMemcpy(groups_d, groups.data(), groups.size() * 8, cudaMemcpyHostToDevice));
@@ -545,12 +571,27 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
             TCH_CK(e, cudaGetLastError());
             for (size_t g0 = 0; g0 < ngroups; g0 += 65535) {
                 const unsigned gcount = (unsigned)std::min<size_t>(65535, ngroups - g0);
-                group_sort_kernel<<<gcount, 256>>>(groups_d + 2 * g0, members, sorted);
+                group_sort_kernel<<<gcount, 256>>>(groups_d + 3 * g0, members, sorted, mpos, L);
                 TCH_CK(e, cudaGetLastError());
             }
         }
 
         mark("rare groups");
+        if (dense_rare) {  // the groups themselves are the rare term; no pair list
+            TCH_CK(e, cudaDeviceSynchronize());
+            out->dense = true;
+            out->n_rare = (size_t)n_rare_pairs;
+            out->cnt_off = cnt_off_d;
+            out->goff = goff_d;
+            out->members = sorted;
+            out->mpos = mpos;
+            out->bytes += ((size_t)L + 1) * 8 + (off_h[L] + 1) * 8 + n_members * 4 + (size_t)n * L * 4;
+            cnt_off_d = nullptr;
+            goff_d = nullptr;
+            sorted = nullptr;
+            mpos = nullptr;
+            goto done;
+        }
         // ---- 6: CSR of rare pairs, ascending per row
         TCH_CK(e, dalloc(&row_count, (size_t)n, &tmp_bytes));
         TCH_CK(e, dalloc(&start64, (size_t)n + 1, &tmp_bytes));
@@ -590,14 +631,16 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
         TCH_CK(e, cudaDeviceSynchronize());
         mark("rare CSR (2 passes)");
     }
+done:
     cudaFree(err_d); cudaFree(nd); cudaFree(cnt_off_d); cudaFree(cnt_flat); cudaFree(col_d); cudaFree(base_d);
     cudaFree(goff_d); cudaFree(members); cudaFree(sorted); cudaFree(gfill); cudaFree(groups_d); cudaFree(row_count);
-    cudaFree(start64);
+    cudaFree(start64); cudaFree(mpos);
     return 0;
 fail:
     cudaFree(err_d); cudaFree(nd); cudaFree(cnt_off_d); cudaFree(cnt_flat); cudaFree(col_d); cudaFree(base_d);
     cudaFree(goff_d); cudaFree(members); cudaFree(sorted); cudaFree(gfill); cudaFree(groups_d); cudaFree(row_count);
     cudaFree(start64); cudaFree(keys); cudaFree(cnts); cudaFree(rank_slot); cudaFree(list_keys); cudaFree(list_slots);
+    cudaFree(mpos);
     free_device_encoding(out);
     return 1;
 }
@@ -607,9 +650,15 @@ void free_device_encoding(DeviceEncoding* d) {
     for (int c = 0; c < d->X.n; c++) cudaFree(d->X.p[c]);
     cudaFree(d->start);
     cudaFree(d->js);
+    cudaFree(d->cnt_off);
+    cudaFree(d->goff);
+    cudaFree(d->members);
+    cudaFree(d->mpos);
     d->x = nullptr;
     d->X = KChunks();
     d->start = d->js = nullptr;
+    d->cnt_off = d->goff = nullptr;
+    d->members = d->mpos = nullptr;
 }
 
 }  // namespace tch

@@ -1,0 +1,215 @@
+// Dense rare counts of a stripe, built on the device from the rare groups.
+//
+// The rare term R[i, j] = #{loci k : x[i,k] == x[j,k] != 0 and that allele is
+// rare} (the reference applies it pair by pair from the host-built lists,
+// tensorcore/rs/src/main.rs:416-447 and tensorcore/rs/cuda/tch.cu:31-38).
+// Here the encoder keeps every rare allele as a group of rows (ascending)
+// plus each row's own place in its groups; row i's partners at locus k are
+// the group members after its own entry.  Per stripe this kernel counts them
+// into a u16 block laid out like the output, which the tensor-core epilogue
+// subtracts with 16-byte loads: no pair list is ever materialised.
+//
+// One CTA per stripe row (persistent over the rows).  The counters of the
+// row's columns sit in shared memory as u16 pairs (65536 columns per pass),
+// each partner adds 1 with a shared atomic, and the finished row is written
+// out with coalesced 16-byte stores.  The partner runs of up to 2048 loci are
+// laid end to end by a block-wide scan of their lengths and cut into 32 equal
+// parts, one per warp, so every warp of the CTA has the same number of
+// partners whatever the group sizes are; a warp walks its part run by run
+// with its lanes on consecutive members (coalesced loads, up to eight in
+// flight per lane).
+
+#include "tch_internal.cuh"
+
+namespace tch {
+namespace {
+
+constexpr int RD_THREADS = 1024;
+constexpr int RD_WORDS = 32768;          // u32 counter words in shared memory (128 KB)
+constexpr int RD_COLS = 2 * RD_WORDS;    // columns per pass
+constexpr int RD_LOCI = 2 * RD_THREADS;  // loci laid out per scan
+constexpr int RD_SMEM = RD_WORDS * 4 + (RD_LOCI + 1) * 4 + RD_LOCI * 4 + 32 * 4;
+constexpr unsigned FULL = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint64_t lower_bound_m(const uint32_t* __restrict__ m, uint64_t lo, uint64_t hi,
+                                                  uint32_t key) {
+    while (lo < hi) {
+        const uint64_t mid = lo + (hi - lo) / 2;
+        if (__ldg(m + mid) < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// Partner run of row i at locus k inside columns [jlo, jhi): members[lo, lo +
+// len).  a = x[i, k], mp = mpos[i, k], coff = cnt_off[k], loaded by the caller.
+__device__ __forceinline__ uint32_t partner_run(const RareGroups& g, int i, uint32_t a, uint32_t mp, uint64_t coff,
+                                                uint32_t jlo, uint32_t jhi, uint32_t* lo_out) {
+    if (!a) return 0;
+    const uint64_t q = coff + a;
+    const uint64_t g1 = __ldg(g.goff + q + 1);
+    if (g1 - __ldg(g.goff + q) < 2) return 0;  // frequent (no group) or a singleton
+    uint64_t b = (uint64_t)mp + 1, e = g1;
+    // members after i's own entry are > i; clip to the pass's columns (only a
+    // pass that starts after i + 1 or ends before n needs it)
+    if (jlo > (uint32_t)i + 1 && b < e && __ldg(g.members + b) < jlo) b = lower_bound_m(g.members, b, e, jlo);
+    if (jhi < (uint32_t)g.n && b < e && __ldg(g.members + e - 1) >= jhi) e = lower_bound_m(g.members, b, e, jhi);
+    *lo_out = (uint32_t)b;
+    return (uint32_t)(e - b);
+}
+
+// This thread's two loci of a row: ranks and own positions.
+struct CellPair {
+    uint32_t a0 = 0, a1 = 0, m0 = 0, m1 = 0;
+};
+
+__device__ __forceinline__ CellPair load_cells(const RareGroups& g, int i, int k0) {
+    CellPair c;
+    const size_t base = (size_t)i * g.L + k0;
+    if (k0 < g.L) {
+        c.a0 = g.x[base];
+        c.m0 = g.mpos[base];
+    }
+    if (k0 + 1 < g.L) {
+        c.a1 = g.x[base + 1];
+        c.m1 = g.mpos[base + 1];
+    }
+    return c;
+}
+
+__device__ __forceinline__ void count_col(uint32_t* cnt, uint32_t c) {
+    atomicAdd(cnt + (c >> 1), 1u << ((c & 1u) * 16u));
+}
+
+__global__ void __launch_bounds__(RD_THREADS, 1)
+    rare_dense_kernel(const RareGroups g, int r0, int rows, uint16_t* __restrict__ R, size_t ldr, int cend) {
+    extern __shared__ uint4 smem_rd[];
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(smem_rd);
+    uint32_t* pre = cnt + RD_WORDS;        // RD_LOCI + 1: exclusive prefix of the run lengths
+    uint32_t* run = pre + RD_LOCI + 1;     // RD_LOCI: first member index of each run
+    uint32_t* wsum = run + RD_LOCI;        // 32: per-warp totals of the scan
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NWARPS = RD_THREADS / 32;
+    const int n = g.n, L = g.L;
+    // with every locus in one scan (L <= RD_LOCI) a thread keeps the same two
+    // loci for all rows: their count offsets stay in registers and the next
+    // row's ranks and positions are fetched while this row is counted
+    const bool one_chunk = L <= RD_LOCI;
+    uint64_t co0 = 0, co1 = 0;
+    if (one_chunk) {
+        if (2 * tid < L) co0 = g.cnt_off[2 * tid];
+        if (2 * tid + 1 < L) co1 = g.cnt_off[2 * tid + 1];
+    }
+    CellPair next;
+    if (one_chunk && (int)blockIdx.x < rows) next = load_cells(g, r0 + (int)blockIdx.x, 2 * tid);
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int i = r0 + r;
+        const CellPair cur = next;
+        if (one_chunk && r + (int)gridDim.x < rows) next = load_cells(g, i + (int)gridDim.x, 2 * tid);
+        const int cbeg = r0 + (r & ~(kRareDenseAlign - 1));  // first column of the row's diagonal tile
+        uint4* Rrow = reinterpret_cast<uint4*>(R + (size_t)r * ldr + (size_t)(cbeg - r0));
+        for (int wb = cbeg; wb < cend; wb += RD_COLS) {
+            const int we = min(cend, wb + RD_COLS);
+            const int nq = (we - wb) >> 3;  // uint4 of counters (8 columns each); we - wb is a multiple of 256
+            for (int w = tid; w < nq; w += RD_THREADS) smem_rd[w] = make_uint4(0, 0, 0, 0);
+            const uint32_t jlo = (uint32_t)max(wb, i + 1), jhi = (uint32_t)min(we, n);
+            for (int kc = 0; jlo < jhi && kc < L; kc += RD_LOCI) {
+                // this thread's two loci, then a block-wide exclusive scan of the run lengths
+                const int k0 = kc + 2 * tid;
+                uint32_t lo0 = 0, lo1 = 0, l0 = 0, l1 = 0;
+                if (one_chunk) {
+                    l0 = partner_run(g, i, cur.a0, cur.m0, co0, jlo, jhi, &lo0);
+                    l1 = partner_run(g, i, cur.a1, cur.m1, co1, jlo, jhi, &lo1);
+                } else {
+                    const CellPair c = load_cells(g, i, k0);
+                    if (k0 < L) l0 = partner_run(g, i, c.a0, c.m0, g.cnt_off[k0], jlo, jhi, &lo0);
+                    if (k0 + 1 < L) l1 = partner_run(g, i, c.a1, c.m1, g.cnt_off[k0 + 1], jlo, jhi, &lo1);
+                }
+                const uint32_t mine = l0 + l1;
+                uint32_t inc = mine;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t t = __shfl_up_sync(FULL, inc, d);
+                    if (lane >= d) inc += t;
+                }
+                if (lane == 31) wsum[warp] = inc;
+                __syncthreads();  // also orders the counter zeroing and the previous chunk's readers
+                if (warp == 0) {
+                    const uint32_t v = wsum[lane];
+                    uint32_t x = v;
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const uint32_t t = __shfl_up_sync(FULL, x, d);
+                        if (lane >= d) x += t;
+                    }
+                    wsum[lane] = x - v;
+                    if (lane == 31) pre[RD_LOCI] = x;
+                }
+                __syncthreads();
+                const uint32_t ex = wsum[warp] + inc - mine;
+                pre[2 * tid] = ex;
+                pre[2 * tid + 1] = ex + l0;
+                run[2 * tid] = lo0;
+                run[2 * tid + 1] = lo1;
+                __syncthreads();
+                const uint32_t total = pre[RD_LOCI];
+                // warp w takes the items [w * part, (w + 1) * part) and walks them run
+                // by run, its 32 lanes on consecutive members of a run
+                const uint32_t part = (total + NWARPS - 1) / NWARPS;
+                uint32_t e = min(total, (uint32_t)warp * part);
+                const uint32_t e_end = min(total, e + part);
+                if (e < e_end) {
+                    int lo = 0, hi = RD_LOCI;  // the run holding item e: the last p with pre[p] <= e
+                    while (hi - lo > 1) {
+                        const int m = (lo + hi) >> 1;
+                        if (pre[m] <= e) lo = m; else hi = m;
+                    }
+                    for (int p = lo; e < e_end; p++) {
+                        const uint32_t stop = min(pre[p + 1], e_end);
+                        if (stop <= e) continue;  // an empty run
+                        const uint32_t* src = g.members + run[p] + (e - pre[p]);
+                        const uint32_t c = stop - e;
+                        uint32_t k = (uint32_t)lane;
+                        for (; k + 224 < c; k += 256) {  // eight loads in flight per lane
+                            uint32_t jj[8];
+#pragma unroll
+                            for (int u = 0; u < 8; u++) jj[u] = __ldg(src + k + 32 * u);
+#pragma unroll
+                            for (int u = 0; u < 8; u++) count_col(cnt, jj[u] - (uint32_t)wb);
+                        }
+                        if (k + 96 < c) {
+                            uint32_t jj[4];
+#pragma unroll
+                            for (int u = 0; u < 4; u++) jj[u] = __ldg(src + k + 32 * u);
+#pragma unroll
+                            for (int u = 0; u < 4; u++) count_col(cnt, jj[u] - (uint32_t)wb);
+                            k += 128;
+                        }
+                        for (; k < c; k += 32) count_col(cnt, __ldg(src + k) - (uint32_t)wb);
+                        e = stop;
+                    }
+                }
+            }
+            __syncthreads();
+            uint4* dst = Rrow + ((wb - cbeg) >> 3);
+            for (int w = tid; w < nq; w += RD_THREADS) dst[w] = smem_rd[w];
+            __syncthreads();
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R, size_t ldr, int sms,
+                              cudaStream_t st) {
+    if (rows <= 0) return cudaSuccess;
+    const size_t width = up((size_t)(g.n - r0), kRareDenseAlign);
+    if (ldr < width || (ldr & 7) || ((uintptr_t)R & 15)) return cudaErrorInvalidValue;
+    const int smem = RD_SMEM;
+    cudaError_t e = cudaFuncSetAttribute(rare_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const int grid = std::max(1, std::min(rows, sms));
+    rare_dense_kernel<<<grid, RD_THREADS, smem, st>>>(g, r0, rows, R, ldr, r0 + (int)width);
+    return cudaGetLastError();
+}
+
+}  // namespace tch

@@ -147,6 +147,8 @@ struct TcParams {
     const uint32_t* js;
     int fuse_rare;
     const int* unsorted;  // optional device flag: non-zero turns the fused subtraction off
+    const uint16_t* rdense;  // dense rare counts of the stripe (row stride ldr, column j at j - r0), or null
+    size_t ldr;
     uint16_t* out;
     size_t ldo;
     int* err;
@@ -306,6 +308,7 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
         uint16_t* stg = epi + (warp - 2) * 32 * EPI_PITCH;
         const int iend = p.r0 + p.rows;
         const bool fuse = p.fuse_rare && !(p.unsorted && *p.unsorted);
+        const bool dense = p.rdense != nullptr;
         int acc = 0;
         uint32_t aph = 0;
         int bad = 0;
@@ -331,6 +334,16 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
 #pragma unroll 1
             for (int cc = 0; cc < CHUNKS; cc++) {
                 const int c = half * CHUNKS + cc;
+                const uint32_t cb = (uint32_t)(j0 + c * 32);
+                // this row's dense rare counts for the chunk's 32 columns (64 bytes),
+                // fetched before the accumulator read so the two overlap
+                uint4 rq[4] = {};
+                if (dense && my_i < iend) {
+                    const uint4* src = reinterpret_cast<const uint4*>(p.rdense + (size_t)(my_i - p.r0) * p.ldr +
+                                                                      (size_t)(cb - (uint32_t)p.r0));
+#pragma unroll
+                    for (int u = 0; u < 4; u++) rq[u] = __ldg(src + u);
+                }
                 uint32_t v[32];
                 tmem_ld32(tbase + (uint32_t)(c * 32), v);
                 tmem_wait_ld();
@@ -353,10 +366,15 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
                         x0 = (int)v[2 * w];
                         x1 = (int)v[2 * w + 1];
                     }
+                    if (dense) {
+                        const uint4& r4 = rq[w / 4];
+                        const uint32_t rw = (w % 4 == 0) ? r4.x : (w % 4 == 1) ? r4.y : (w % 4 == 2) ? r4.z : r4.w;
+                        x0 -= (int)(rw & 0xFFFF);
+                        x1 -= (int)(rw >> 16);
+                    }
                     row32[w] = (uint32_t)(x0 & 0xFFFF) | ((uint32_t)(x1 & 0xFFFF) << 16);
                 }
                 // rare pairs of this row in columns [cb, cb + 32)
-                const uint32_t cb = (uint32_t)(j0 + c * 32);
                 for (;;) {
                     if (bpos == nbuf) {
                         if (rp >= rhi) break;
@@ -508,8 +526,11 @@ cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCS
     }
     p.start = rare.start;
     p.js = rare.js;
-    p.fuse_rare = (rare.n_rare > 0 && (rare.sorted || rare.unsorted_flag)) ? 1 : 0;
+    p.fuse_rare = (!rare.dense && rare.n_rare > 0 && (rare.sorted || rare.unsorted_flag)) ? 1 : 0;
     p.unsorted = rare.unsorted_flag;
+    p.rdense = rare.dense;
+    p.ldr = rare.ldr;
+    if (rare.dense && ((rare.ldr & 7) || ((uintptr_t)rare.dense & 15))) return cudaErrorInvalidValue;
     p.out = a.out;
     p.ldo = a.ldo;
     p.err = a.err;
@@ -518,7 +539,7 @@ cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCS
     cfg.gridDim = dim3(CM * clusters);
     cudaError_t e = cudaLaunchKernelEx(&cfg, kern, maps, p);
     if (e != cudaSuccess) return e;
-    if (rare.n_rare > 0 && !rare.sorted) return launch_rare_atomic(rare, a, st);
+    if (!rare.dense && rare.n_rare > 0 && !rare.sorted) return launch_rare_atomic(rare, a, st);
     return cudaSuccess;
 }
 
@@ -552,8 +573,10 @@ cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t*
         s.r0 = a.r0 + done;
         s.rows = std::min(max_rows, a.rows - done);
         s.out = a.out + (size_t)done * a.ldo + (size_t)done;
-        const cudaError_t e = cluster_size() == 2 ? launch_kind<KIND_F8, 2>(ops, ops.X, rare, s, num_sms, st)
-                                                  : launch_kind<KIND_F8, 1>(ops, ops.X, rare, s, num_sms, st);
+        RareCSR rs = rare;
+        if (rare.dense) rs.dense = rare.dense + (size_t)done * rare.ldr + (size_t)done;
+        const cudaError_t e = cluster_size() == 2 ? launch_kind<KIND_F8, 2>(ops, ops.X, rs, s, num_sms, st)
+                                                  : launch_kind<KIND_F8, 1>(ops, ops.X, rs, s, num_sms, st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;

@@ -50,6 +50,11 @@ struct RareCSR {
     // not (the separate atomic pass).  Lets the host launch both without
     // waiting for the check.
     const int* unsorted_flag = nullptr;
+    // Dense alternative: the stripe's rare counts as a u16 block laid out
+    // like the output (row stride ldr, column j at j - r0); subtracted in the
+    // tile epilogue.  Takes precedence over the pair list.
+    const uint16_t* dense = nullptr;
+    size_t ldr = 0;
 };
 
 // Bit-packed operands in the reference layout, u32 words, LSB first.
@@ -136,8 +141,31 @@ cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t*
 // Rates of the analytic tau model on this GPU.
 struct TauModel {
     double gemm_rate = 1.6e15;  // pair x one-byte-column MACs per second of the stripe kernel
-    double rare_rate = 6.0e11;  // rare pairs per second of the fused subtraction
+    double rare_rate = 6.0e11;  // rare pairs per second of the fused subtraction (pair lists)
+    // rare pairs per second of the dense rare-count build, at the margin (its
+    // fixed part, the u16 block written per stripe, does not depend on tau)
+    double dense_rate = 1.8e12;
 };
+
+// The rare alleles as groups of rows, kept on the device: the dense rare
+// counts of any stripe are built from them on demand.
+struct RareGroups {
+    const uint16_t* x = nullptr;        // n x L ranks
+    const uint64_t* cnt_off = nullptr;  // L + 1: slot of (locus k, rank a) is cnt_off[k] + a
+    const uint64_t* goff = nullptr;     // slots + 1: a rare group's rows are members[goff[q] .. goff[q+1])
+    const uint32_t* members = nullptr;  // rows of every rare group (count >= 2), ascending per group
+    const uint32_t* mpos = nullptr;     // n x L: index in members of row i's own entry (rare cells only)
+    int n = 0, L = 0;
+};
+
+// R[(i - r0) * ldr + (j - r0)] = number of loci where rows i and j share a
+// rare allele, for r0 <= i < r0 + rows and i < j < n; written as 0 for the
+// other columns from the start of row i's diagonal tile, r0 + ((i - r0) &
+// ~255), up to r0 + up(n - r0, 256); columns before that are left as they
+// are.  ldr >= up(n - r0, 256) and a multiple of 8; R 16-byte aligned.
+constexpr int kRareDenseAlign = 256;
+cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R, size_t ldr, int sms,
+                              cudaStream_t st);
 
 // Operands built on the device from allele calls; device memory owned here.
 struct DeviceEncoding {
@@ -147,14 +175,20 @@ struct DeviceEncoding {
     KChunks X;                // x_rows x kb e4m3 operand rows, split along K
     size_t x_rows = 0;
     int kb = 0, kp = 0;
-    uint32_t* start = nullptr;  // n + 1
-    uint32_t* js = nullptr;     // n_rare, ascending per row
+    uint32_t* start = nullptr;  // n + 1 (CSR mode)
+    uint32_t* js = nullptr;     // n_rare, ascending per row (CSR mode)
     size_t n_rare = 0;
+    // dense mode: the rare groups stay on the device instead of a pair list
+    bool dense = false;
+    uint64_t* cnt_off = nullptr;
+    uint64_t* goff = nullptr;
+    uint32_t* members = nullptr;
+    uint32_t* mpos = nullptr;
     size_t bytes = 0;
 };
 
 int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_req, const TauModel& model,
-                     bool verbose, size_t max_chunk_bytes, DeviceEncoding* out, Err& e);
+                     bool verbose, size_t max_chunk_bytes, bool dense_rare, DeviceEncoding* out, Err& e);
 void free_device_encoding(DeviceEncoding* d);
 
 }  // namespace tch

@@ -54,6 +54,42 @@ static size_t max_chunk_bytes() {
     return (size_t)g_max_chunk;
 }
 
+// Rare term of solvers built from calls: 1 = dense per-stripe counts from the
+// rare groups, 0 = pair lists.  Set by tch_set_rare_term or TCH_RARE.
+static int g_rare_dense = -1;
+
+static bool rare_dense_default() {
+    if (g_rare_dense < 0) {
+        const char* v = getenv("TCH_RARE");
+        g_rare_dense = (v && !strcmp(v, "lists")) ? 0 : 1;
+    }
+    return g_rare_dense == 1;
+}
+
+// Stream-ordered pool of the per-stripe rare-count blocks, one per device; it
+// keeps freed blocks for the next stripe instead of returning them at every
+// synchronisation.
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pool[64];
+
+static cudaError_t stripe_pool(int device, cudaMemPool_t* out) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    if (!g_pool[device]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        cudaError_t e = cudaMemPoolCreate(&g_pool[device], &props);
+        if (e != cudaSuccess) return e;
+        uint64_t keep = ~0ull;
+        e = cudaMemPoolSetAttribute(g_pool[device], cudaMemPoolAttrReleaseThreshold, &keep);
+        if (e != cudaSuccess) return e;
+    }
+    *out = g_pool[device];
+    return cudaSuccess;
+}
+
 static const char* kKernelNames[TCH_KERNEL_COUNT] = {"auto", "popc", "mma_b1", "tc_f8", "tc_i8", "tc_f16"};
 
 static bool kernel_compiled(int k) {
@@ -115,6 +151,15 @@ struct tch_solver {
     const uint32_t* defer_js = nullptr;
     const uint32_t* hStart = nullptr;       // borrowed for the host fallback
     const uint32_t* hJs = nullptr;
+    // dense rare term: the rare groups stay on the device and every stripe's
+    // counts are built just before its tile pass
+    bool dense = false;
+    uint16_t* gx = nullptr;          // n x L ranks
+    uint64_t* gcnt_off = nullptr;
+    uint64_t* ggoff = nullptr;
+    uint32_t* gmembers = nullptr;
+    uint32_t* gmpos = nullptr;
+    int gL = 0;                      // loci of the rank rows (>= 1)
     int* dErr = nullptr;
     int num_sms = 0;
     size_t bytes = 0;
@@ -139,6 +184,18 @@ static void solver_free(tch_solver* s) {
     cudaFree(s->dStart);
     cudaFree(s->dJs);
     cudaFree(s->dErr);
+    cudaFree(s->gx);
+    cudaFree(s->gcnt_off);
+    cudaFree(s->ggoff);
+    cudaFree(s->gmembers);
+    cudaFree(s->gmpos);
+    if (s->dense) {  // hand the pool's idle stripe blocks back
+        cudaMemPool_t pool;
+        if (stripe_pool(s->device, &pool) == cudaSuccess) {
+            cudaDeviceSynchronize();
+            cudaMemPoolTrimTo(pool, 0);
+        }
+    }
     if (cur >= 0) cudaSetDevice(cur);
     delete s;
 }
@@ -315,11 +372,23 @@ static int solver_from_calls(int device, int n, int L, const uint64_t* calls, in
     } else {
         TCH_CK(e, cudaMemset(d_calls, 0, std::max<size_t>((size_t)n, 1) * 8));
     }
-    if (encode_on_device(device, n, Le, d_calls, tau, g_tau_model, verbose, max_chunk_bytes(), &enc, e)) goto fail;
+    if (encode_on_device(device, n, Le, d_calls, tau, g_tau_model, verbose, max_chunk_bytes(), rare_dense_default(),
+                         &enc, e))
+        goto fail;
     cudaFree(d_calls);
     d_calls = nullptr;
-    cudaFree(enc.x);
-    enc.bytes -= (size_t)n * Le * 2;
+    if (enc.dense) {  // the solver takes the rare groups
+        s->dense = true;
+        s->gL = Le;
+        s->gx = enc.x;
+        s->gcnt_off = enc.cnt_off;
+        s->ggoff = enc.goff;
+        s->gmembers = enc.members;
+        s->gmpos = enc.mpos;
+    } else {
+        cudaFree(enc.x);
+        enc.bytes -= (size_t)n * Le * 2;
+    }
     enc.x = nullptr;
     s->xc = enc.X;
     s->x_rows = enc.x_rows;
@@ -341,6 +410,38 @@ fail:
     if (d_calls) cudaFree(d_calls);
     solver_free(s);
     return 1;
+}
+
+static RareGroups rare_groups(const tch_solver* s) {
+    RareGroups g;
+    g.x = s->gx;
+    g.cnt_off = s->gcnt_off;
+    g.goff = s->ggoff;
+    g.members = s->gmembers;
+    g.mpos = s->gmpos;
+    g.n = s->n;
+    g.L = s->gL;
+    return g;
+}
+
+static ByteOperands byte_operands(const tch_solver* s) {
+    ByteOperands ops;
+    ops.X = s->xc.p[0];
+    ops.chunks = s->xc;
+    ops.n_rows = s->x_rows;
+    ops.kb = s->kb;
+    ops.kp = s->kp;
+    return ops;
+}
+
+// The tile pass of a dense-rare solver with the stripe's counts in R.
+static cudaError_t launch_dense_stripe(tch_solver* s, const StripeArgs& a, const uint16_t* R, size_t ldr,
+                                       cudaStream_t st) {
+    RareCSR dr;
+    dr.dense = R;
+    dr.ldr = ldr;
+    dr.n_rare = s->n_rare;
+    return launch_tc_stripe(s->kernel, byte_operands(s), nullptr, dr, a, s->num_sms, st);
 }
 
 static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e,
@@ -368,6 +469,22 @@ static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_
         rare.unsorted_flag = unsorted_flag;
     }
     cudaError_t ce;
+    if (s->dense) {
+        // the stripe's rare counts, from the rare groups, into a block of the pool
+        const size_t ldr = up((size_t)(s->n - r0), kRareDenseAlign);
+        const size_t rbytes = (size_t)rows * ldr * 2;
+        cudaMemPool_t pool;
+        uint16_t* R = nullptr;
+        ce = stripe_pool(s->device, &pool);
+        if (ce == cudaSuccess) ce = cudaMallocFromPoolAsync((void**)&R, rbytes, pool, st);
+        if (ce != cudaSuccess) return e.set("rare counts of the stripe (%zu bytes): %s", rbytes, cudaGetErrorString(ce));
+        ce = launch_rare_dense(rare_groups(s), r0, rows, R, ldr, s->num_sms, st);
+        if (ce == cudaSuccess) ce = launch_dense_stripe(s, a, R, ldr, st);
+        const cudaError_t fe = cudaFreeAsync(R, st);
+        if (ce == cudaSuccess) ce = fe;
+        if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
+        return 0;
+    }
     if (s->kernel == TCH_KERNEL_POPC) {
         BitOperands ops;
         ops.P = s->dP;
@@ -376,13 +493,7 @@ static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_
         ops.wO = (int)(s->K1 / 32);
         ce = launch_popc_stripe(ops, rare, a, st);
     } else {
-        ByteOperands ops;
-        ops.X = s->xc.p[0];
-        ops.chunks = s->xc;
-        ops.n_rows = s->x_rows;
-        ops.kb = s->kb;
-        ops.kp = s->kp;
-        ce = launch_tc_stripe(s->kernel, ops, nullptr, rare, a, s->num_sms, st);
+        ce = launch_tc_stripe(s->kernel, byte_operands(s), nullptr, rare, a, s->num_sms, st);
     }
     if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
     return 0;
@@ -685,6 +796,17 @@ int tch_set_max_chunk_bytes(size_t bytes) {
     return 0;
 }
 
+int tch_set_dense_rare_rate(double rate) {
+    if (!(rate > 0)) return 1;
+    g_tau_model.dense_rate = rate;
+    return 0;
+}
+
+int tch_set_rare_term(int dense) {
+    g_rare_dense = dense ? 1 : 0;
+    return 0;
+}
+
 int tch_set_tau_model(double gemm_rate, double rare_rate) {
     if (!(gemm_rate > 0) || !(rare_rate > 0)) return 1;
     g_tau_model.gemm_rate = gemm_rate;
@@ -707,6 +829,7 @@ int tch_solver_info(const tch_solver* s, tch_info* info) {
     info->rare_sorted = s->sorted ? 1 : 0;
     info->device_bytes = s->bytes;
     info->k_chunks = s->xc.n;
+    info->rare_dense = s->dense ? 1 : 0;
     return 0;
 }
 
@@ -717,6 +840,50 @@ int tch_solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t l
     if (!d_out && rows > 0) return e.set("null output");
     if (cudaSetDevice(s->device) != cudaSuccess) return e.set("cudaSetDevice(%d) failed", s->device);
     return solver_stripe(s, r0, rows, d_out, ldo, (cudaStream_t)stream, e);
+}
+
+int tch_solver_rare_counts(tch_solver* s, int r0, int rows, uint16_t* d_R, size_t ldr, void* stream, char* err,
+                           int errlen) {
+    Err e{err, errlen};
+    if (!s) return e.set("null solver");
+    if (!s->dense) return e.set("the solver holds pair lists, not rare groups");
+    if (r0 < 0 || rows < 0 || r0 > s->n) return e.set("stripe out of range (r0=%d rows=%d n=%d)", r0, rows, s->n);
+    if (r0 + rows > s->n) rows = s->n - r0;
+    if (rows == 0) return 0;
+    const size_t width = up((size_t)(s->n - r0), kRareDenseAlign);
+    if (!d_R || ldr < width || (ldr & 7) || ((uintptr_t)d_R & 15))
+        return e.set("rare counts need a 16-byte aligned block with ldr >= %zu, a multiple of 8 (got %zu)", width, ldr);
+    if (cudaSetDevice(s->device) != cudaSuccess) return e.set("cudaSetDevice(%d) failed", s->device);
+    const cudaError_t ce = launch_rare_dense(rare_groups(s), r0, rows, d_R, ldr, s->num_sms, (cudaStream_t)stream);
+    if (ce != cudaSuccess) return e.set("rare counts: %s", cudaGetErrorString(ce));
+    return 0;
+}
+
+int tch_solver_stripe_counts(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, const uint16_t* d_R,
+                             size_t ldr, void* stream, char* err, int errlen) {
+    Err e{err, errlen};
+    if (!s) return e.set("null solver");
+    if (!s->dense) return e.set("the solver holds pair lists, not rare groups");
+    if (r0 < 0 || rows < 0 || r0 > s->n) return e.set("stripe out of range (r0=%d rows=%d n=%d)", r0, rows, s->n);
+    if (r0 + rows > s->n) rows = s->n - r0;
+    if (rows == 0) return 0;
+    if (!d_out) return e.set("null output");
+    if (ldo < (size_t)(s->n - r0) || (ldo & 1)) return e.set("ldo must be even and >= n - r0 (got %zu)", ldo);
+    if (((uintptr_t)d_out & 15) != 0) return e.set("output pointer must be 16-byte aligned");
+    const size_t width = up((size_t)(s->n - r0), kRareDenseAlign);
+    if (!d_R || ldr < width || (ldr & 7) || ((uintptr_t)d_R & 15))
+        return e.set("rare counts need a 16-byte aligned block with ldr >= %zu, a multiple of 8 (got %zu)", width, ldr);
+    if (cudaSetDevice(s->device) != cudaSuccess) return e.set("cudaSetDevice(%d) failed", s->device);
+    StripeArgs a;
+    a.n = s->n;
+    a.r0 = r0;
+    a.rows = rows;
+    a.out = d_out;
+    a.ldo = ldo;
+    a.err = s->dErr;
+    const cudaError_t ce = launch_dense_stripe(s, a, d_R, ldr, (cudaStream_t)stream);
+    if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
+    return 0;
 }
 
 int tch_solver_check(tch_solver* s, char* err, int errlen) {

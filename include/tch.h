@@ -109,6 +109,7 @@ typedef struct tch_info {
     int rare_sorted;   /* 1 if every row's partner list is ascending */
     size_t device_bytes; /* device memory held by the solver */
     int k_chunks;        /* separate allocations the operand rows are split into along K */
+    int rare_dense;      /* 1 if the rare term is counted per stripe from rare groups */
 } tch_info;
 
 /* Largest single device allocation of a solver's operand rows, in bytes
@@ -132,9 +133,12 @@ int tch_solver_from_bits(int device, int n, size_t n_pad, const uint8_t* O, size
  * 0 = missing; any other value is an allele id compared for equality only).
  * The encoding the reference's host does (main.rs:134-165, 366-444: dense
  * ranks, frequent one-hot columns, presence, rare equal pairs) runs on the
- * device.  tau <= 0 picks tau with the analytic GB300 cost model.  Fails like
- * the reference when a locus has more than 65535 distinct ids, L > 65535, or
- * the rare pairs reach 2^32. */
+ * device.  tau <= 0 picks tau with the analytic GB300 cost model.  The rare
+ * term is kept as groups of rows per rare allele and counted per stripe into
+ * a dense u16 block (tch_set_rare_term(1), the default), or built as the
+ * reference's pair lists (tch_set_rare_term(0)).  Fails like the reference
+ * when a locus has more than 65535 distinct ids or L > 65535; pair lists also
+ * fail when the rare pairs reach 2^32, dense counts when the rare cells do. */
 int tch_solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, tch_solver** out,
                           char* err, int errlen);
 
@@ -148,6 +152,17 @@ int tch_run_calls(int device, int n, int L, const uint64_t* calls, int tau, int 
  * stripe kernel, rare pairs per second); defaults are GB300 measurements. */
 int tch_set_tau_model(double gemm_rate, double rare_rate);
 
+/* Rare pairs per second of the dense rare-count build (tau model of
+ * solvers with dense rare counts). */
+int tch_set_dense_rare_rate(double rate);
+
+/* How solvers built from allele calls hold the rare term, for solvers
+ * created afterwards: 1 = rare groups on the device, counted per stripe into
+ * a dense block subtracted in the tile epilogue (default); 0 = per-row
+ * ascending pair lists walked in the epilogue.  Also TCH_RARE=lists|dense.
+ * No reference counterpart (the reference always builds pair lists). */
+int tch_set_rare_term(int dense);
+
 /* Fill *info. */
 int tch_solver_info(const tch_solver* s, tch_info* info);
 
@@ -159,6 +174,21 @@ int tch_solver_info(const tch_solver* s, tch_info* info);
  * device (an invalid rare pair) are reported by the next tch_solver_check. */
 int tch_solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, void* stream, char* err,
                       int errlen);
+
+/* The two passes of tch_solver_stripe for a solver with dense rare counts
+ * (tch_info.rare_dense = 1), for callers that schedule them apart (e.g. the
+ * counts of the next stripe on a second stream):
+ *   tch_solver_rare_counts: d_R[(i - r0) * ldr + (j - r0)] = rare loci shared
+ *     by i and j, for r0 <= i < r0 + rows and i < j < n; 0 in the row's other
+ *     columns from r0 + ((i - r0) & ~255) to r0 + up(n - r0, 256).
+ *   tch_solver_stripe_counts: the stripe of tch_solver_stripe with the rare
+ *     term taken from d_R.
+ * d_R 16-byte aligned, ldr >= up(n - r0, 256) and a multiple of 8.  No
+ * reference counterpart. */
+int tch_solver_rare_counts(tch_solver* s, int r0, int rows, uint16_t* d_R, size_t ldr, void* stream, char* err,
+                           int errlen);
+int tch_solver_stripe_counts(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, const uint16_t* d_R,
+                             size_t ldr, void* stream, char* err, int errlen);
 
 /* Synchronise the device and report any error recorded by earlier stripes. */
 int tch_solver_check(tch_solver* s, char* err, int errlen);

@@ -10,10 +10,14 @@ import refgen
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def tch(pkg):
+@pytest.fixture(scope="module", params=["dense", "lists"])
+def tch(pkg, request):
+    """Every test runs for both holdings of the rare term: per-stripe dense
+    counts from the rare groups, and the reference's pair lists."""
     assert pkg.device_count() > 0, "no CUDA device visible"
-    return pkg
+    pkg.set_rare_term(request.param == "dense")
+    yield pkg
+    pkg.set_rare_term(True)
 
 
 def upper_equal(H, ref):
@@ -89,3 +93,51 @@ def test_longtail_sample_device_vs_host_encoder(tch):
         iu = np.triu_indices(3000, 1)
         np.testing.assert_array_equal(Hd[iu], Hh[iu])
     upper_equal(Hd, oracle.hamming(x))
+
+
+def test_rare_term_mode_reported(tch, pkg):
+    rng = np.random.default_rng(12)
+    A = rng.integers(1, 30, size=(200, 40)).astype(np.uint64)
+    with tch.Solver.from_calls(A, tau=8) as s:
+        info = s.info()
+        H, _ = s.run(64)
+    upper_equal(H, oracle.hamming(oracle.dense_ranks(A)[0]))
+    x, cnt = oracle.dense_ranks(A)
+    assert info["n_rare"] == len(oracle.encode(x, cnt, 8).js)
+    assert info["rare_dense"] in (0, 1)
+
+
+def test_more_loci_than_threads(tch):
+    """More loci than one CTA pass of the rare-count kernel covers (1024)."""
+    rng = np.random.default_rng(21)
+    n, L = 400, 2500
+    A = rng.integers(1, 12, size=(n, L)).astype(np.uint64)
+    A[rng.random((n, L)) < 0.02] = 0
+    x = oracle.dense_ranks(A)[0]
+    ref = oracle.hamming(x)
+    for tau in (4, 64, 1000):
+        with tch.Solver.from_calls(A, tau=tau) as s:
+            H, _ = s.run(96)
+        upper_equal(H, ref)
+
+
+def test_wide_stripe_blocks(tch):
+    """n above 65 536 columns: the rare counts of a row take several passes
+    of the shared-memory counters.  Rows checked against the oracle's block."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(33)
+    n, L = 70001, 12
+    A = rng.integers(1, 3000, size=(n, L)).astype(np.uint64)  # ~23 rows per allele: rare at tau 64
+    A[:, :3] = rng.integers(1, 4, size=(n, 3))  # frequent loci
+    x = oracle.dense_ranks(A)[0]
+    with tch.Solver.from_calls(A, tau=64) as s:
+        assert s.info()["n_rare"] > 0
+        for r0, rows in ((0, 200), (4097, 131), (n - 300, 300)):
+            ldo = (n - r0 + 7) // 8 * 8
+            out = torch.zeros((rows, ldo), dtype=torch.int16, device="cuda")
+            s.stripe(r0, rows, out.data_ptr(), ldo, torch.cuda.current_stream().cuda_stream)
+            s.check()
+            got = out.cpu().numpy().view(np.uint16)
+            ref = oracle.hamming_block(x, r0, r0 + rows, r0, n)
+            for r in range(rows):
+                np.testing.assert_array_equal(got[r, r + 1: n - r0], ref[r, r + 1:])
