@@ -319,10 +319,15 @@ def main():
                 "algorithmic_ops_per_launch": ops_per_launch, "k_per_pair": k_alg,
                 "k_padded_bytes": info["k_presence"] + info["k_onehot"],
                 "bf16_measured_tflops": (mp or {}).get("bf16_tflops"), "traffic": None}
-    prof = os.path.join(ROOT, "profiles", "tc_stripe_longtail_traffic.json")
-    if os.path.exists(prof):
+    # DRAM bytes of one whole-triangle tile pass, from the ncu capture of this
+    # workload (valid for the tau and row share it was taken at)
+    prof = os.path.join(ROOT, "profiles", "tc_stripe_longtail_traffic.txt")
+    if os.path.exists(prof) and ws == 1:
         with open(prof) as f:
-            roofline["traffic"] = json.load(f).get("bytes_per_launch")
+            kv = dict(line.split(":", 1) for line in f if ":" in line)
+        if int(kv.get("tau", "0")) == tau and int(kv.get("n", "0")) == n:
+            roofline["traffic"] = int(kv["bytes_per_launch"])
+            roofline["traffic_source"] = kv.get("source", "").strip()
 
     # e2e through the C ABI with host buffers: tch_run (the reference's entry
     # point, host-encoded operands) and tch_run_calls (allele calls, device encoder)
