@@ -51,7 +51,7 @@ constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int EPI_PITCH = 34;      // u16 per staged row: 32 + 2 keeps row writes conflict-free
 constexpr int EPI_BYTES = EPI_WARPS * 32 * EPI_PITCH * 2;
 constexpr int TMEM_COLS = 2 * BN;  // two accumulators
-constexpr int GROUP_M = 8;         // row blocks per raster group
+constexpr int GROUP_M = 16;        // row blocks per raster group (default; TCH_TC_GROUP overrides)
 constexpr int RBUF = 16;           // rare partners fetched per batch in the epilogue
 constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + EPI_BYTES + 256;
 
@@ -64,9 +64,23 @@ using namespace ptx;
 // "super-row" sr of CM * 128 rows) against one 256-column block bj; CTA rank r
 // owns row block bi = sr * CM + r.  With CM = 2 the two CTAs share the B tile:
 // each loads one 128-row half and multicasts it to both.
+// Row blocks per raster group: GROUP_M unless TCH_TC_GROUP gives another even
+// count in [2, 256].  Larger groups read the column side of the operand fewer
+// times (once per group) at the cost of a larger row-side working set.
+int group_row_blocks() {
+    static int g = 0;
+    if (!g) {
+        const char* v = getenv("TCH_TC_GROUP");
+        const int x = v ? atoi(v) : 0;
+        g = (x >= 2 && x <= 256 && x % 2 == 0) ? x : GROUP_M;
+    }
+    return g;
+}
+
 struct TileSpace {
     int nsr, nbj;  // super-rows of the stripe, column blocks of [r0, n)
     int cm;        // row blocks per super-row (cluster size)
+    int gs;        // super-rows per raster group
 };
 
 // Columns of super-row sr: bj >= sr * cm / 2 (128-row blocks against 256-wide
@@ -81,7 +95,7 @@ __host__ __device__ __forceinline__ long long count_tiles(const TileSpace& ts) {
 
 constexpr int MAX_GROUPS = 1024;   // raster groups with a precomputed first tile
 
-// First tile index of every raster group (groups of GROUP_M row blocks,
+// First tile index of every raster group (groups of gs super-rows,
 // column-major inside a group), so a tile's coordinates cost a binary search
 // over groups plus a few steps instead of a walk over the whole stripe.
 struct GroupTable {
@@ -97,7 +111,7 @@ __host__ __device__ __forceinline__ int group_tiles(const TileSpace& ts, int g0,
 
 // t -> (sr, bj).
 __device__ bool tile_coords(const TileSpace& ts, const GroupTable& gt, int t, int* sr_out, int* bj_out) {
-    const int gs = GROUP_M / ts.cm;  // super-rows per group
+    const int gs = ts.gs;
     int lo = 0, hi = gt.ngroups;     // last group whose first tile is <= t
     while (hi - lo > 1) {
         const int mid = (lo + hi) / 2;
@@ -510,11 +524,12 @@ cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCS
     p.kblocks = ops.kb / BK;
     p.kblocks_p = ops.kp / BK;
     p.ts.cm = CM;
+    p.ts.gs = group_row_blocks() / CM;
     p.ts.nsr = ((a.rows + BM - 1) / BM + CM - 1) / CM;
     p.ts.nbj = (a.n - a.r0 + BN - 1) / BN;
     p.num_tiles = (int)count_tiles(p.ts);
     {
-        const int gs = GROUP_M / CM;
+        const int gs = p.ts.gs;
         p.gt.ngroups = (p.ts.nsr + gs - 1) / gs;
         if (p.gt.ngroups > MAX_GROUPS) return cudaErrorInvalidValue;  // callers split taller stripes
         int acc = 0;
@@ -567,7 +582,7 @@ cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t*
     if (kernel != TCH_KERNEL_TC_F8) return cudaErrorNotSupported;
     // one launch covers at most MAX_GROUPS raster groups of rows; a taller
     // stripe runs as consecutive sub-stripes writing into the same output
-    const int max_rows = MAX_GROUPS * GROUP_M * BM;
+    const int max_rows = MAX_GROUPS * group_row_blocks() * BM;
     for (int done = 0; done < a.rows; done += max_rows) {
         StripeArgs s = a;
         s.r0 = a.r0 + done;
