@@ -117,6 +117,34 @@ def lib():
         L.tch_set_max_chunk_bytes.argtypes, L.tch_set_max_chunk_bytes.restype = [c_size], c_int
         L.tch_set_dense_rare_rate.argtypes, L.tch_set_dense_rare_rate.restype = [c_double], c_int
         L.tch_set_rare_term.argtypes, L.tch_set_rare_term.restype = [c_int], c_int
+        L.tch_tau_features.argtypes = [c_int, c_int, c_int, c_void, c_int, c_void, c_void, c_void, P(c_int),
+                                       c_char_p, c_int]
+        L.tch_tau_features.restype = c_int
+        L.tch_mlp_init.argtypes, L.tch_mlp_init.restype = [c_void, ctypes.c_uint64], c_int
+        L.tch_mlp_train.argtypes = [c_int, c_void, c_void, c_void, c_int, c_int, ctypes.c_float,
+                                    P(ctypes.c_float), c_char_p, c_int]
+        L.tch_mlp_train.restype = c_int
+        L.tch_mlp_predict.argtypes = [c_int, c_void, c_void, c_int, c_void, c_char_p, c_int]
+        L.tch_mlp_predict.restype = c_int
+        L.tch_mlp_loss_grad.argtypes = [c_int, c_void, c_void, c_void, c_int, P(ctypes.c_float), c_void, c_char_p,
+                                        c_int]
+        L.tch_mlp_loss_grad.restype = c_int
+        L.tch_set_tau_mlp.argtypes, L.tch_set_tau_mlp.restype = [c_void], c_int
+        L.tch_db_create.argtypes = [c_int, c_int, c_int, c_void, c_int, P(c_void), c_char_p, c_int]
+        L.tch_db_create.restype = c_int
+        L.tch_db_destroy.argtypes, L.tch_db_destroy.restype = [c_void], None
+        L.tch_db_info.argtypes = [c_void, P(c_int), P(c_int), P(c_int), P(c_size), P(c_size)]
+        L.tch_db_info.restype = c_int
+        L.tch_db_query_bytes.argtypes, L.tch_db_query_bytes.restype = [c_void, c_int], c_size
+        L.tch_db_query.argtypes = [c_void, c_int, c_void, c_void, c_void, c_void, c_char_p, c_int]
+        L.tch_db_query.restype = c_int
+        L.tch_server_create.argtypes = [c_void, c_int, c_size, P(c_void), c_char_p, c_int]
+        L.tch_server_create.restype = c_int
+        L.tch_server_submit.argtypes = [c_void, c_int, c_void, c_void, c_void]
+        L.tch_server_submit.restype = ctypes.c_int64
+        L.tch_server_wait.argtypes = [c_void, ctypes.c_int64, P(c_double), P(c_double), c_char_p, c_int]
+        L.tch_server_wait.restype = c_int
+        L.tch_server_destroy.argtypes, L.tch_server_destroy.restype = [c_void], None
         _lib = L
     return _lib
 
@@ -279,6 +307,89 @@ def set_tau_model(gemm_rate: float, rare_rate: float, dense_rare_rate: float | N
         raise TchError("rates must be positive")
 
 
+# ---------------------------------------------------------------------------------------
+# learned tau (no reference counterpart)
+# ---------------------------------------------------------------------------------------
+
+TAU_FEATURES = 12
+MLP_HIDDEN = 32
+MLP_PARAMS = TAU_FEATURES * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN + 1
+TAU_MLP_PATH = os.path.join(HERE, "tau_mlp_gb300.f32")
+
+
+def tau_features(calls: np.ndarray, device: int = 0):
+    """(taus, features [rows x TAU_FEATURES] f32, analytic estimates in s) of
+    the candidate taus whose encoding fits on the device."""
+    calls = np.ascontiguousarray(calls, dtype=np.uint64)
+    n, L = calls.shape
+    taus = np.zeros(32, np.int32)
+    feats = np.zeros((32, TAU_FEATURES), np.float32)
+    est = np.zeros(32, np.float64)
+    rows = ctypes.c_int(0)
+    err = _errbuf()
+    _check(lib().tch_tau_features(device, n, L, _ptr(calls), 32, _ptr(taus), _ptr(feats), _ptr(est),
+                                  ctypes.byref(rows), err, len(err)), err)
+    r = rows.value
+    return taus[:r].copy(), feats[:r].copy(), est[:r].copy()
+
+
+def mlp_init(seed: int) -> np.ndarray:
+    w = np.zeros(MLP_PARAMS, np.float32)
+    lib().tch_mlp_init(_ptr(w), seed)
+    return w
+
+
+def mlp_train(w: np.ndarray, X: np.ndarray, y: np.ndarray, steps: int, lr: float, device: int = 0):
+    """Adam on the GPU (the library's kernels); returns (new weights, final loss)."""
+    w = np.ascontiguousarray(w, dtype=np.float32).copy()
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    loss = ctypes.c_float(0)
+    err = _errbuf()
+    _check(lib().tch_mlp_train(device, _ptr(w), _ptr(X), _ptr(y), len(y), steps, lr, ctypes.byref(loss), err,
+                               len(err)), err)
+    return w, loss.value
+
+
+def mlp_predict(w: np.ndarray, X: np.ndarray, device: int = 0) -> np.ndarray:
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    out = np.zeros(len(X), np.float32)
+    err = _errbuf()
+    _check(lib().tch_mlp_predict(device, _ptr(w), _ptr(X), len(X), _ptr(out), err, len(err)), err)
+    return out
+
+
+def mlp_loss_grad(w: np.ndarray, X: np.ndarray, y: np.ndarray, device: int = 0):
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    g = np.zeros(MLP_PARAMS, np.float32)
+    loss = ctypes.c_float(0)
+    err = _errbuf()
+    _check(lib().tch_mlp_loss_grad(device, _ptr(w), _ptr(X), _ptr(y), len(y), ctypes.byref(loss), _ptr(g), err,
+                                   len(err)), err)
+    return loss.value, g
+
+
+def set_tau_mlp(w: np.ndarray | None) -> None:
+    """Model used by tau <= 0 (None: the analytic model)."""
+    if w is None:
+        lib().tch_set_tau_mlp(None)
+        return
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    if w.size != MLP_PARAMS or lib().tch_set_tau_mlp(_ptr(w)):
+        raise TchError("invalid tau model parameters")
+
+
+def load_tau_mlp(path: str = TAU_MLP_PATH) -> np.ndarray:
+    """The trained model shipped with the package (little-endian f32), set
+    as the solver's tau model; returns its parameters."""
+    w = np.fromfile(path, dtype="<f4")
+    set_tau_mlp(w)
+    return w
+
+
 def set_rare_term(dense: bool) -> None:
     """Rare term of solvers built from calls: dense per-stripe counts from the
     rare groups (True, default) or per-row pair lists (False)."""
@@ -365,3 +476,97 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------------------
+# serving: resident database, query batches, continuous batching
+# ---------------------------------------------------------------------------------------
+
+class Database:
+    """A profile database resident on the device (tch_db)."""
+
+    def __init__(self, calls: np.ndarray, tau: int = 0, device: int = 0):
+        calls = np.ascontiguousarray(calls, dtype=np.uint64)
+        self.n, self.L = calls.shape
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        _check(lib().tch_db_create(device, self.n, self.L, _ptr(calls), tau, ctypes.byref(h), err, len(err)), err)
+        self._h = h
+
+    def info(self) -> dict:
+        n, L, tau = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        d, b = ctypes.c_size_t(), ctypes.c_size_t()
+        lib().tch_db_info(self._h, ctypes.byref(n), ctypes.byref(L), ctypes.byref(tau), ctypes.byref(d),
+                          ctypes.byref(b))
+        return dict(n=n.value, L=L.value, tau=tau.value, d_onehot=d.value, device_bytes=b.value)
+
+    def query_bytes(self, m: int) -> int:
+        return lib().tch_db_query_bytes(self._h, m)
+
+    def query(self, q: np.ndarray, want_qq: bool = True, stream: int = 0):
+        """(q x database distances [m x n], q x q upper triangle [m x m] or None)."""
+        q = np.ascontiguousarray(q, dtype=np.uint64)
+        m = q.shape[0]
+        if q.shape[1] != self.L:
+            raise TchError(f"queries have {q.shape[1]} loci, the database {self.L}")
+        qdb = np.zeros((m, self.n), np.uint16)
+        qq = np.zeros((m, m), np.uint16) if want_qq else None
+        err = _errbuf()
+        _check(lib().tch_db_query(self._h, m, _ptr(q), _ptr(qdb), _ptr(qq) if want_qq else None,
+                                  ctypes.c_void_p(stream) if stream else None, err, len(err)), err)
+        return qdb, qq
+
+    def close(self):
+        if self._h:
+            lib().tch_db_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Server:
+    """Continuous batching over a Database (tch_server): submit() returns at
+    once; wait() blocks until that request's results are in its buffers."""
+
+    def __init__(self, db: Database, slots: int = 4, budget: int = 0):
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        _check(lib().tch_server_create(db._h, slots, budget, ctypes.byref(h), err, len(err)), err)
+        self._h = h
+        self.db = db
+        self._live = {}
+
+    def submit(self, q: np.ndarray, want_qq: bool = True) -> int:
+        q = np.ascontiguousarray(q, dtype=np.uint64)
+        m = q.shape[0]
+        qdb = np.zeros((m, self.db.n), np.uint16)
+        qq = np.zeros((m, m), np.uint16) if want_qq else None
+        rid = lib().tch_server_submit(self._h, m, _ptr(q), _ptr(qdb), _ptr(qq) if want_qq else None)
+        if rid < 0:
+            raise TchError("request rejected")
+        self._live[rid] = (q, qdb, qq)  # buffers live until wait()
+        return rid
+
+    def wait(self, rid: int):
+        """(qdb, qq, queued seconds, latency seconds)."""
+        qs, ls = ctypes.c_double(), ctypes.c_double()
+        err = _errbuf()
+        rc = lib().tch_server_wait(self._h, rid, ctypes.byref(qs), ctypes.byref(ls), err, len(err))
+        q, qdb, qq = self._live.pop(rid)
+        _check(rc, err)
+        return qdb, qq, qs.value, ls.value
+
+    def close(self):
+        if self._h:
+            lib().tch_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -30,6 +30,8 @@
 #include <chrono>
 #include <vector>
 
+#include <math.h>
+
 #include "tch_internal.cuh"
 
 namespace tch {
@@ -75,7 +77,8 @@ __global__ void insert_kernel(const uint64_t* __restrict__ calls, int n, int L, 
 // One CTA per locus of the batch.  rank = 1 + #(distinct ids smaller than it).
 __global__ void rank_kernel(int k0, const unsigned long long* keys, const uint32_t* cnts, int logC,
                             const uint32_t* nd, const uint64_t* cnt_off, uint32_t* cnt_flat, uint16_t* rank_slot,
-                            unsigned long long* list_keys, uint32_t* list_slots, int* err) {
+                            unsigned long long* list_keys, uint32_t* list_slots, unsigned long long* slot_ids,
+                            int* err) {
     const int kk = blockIdx.x;
     const size_t C = (size_t)1 << logC;
     const unsigned long long* kt = keys + kk * C;
@@ -130,6 +133,7 @@ __global__ void rank_kernel(int k0, const unsigned long long* keys, const uint32
                 const uint32_t slot = ls[e];
                 rank_slot[kk * C + slot] = (uint16_t)(r[q] + 1);
                 cnt_flat[off + r[q] + 1] = cnts[kk * C + slot];
+                if (slot_ids) slot_ids[off + r[q] + 1] = mine[q];  // ids in rank order
             }
         }
     }
@@ -338,11 +342,20 @@ int grid_for(size_t total, int sms) { return (int)std::min<size_t>((total + 255)
 
 }  // namespace
 
+// One candidate tau: its encoding sizes, device memory and analytic time.
+struct TauRow {
+    int tau = 0;
+    size_t d = 0;             // frequent one-hot columns
+    double r = 0, cells = 0;  // rare pairs, cells in rare groups
+    double kb = 0, mem = 0, t = 0;
+    bool fits = false;
+};
+
 // Analytic cost of tau on GB300: tensor-core time for the one-hot columns plus
 // the rare term (fused pair-list walk, or the dense rare-count build), subject
 // to device memory.
-int choose_tau_gb300(const std::vector<uint32_t>& cnt_flat, const std::vector<uint64_t>& off, int n, int L,
-                     size_t free_bytes, const TauModel& m, bool dense, bool verbose) {
+std::vector<TauRow> tau_rows(const std::vector<uint32_t>& cnt_flat, const std::vector<uint64_t>& off, int n, int L,
+                             size_t free_bytes, const TauModel& m, bool dense) {
     std::vector<double> cs;
     for (int k = 0; k < L; k++)
         for (uint64_t q = off[k] + 1; q < off[k + 1]; q++)
@@ -350,43 +363,113 @@ int choose_tau_gb300(const std::vector<uint32_t>& cnt_flat, const std::vector<ui
     const double pairs = (double)n * (double)(n - 1) / 2.0;
     const size_t rows = up((size_t)std::max(n, 1), 256), kp = up((size_t)L, 128);
     const double nl = (double)n * (double)L;
-    int best = 0;
-    double best_t = 1e300;
+    std::vector<TauRow> out;
     for (int tau = 2; tau <= (dense ? 65536 : 4096); tau *= 2) {
-        size_t d = 0;
-        double r = 0, cells = 0;
+        TauRow w;
+        w.tau = tau;
         for (double v : cs) {
-            if (v >= tau) d++;
+            if (v >= tau) w.d++;
             else if (v >= 2) {
-                r += v * (v - 1.0) / 2.0;
-                cells += v;
+                w.r += v * (v - 1.0) / 2.0;
+                w.cells += v;
             }
         }
-        const double kb = (double)(kp + up(d, 128));
-        double mem, t;
-        bool fits;
+        w.kb = (double)(kp + up(w.d, 128));
         if (dense) {  // ranks, own positions, group members (a stripe's counts come later)
-            mem = (double)rows * kb + nl * 6.0 + 4.0 * cells;
-            t = pairs * kb / m.gemm_rate + r / m.dense_rate;
-            fits = mem <= (double)free_bytes && cells < 4.0e9;
+            w.mem = (double)rows * w.kb + nl * 6.0 + 4.0 * w.cells;
+            w.t = pairs * w.kb / m.gemm_rate + w.r / m.dense_rate;
+            w.fits = w.mem <= (double)free_bytes && w.cells < 4.0e9;
         } else {
-            mem = (double)rows * kb + 4.0 * (r + n + 1.0) + 2.0 * (double)n * (double)up((size_t)n, 8) / 4;
-            t = pairs * kb / m.gemm_rate + r / m.rare_rate;
-            fits = mem <= (double)free_bytes && r < 4.0e9;
+            w.mem = (double)rows * w.kb + 4.0 * (w.r + n + 1.0) + 2.0 * (double)n * (double)up((size_t)n, 8) / 4;
+            w.t = pairs * w.kb / m.gemm_rate + w.r / m.rare_rate;
+            w.fits = w.mem <= (double)free_bytes && w.r < 4.0e9;
         }
-        if (verbose)
-            fprintf(stderr, "  tau=%5d  one-hot=%8zu  rare=%14.0f  est %.4fs  vram %.2f GB%s\n", tau, d, r, t,
-                    mem / 1e9, fits ? "" : "  (does not fit)");
-        if (fits && t < best_t) {
-            best = tau;
-            best_t = t;
-        }
+        out.push_back(w);
     }
+    return out;
+}
+
+int choose_tau_analytic(const std::vector<TauRow>& rows) {
+    int best = 0;
+    double best_t = 1e300;
+    for (const TauRow& w : rows)
+        if (w.fits && w.t < best_t) {
+            best = w.tau;
+            best_t = w.t;
+        }
     return best;
 }
 
+// Feature rows of the candidates that fit (the layout tch.h documents).
+void tau_features(const std::vector<TauRow>& rows, const std::vector<uint32_t>& cnt_flat,
+                  const std::vector<uint64_t>& off, int n, int L, TauTable* t) {
+    std::vector<double> lnd((size_t)L);
+    double present = 0;
+    for (int k = 0; k < L; k++) {
+        lnd[k] = log1p((double)(off[k + 1] - off[k] - 1));
+        for (uint64_t q = off[k] + 1; q < off[k + 1]; q++) present += cnt_flat[q];
+    }
+    std::sort(lnd.begin(), lnd.end());
+    auto quant = [&](double f) { return L ? lnd[(size_t)std::min<double>(L - 1, f * (L - 1) + 0.5)] : 0.0; };
+    const double nl = std::max(1.0, (double)n * (double)L);
+    const double pairs = std::max(1.0, (double)n * (double)(n - 1) / 2.0);
+    const float base[6] = {(float)log((double)std::max(n, 1)), (float)log((double)std::max(L, 1)), (float)quant(0.25),
+                           (float)quant(0.5), (float)quant(0.9), (float)(1.0 - present / nl)};
+    t->taus.clear();
+    t->feats.clear();
+    t->est_s.clear();
+    for (const TauRow& w : rows) {
+        if (!w.fits) continue;
+        t->taus.push_back(w.tau);
+        t->est_s.push_back(w.t);
+        for (float b : base) t->feats.push_back(b);
+        t->feats.push_back((float)log((double)w.tau));
+        t->feats.push_back((float)log1p((double)w.d));
+        t->feats.push_back((float)log1p(w.r));
+        t->feats.push_back((float)log1p(w.cells));
+        t->feats.push_back((float)log(pairs * w.kb));
+        t->feats.push_back((float)log(std::max(w.t, 1e-9)));
+    }
+}
+
+// tau <= 0: the learned model's pick when one is set, else the analytic one.
+int choose_tau_gb300(int device, const std::vector<uint32_t>& cnt_flat, const std::vector<uint64_t>& off, int n,
+                     int L, size_t free_bytes, const TauModel& m, bool dense, bool verbose) {
+    const std::vector<TauRow> rows = tau_rows(cnt_flat, off, n, L, free_bytes, m, dense);
+    const int analytic = choose_tau_analytic(rows);
+    int learned = 0;
+    std::vector<float> pred;
+    TauTable t;
+    float w[kMlpParams];
+    if (tau_mlp_weights(w)) {
+        tau_features(rows, cnt_flat, off, n, L, &t);
+        pred.resize(t.taus.size());
+        Err quiet{nullptr, 0};
+        if (!t.taus.empty() && !mlp_run(device, w, t.feats.data(), nullptr, (int)t.taus.size(), pred.data(), nullptr,
+                                        nullptr, quiet)) {
+            float best = INFINITY;
+            for (size_t q = 0; q < t.taus.size(); q++)
+                if (pred[q] < best) best = pred[q], learned = t.taus[q];
+        }
+    }
+    if (verbose) {
+        size_t c = 0;
+        for (const TauRow& r : rows) {
+            fprintf(stderr, "  tau=%5d  one-hot=%8zu  rare=%14.0f  est %.4fs  vram %.2f GB%s", r.tau, r.d, r.r, r.t,
+                    r.mem / 1e9, r.fits ? "" : "  (does not fit)");
+            if (r.fits && c < pred.size() && t.taus[c] == r.tau) fprintf(stderr, "  learned %.2f ms", exp(pred[c++]));
+            fprintf(stderr, "\n");
+        }
+        fprintf(stderr, "  tau: analytic %d, learned %d\n", analytic, learned);
+    }
+    return learned ? learned : analytic;
+}
+
 int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_req, const TauModel& model,
-                     bool verbose, size_t max_chunk_bytes, bool dense_rare, DeviceEncoding* out, Err& e) {
+                     bool verbose, size_t max_chunk_bytes, int flags, DeviceEncoding* out, Err& e,
+                     TauTable* table) {
+    const bool dense_rare = (flags & (ENC_DENSE | ENC_QUERY)) != 0;
+    const bool query_maps = (flags & ENC_QUERY) != 0;
     int sms = 0, hflag = 0;
     size_t freeb = 0, totb = 0, tmp_bytes = 0;
     int logC = 10;
@@ -402,6 +485,7 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
     unsigned long long* list_keys = nullptr;
     uint64_t *cnt_off_d = nullptr, *goff_d = nullptr, *groups_d = nullptr, *start64 = nullptr;
     int32_t* col_d = nullptr;
+    unsigned long long* slot_ids = nullptr;
     int* err_d = nullptr;
     std::vector<uint32_t> nd_h(L), cnt_h;
     std::vector<uint64_t> off_h((size_t)L + 1, 0);
@@ -457,6 +541,10 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
         TCH_CK(e, cudaMemcpy(cnt_off_d, off_h.data(), ((size_t)L + 1) * 8, cudaMemcpyHostToDevice));
         TCH_CK(e, dalloc(&cnt_flat, off_h[L], &tmp_bytes));
         TCH_CK(e, cudaMemset(cnt_flat, 0, std::max<uint64_t>(off_h[L], 1) * 4));
+        if (query_maps) {
+            TCH_CK(e, dalloc(&slot_ids, off_h[L], nullptr));
+            TCH_CK(e, cudaMemset(slot_ids, 0, std::max<uint64_t>(off_h[L], 1) * 8));
+        }
         const bool one_batch = nk_max >= L;  // the first sweep's tables are still in place
         if (!one_batch) TCH_CK(e, cudaMemset(nd, 0, (size_t)L * 4));
         for (int k0 = 0; k0 < L; k0 += nk_max) {
@@ -469,7 +557,7 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
                 TCH_CK(e, cudaGetLastError());
             }
             rank_kernel<<<nk, 512>>>(k0, keys, cnts, logC, nd, cnt_off_d, cnt_flat, rank_slot, list_keys, list_slots,
-                                     err_d);
+                                     slot_ids, err_d);
             TCH_CK(e, cudaGetLastError());
             cell_rank_kernel<<<grid_for((size_t)n * nk, sms), 256>>>(d_calls, n, L, k0, nk, keys, rank_slot, logC,
                                                                       out->x, err_d);
@@ -491,8 +579,13 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
     {
         int tau = tau_req;
         TCH_CK(e, cudaMemGetInfo(&freeb, &totb));
+        if (table) {  // candidates and features only
+            tau_features(tau_rows(cnt_h, off_h, n, L, freeb, model, dense_rare), cnt_h, off_h, n, L, table);
+            free_device_encoding(out);
+            goto done;
+        }
         if (tau <= 0) {
-            tau = choose_tau_gb300(cnt_h, off_h, n, L, freeb, model, dense_rare, verbose);
+            tau = choose_tau_gb300(device, cnt_h, off_h, n, L, freeb, model, dense_rare, verbose);
             if (!tau) { e.set("no tau fits in %.2f GB of free device memory", freeb / 1e9); goto fail; }
         }
         out->tau = tau;
@@ -510,7 +603,9 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
                 const uint32_t c = cnt_h[q];
                 const bool freq = is_rank && c >= (uint32_t)tau;
                 if (freq) col[q] = (int32_t)d++;
-                const bool rare = is_rank && !freq && c >= 2;
+                // a query database also keeps single-row groups: a new profile with that
+                // allele equals its one row
+                const bool rare = is_rank && !freq && c >= (query_maps ? 1u : 2u);
                 goff[q + 1] = goff[q] + (rare ? c : 0);
                 if (rare) {
                     groups.push_back(goff[q]);
@@ -586,6 +681,15 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
             out->members = sorted;
             out->mpos = mpos;
             out->bytes += ((size_t)L + 1) * 8 + (off_h[L] + 1) * 8 + n_members * 4 + (size_t)n * L * 4;
+            if (query_maps) {  // what new profiles need to be encoded like these
+                out->slot_ids = reinterpret_cast<uint64_t*>(slot_ids);
+                out->col = col_d;
+                out->base = base_d;
+                out->bytes += off_h[L] * 12 + ((size_t)L + 1) * 4;
+                slot_ids = nullptr;
+                col_d = nullptr;
+                base_d = nullptr;
+            }
             cnt_off_d = nullptr;
             goff_d = nullptr;
             sorted = nullptr;
@@ -634,13 +738,13 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
 done:
     cudaFree(err_d); cudaFree(nd); cudaFree(cnt_off_d); cudaFree(cnt_flat); cudaFree(col_d); cudaFree(base_d);
     cudaFree(goff_d); cudaFree(members); cudaFree(sorted); cudaFree(gfill); cudaFree(groups_d); cudaFree(row_count);
-    cudaFree(start64); cudaFree(mpos);
+    cudaFree(start64); cudaFree(mpos); cudaFree(slot_ids);
     return 0;
 fail:
     cudaFree(err_d); cudaFree(nd); cudaFree(cnt_off_d); cudaFree(cnt_flat); cudaFree(col_d); cudaFree(base_d);
     cudaFree(goff_d); cudaFree(members); cudaFree(sorted); cudaFree(gfill); cudaFree(groups_d); cudaFree(row_count);
     cudaFree(start64); cudaFree(keys); cudaFree(cnts); cudaFree(rank_slot); cudaFree(list_keys); cudaFree(list_slots);
-    cudaFree(mpos);
+    cudaFree(mpos); cudaFree(slot_ids);
     free_device_encoding(out);
     return 1;
 }
@@ -654,6 +758,12 @@ void free_device_encoding(DeviceEncoding* d) {
     cudaFree(d->goff);
     cudaFree(d->members);
     cudaFree(d->mpos);
+    cudaFree(d->slot_ids);
+    cudaFree(d->col);
+    cudaFree(d->base);
+    d->slot_ids = nullptr;
+    d->col = nullptr;
+    d->base = nullptr;
     d->x = nullptr;
     d->X = KChunks();
     d->start = d->js = nullptr;

@@ -80,6 +80,81 @@ __device__ __forceinline__ void count_col(uint32_t* cnt, uint32_t c) {
     atomicAdd(cnt + (c >> 1), 1u << ((c & 1u) * 16u));
 }
 
+// Lays this thread's two runs (l0 partners from members[lo0], l1 from
+// members[lo1]) end to end with every other thread's by a block-wide scan, cuts
+// the total into one equal part per warp and counts every partner j at column
+// j - wb.  Called by all threads of the CTA (it synchronises them).
+__device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_t* run, uint32_t* wsum, uint32_t l0,
+                                           uint32_t lo0, uint32_t l1, uint32_t lo1,
+                                           const uint32_t* __restrict__ members, int wb) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NWARPS = RD_THREADS / 32;
+    const uint32_t mine = l0 + l1;
+    uint32_t inc = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, inc, d);
+        if (lane >= d) inc += t;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();  // also orders the counter zeroing and the previous chunk's readers
+    if (warp == 0) {
+        const uint32_t v = wsum[lane];
+        uint32_t x = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(FULL, x, d);
+            if (lane >= d) x += t;
+        }
+        wsum[lane] = x - v;
+        if (lane == 31) pre[RD_LOCI] = x;
+    }
+    __syncthreads();
+    const uint32_t ex = wsum[warp] + inc - mine;
+    pre[2 * tid] = ex;
+    pre[2 * tid + 1] = ex + l0;
+    run[2 * tid] = lo0;
+    run[2 * tid + 1] = lo1;
+    __syncthreads();
+    const uint32_t total = pre[RD_LOCI];
+    // warp w takes the items [w * part, (w + 1) * part) and walks them run
+    // by run, its 32 lanes on consecutive members of a run
+    const uint32_t part = (total + NWARPS - 1) / NWARPS;
+    uint32_t e = min(total, (uint32_t)warp * part);
+    const uint32_t e_end = min(total, e + part);
+    if (e < e_end) {
+        int lo = 0, hi = RD_LOCI;  // the run holding item e: the last p with pre[p] <= e
+        while (hi - lo > 1) {
+            const int m = (lo + hi) >> 1;
+            if (pre[m] <= e) lo = m; else hi = m;
+        }
+        for (int p = lo; e < e_end; p++) {
+            const uint32_t stop = min(pre[p + 1], e_end);
+            if (stop <= e) continue;  // an empty run
+            const uint32_t* src = members + run[p] + (e - pre[p]);
+            const uint32_t c = stop - e;
+            uint32_t k = (uint32_t)lane;
+            for (; k + 224 < c; k += 256) {  // eight loads in flight per lane
+                uint32_t jj[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) jj[u] = __ldg(src + k + 32 * u);
+#pragma unroll
+                for (int u = 0; u < 8; u++) count_col(cnt, jj[u] - (uint32_t)wb);
+            }
+            if (k + 96 < c) {
+                uint32_t jj[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) jj[u] = __ldg(src + k + 32 * u);
+#pragma unroll
+                for (int u = 0; u < 4; u++) count_col(cnt, jj[u] - (uint32_t)wb);
+                k += 128;
+            }
+            for (; k < c; k += 32) count_col(cnt, __ldg(src + k) - (uint32_t)wb);
+            e = stop;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(RD_THREADS, 1)
     rare_dense_kernel(const RareGroups g, int r0, int rows, uint16_t* __restrict__ R, size_t ldr, int cend) {
     extern __shared__ uint4 smem_rd[];
@@ -87,8 +162,7 @@ __global__ void __launch_bounds__(RD_THREADS, 1)
     uint32_t* pre = cnt + RD_WORDS;        // RD_LOCI + 1: exclusive prefix of the run lengths
     uint32_t* run = pre + RD_LOCI + 1;     // RD_LOCI: first member index of each run
     uint32_t* wsum = run + RD_LOCI;        // 32: per-warp totals of the scan
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr int NWARPS = RD_THREADS / 32;
+    const int tid = threadIdx.x;
     const int n = g.n, L = g.L;
     // with every locus in one scan (L <= RD_LOCI) a thread keeps the same two
     // loci for all rows: their count offsets stay in registers and the next
@@ -124,73 +198,60 @@ __global__ void __launch_bounds__(RD_THREADS, 1)
                     if (k0 < L) l0 = partner_run(g, i, c.a0, c.m0, g.cnt_off[k0], jlo, jhi, &lo0);
                     if (k0 + 1 < L) l1 = partner_run(g, i, c.a1, c.m1, g.cnt_off[k0 + 1], jlo, jhi, &lo1);
                 }
-                const uint32_t mine = l0 + l1;
-                uint32_t inc = mine;
-#pragma unroll
-                for (int d = 1; d < 32; d <<= 1) {
-                    const uint32_t t = __shfl_up_sync(FULL, inc, d);
-                    if (lane >= d) inc += t;
-                }
-                if (lane == 31) wsum[warp] = inc;
-                __syncthreads();  // also orders the counter zeroing and the previous chunk's readers
-                if (warp == 0) {
-                    const uint32_t v = wsum[lane];
-                    uint32_t x = v;
-#pragma unroll
-                    for (int d = 1; d < 32; d <<= 1) {
-                        const uint32_t t = __shfl_up_sync(FULL, x, d);
-                        if (lane >= d) x += t;
-                    }
-                    wsum[lane] = x - v;
-                    if (lane == 31) pre[RD_LOCI] = x;
-                }
-                __syncthreads();
-                const uint32_t ex = wsum[warp] + inc - mine;
-                pre[2 * tid] = ex;
-                pre[2 * tid + 1] = ex + l0;
-                run[2 * tid] = lo0;
-                run[2 * tid + 1] = lo1;
-                __syncthreads();
-                const uint32_t total = pre[RD_LOCI];
-                // warp w takes the items [w * part, (w + 1) * part) and walks them run
-                // by run, its 32 lanes on consecutive members of a run
-                const uint32_t part = (total + NWARPS - 1) / NWARPS;
-                uint32_t e = min(total, (uint32_t)warp * part);
-                const uint32_t e_end = min(total, e + part);
-                if (e < e_end) {
-                    int lo = 0, hi = RD_LOCI;  // the run holding item e: the last p with pre[p] <= e
-                    while (hi - lo > 1) {
-                        const int m = (lo + hi) >> 1;
-                        if (pre[m] <= e) lo = m; else hi = m;
-                    }
-                    for (int p = lo; e < e_end; p++) {
-                        const uint32_t stop = min(pre[p + 1], e_end);
-                        if (stop <= e) continue;  // an empty run
-                        const uint32_t* src = g.members + run[p] + (e - pre[p]);
-                        const uint32_t c = stop - e;
-                        uint32_t k = (uint32_t)lane;
-                        for (; k + 224 < c; k += 256) {  // eight loads in flight per lane
-                            uint32_t jj[8];
-#pragma unroll
-                            for (int u = 0; u < 8; u++) jj[u] = __ldg(src + k + 32 * u);
-#pragma unroll
-                            for (int u = 0; u < 8; u++) count_col(cnt, jj[u] - (uint32_t)wb);
-                        }
-                        if (k + 96 < c) {
-                            uint32_t jj[4];
-#pragma unroll
-                            for (int u = 0; u < 4; u++) jj[u] = __ldg(src + k + 32 * u);
-#pragma unroll
-                            for (int u = 0; u < 4; u++) count_col(cnt, jj[u] - (uint32_t)wb);
-                            k += 128;
-                        }
-                        for (; k < c; k += 32) count_col(cnt, __ldg(src + k) - (uint32_t)wb);
-                        e = stop;
-                    }
-                }
+                count_runs(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, wb);
             }
             __syncthreads();
             uint4* dst = Rrow + ((wb - cbeg) >> 3);
+            for (int w = tid; w < nq; w += RD_THREADS) dst[w] = smem_rd[w];
+            __syncthreads();
+        }
+    }
+}
+
+// Group run of a new profile at locus k: every member of the group of its
+// allele (a = its rank in the groups' numbering; 0 missing, kNovelRank not in
+// the set), clipped to columns [jlo, jhi).
+__device__ __forceinline__ uint32_t group_run(const RareGroups& g, uint32_t a, uint64_t coff, uint32_t jlo,
+                                              uint32_t jhi, uint32_t* lo_out) {
+    if (!a || a == kNovelRank) return 0;
+    const uint64_t q = coff + a;
+    uint64_t b = __ldg(g.goff + q), e = __ldg(g.goff + q + 1);
+    if (e <= b) return 0;  // frequent in the set: counted by the one-hot columns
+    if (jlo > 0 && __ldg(g.members + b) < jlo) b = lower_bound_m(g.members, b, e, jlo);
+    if (jhi < (uint32_t)g.n && b < e && __ldg(g.members + e - 1) >= jhi) e = lower_bound_m(g.members, b, e, jhi);
+    *lo_out = (uint32_t)b;
+    return (uint32_t)(e - b);
+}
+
+// Rare counts of m new profiles against every row of the set:
+// R[r * ldr + j] = loci where new profile r and row j share an allele that is
+// rare in the set, for j < n (0 up to cend).  Same counting as rare_dense_kernel.
+__global__ void __launch_bounds__(RD_THREADS, 1)
+    rare_query_kernel(const RareGroups g, const uint32_t* __restrict__ xq, int m, uint16_t* __restrict__ R,
+                      size_t ldr, int cend) {
+    extern __shared__ uint4 smem_rd[];
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(smem_rd);
+    uint32_t* pre = cnt + RD_WORDS;
+    uint32_t* run = pre + RD_LOCI + 1;
+    uint32_t* wsum = run + RD_LOCI;
+    const int tid = threadIdx.x;
+    const int n = g.n, L = g.L;
+    for (int r = blockIdx.x; r < m; r += gridDim.x) {
+        uint4* Rrow = reinterpret_cast<uint4*>(R + (size_t)r * ldr);
+        for (int wb = 0; wb < cend; wb += RD_COLS) {
+            const int we = min(cend, wb + RD_COLS);
+            const int nq = (we - wb) >> 3;
+            for (int w = tid; w < nq; w += RD_THREADS) smem_rd[w] = make_uint4(0, 0, 0, 0);
+            const uint32_t jlo = (uint32_t)wb, jhi = (uint32_t)min(we, n);
+            for (int kc = 0; jlo < jhi && kc < L; kc += RD_LOCI) {
+                const int k0 = kc + 2 * tid;
+                uint32_t lo0 = 0, lo1 = 0, l0 = 0, l1 = 0;
+                if (k0 < L) l0 = group_run(g, xq[(size_t)r * L + k0], g.cnt_off[k0], jlo, jhi, &lo0);
+                if (k0 + 1 < L) l1 = group_run(g, xq[(size_t)r * L + k0 + 1], g.cnt_off[k0 + 1], jlo, jhi, &lo1);
+                count_runs(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, wb);
+            }
+            __syncthreads();
+            uint4* dst = Rrow + (wb >> 3);
             for (int w = tid; w < nq; w += RD_THREADS) dst[w] = smem_rd[w];
             __syncthreads();
         }
@@ -209,6 +270,21 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
     if (e != cudaSuccess) return e;
     const int grid = std::max(1, std::min(rows, sms));
     rare_dense_kernel<<<grid, RD_THREADS, smem, st>>>(g, r0, rows, R, ldr, r0 + (int)width);
+    return cudaGetLastError();
+}
+
+}  // namespace tch
+
+namespace tch {
+
+cudaError_t launch_rare_query(const RareGroups& g, const uint32_t* xq, int m, uint16_t* R, size_t ldr, int sms,
+                              cudaStream_t st) {
+    if (m <= 0) return cudaSuccess;
+    const size_t width = up((size_t)std::max(g.n, 1), kRareDenseAlign);
+    if (ldr < width || (ldr & 7) || ((uintptr_t)R & 15)) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(rare_query_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, RD_SMEM);
+    if (e != cudaSuccess) return e;
+    rare_query_kernel<<<std::max(1, std::min(m, sms)), RD_THREADS, RD_SMEM, st>>>(g, xq, m, R, ldr, (int)width);
     return cudaGetLastError();
 }
 

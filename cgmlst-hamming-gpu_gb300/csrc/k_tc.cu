@@ -78,14 +78,18 @@ int group_row_blocks() {
 }
 
 struct TileSpace {
-    int nsr, nbj;  // super-rows of the stripe, column blocks of [r0, n)
+    int nsr, nbj;  // super-rows of the stripe, column blocks of [c0, n)
     int cm;        // row blocks per super-row (cluster size)
     int gs;        // super-rows per raster group
+    int rect;      // 1: every tile of the rectangle (rows of one set against columns of another)
 };
 
 // Columns of super-row sr: bj >= sr * cm / 2 (128-row blocks against 256-wide
-// column blocks that both start at r0; earlier columns lie below the diagonal).
-__host__ __device__ __forceinline__ int first_col(const TileSpace& ts, int sr) { return sr * ts.cm / 2; }
+// column blocks that both start at r0; earlier columns lie below the diagonal);
+// all of them for a rectangle.
+__host__ __device__ __forceinline__ int first_col(const TileSpace& ts, int sr) {
+    return ts.rect ? 0 : sr * ts.cm / 2;
+}
 
 __host__ __device__ __forceinline__ long long count_tiles(const TileSpace& ts) {
     long long c = 0;
@@ -122,7 +126,7 @@ __device__ bool tile_coords(const TileSpace& ts, const GroupTable& gt, int t, in
     // columns where only part of the group lies on or above the diagonal
     // (super-row sr is present in column bj iff sr * cm <= 2 bj + 1)
     int bj = first_col(ts, g0);
-    for (; bj < ts.nbj; bj++) {
+    for (; !ts.rect && bj < ts.nbj; bj++) {
         const int rows = min(g1 - 1, (2 * bj + 1) / ts.cm) - g0 + 1;
         if (rows == g1 - g0) break;  // from here on every column holds the whole group
         if (rows > 0) {
@@ -152,7 +156,8 @@ struct TcMaps {
 };
 
 struct TcParams {
-    int n, r0, rows;
+    int n, r0, rows;  // columns end at n; rows [r0, r0 + rows) of the A operand
+    int c0;           // first column: r0 (upper triangle) or 0 (rectangle against the B operand)
     int kblocks, kblocks_p;  // K stages in total and in the presence part
     TileSpace ts;
     GroupTable gt;
@@ -245,7 +250,7 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
                 int sr, bj;
                 if (!tile_coords(p.ts, p.gt, t, &sr, &bj)) break;
                 const int bi = sr * CM + (int)rank;
-                const int y_a = p.r0 + bi * BM, y_b = p.r0 + bj * BN + (int)rank * (BN / CM);
+                const int y_a = p.r0 + bi * BM, y_b = p.c0 + bj * BN + (int)rank * (BN / CM);
                 int ch = 0, kbl = 0;  // K chunk and block inside it
                 for (int kb = 0; kb < p.kblocks; kb++) {
                     if (!mbar_wait(&empty[s], ph ^ 1, abort_flag, p.err)) { ok = false; break; }
@@ -330,7 +335,7 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
             int sr, bj;
             if (!tile_coords(p.ts, p.gt, t, &sr, &bj)) break;
             const int bi = sr * CM + (int)rank;
-            const int i0 = p.r0 + bi * BM, j0 = p.r0 + bj * BN;
+            const int i0 = p.r0 + bi * BM, j0 = p.c0 + bj * BN;
             const int my_i = i0 + q * 32 + lane;
             // this row's rare partners inside the tile: an ascending run of js
             uint32_t rp = 0, rhi = 0;
@@ -354,7 +359,7 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
                 uint4 rq[4] = {};
                 if (dense && my_i < iend) {
                     const uint4* src = reinterpret_cast<const uint4*>(p.rdense + (size_t)(my_i - p.r0) * p.ldr +
-                                                                      (size_t)(cb - (uint32_t)p.r0));
+                                                                      (size_t)(cb - (uint32_t)p.c0));
 #pragma unroll
                     for (int u = 0; u < 4; u++) rq[u] = __ldg(src + u);
                 }
@@ -418,7 +423,7 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
                     const int j = (int)cb + 2 * w;
                     if (i < iend && j < p.n) {
                         const uint32_t val = reinterpret_cast<const uint32_t*>(stg + rr * EPI_PITCH)[w];
-                        uint16_t* dst = p.out + (size_t)(i - p.r0) * p.ldo + (size_t)(j - p.r0);
+                        uint16_t* dst = p.out + (size_t)(i - p.r0) * p.ldo + (size_t)(j - p.c0);
                         if (j + 1 < p.n) *reinterpret_cast<uint32_t*>(dst) = val;
                         else *dst = (uint16_t)(val & 0xFFFF);
                     }
@@ -467,8 +472,22 @@ bool make_map(CUtensorMap* m, const uint8_t* X, size_t rows, int kb, int box_row
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The K chunks of an operand (one chunk when it is a single allocation).
+KChunks chunks_of(const ByteOperands& ops) {
+    KChunks ch = ops.chunks;
+    if (ch.n == 0) {
+        ch.p[0] = const_cast<uint8_t*>(ops.X);
+        ch.n = 1;
+        ch.width = ops.kb;
+        ch.kb = ops.kb;
+    }
+    return ch;
+}
+
+// ops: the A operand (the stripe's rows); bops: the B operand (the columns),
+// the same rows for the upper triangle, another set for a rectangle.
 template <int KIND, int CM>
-cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCSR& rare, const StripeArgs& a,
+cudaError_t launch_kind(const ByteOperands& ops, const ByteOperands& bops, const RareCSR& rare, const StripeArgs& a,
                         int num_sms, cudaStream_t st) {
     static bool attr = false;
     static int max_clusters = 0;
@@ -498,35 +517,34 @@ cudaError_t launch_kind(const ByteOperands& ops, const uint8_t* xb, const RareCS
         attr = true;
     }
     if ((ops.kb % BK) || (ops.kp % BK) || ops.kb <= 0) return cudaErrorInvalidValue;
+    if (bops.kb != ops.kb || bops.kp != ops.kp) return cudaErrorInvalidValue;
     if ((a.ldo & 1) || ((uintptr_t)a.out & 3)) return cudaErrorInvalidValue;
-    (void)xb;
-    KChunks ch = ops.chunks;
-    if (ch.n == 0) {  // one allocation
-        ch.p[0] = const_cast<uint8_t*>(ops.X);
-        ch.n = 1;
-        ch.width = ops.kb;
-        ch.kb = ops.kb;
-    }
+    if (a.rect && !rare.dense && rare.n_rare > 0) return cudaErrorInvalidValue;  // rectangles take dense counts
+    const KChunks ch = chunks_of(ops), chb = chunks_of(bops);
     if (ch.kb != ops.kb || (ch.width % BK)) return cudaErrorInvalidValue;
+    if (chb.n != ch.n || chb.width != ch.width || chb.kb != ch.kb) return cudaErrorInvalidValue;
     TcMaps maps;
     maps.n = ch.n;
     for (int c = 0; c < ch.n; c++) {
         const int wc = ch.width_of(c);
         if (wc <= 0 || (wc % BK)) return cudaErrorInvalidValue;
-        if (!make_map(&maps.a[c], ch.p[c], ops.n_rows, wc, BM) || !make_map(&maps.b[c], ch.p[c], ops.n_rows, wc, BN / CM))
+        if (!make_map(&maps.a[c], ch.p[c], ops.n_rows, wc, BM) ||
+            !make_map(&maps.b[c], chb.p[c], bops.n_rows, wc, BN / CM))
             return cudaErrorInvalidValue;
         maps.kblocks[c] = wc / BK;
     }
     TcParams p;
     p.n = a.n;
     p.r0 = a.r0;
+    p.c0 = a.rect ? 0 : a.r0;
     p.rows = a.rows;
     p.kblocks = ops.kb / BK;
     p.kblocks_p = ops.kp / BK;
     p.ts.cm = CM;
     p.ts.gs = group_row_blocks() / CM;
     p.ts.nsr = ((a.rows + BM - 1) / BM + CM - 1) / CM;
-    p.ts.nbj = (a.n - a.r0 + BN - 1) / BN;
+    p.ts.rect = a.rect ? 1 : 0;
+    p.ts.nbj = (a.n - p.c0 + BN - 1) / BN;
     p.num_tiles = (int)count_tiles(p.ts);
     {
         const int gs = p.ts.gs;
@@ -575,10 +593,11 @@ int cluster_size() {
 // supported on .target 'sm_103a'"), so TCH_KERNEL_TC_I8 is never compiled in.
 bool tc_kernel_compiled(int kernel) { return kernel == TCH_KERNEL_TC_F8; }
 
-cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t* Xneg, const RareCSR& rare,
+cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const ByteOperands* bops, const RareCSR& rare,
                              const StripeArgs& a, int num_sms, cudaStream_t st) {
-    (void)Xneg;
-    if (a.rows <= 0 || a.r0 >= a.n) return cudaSuccess;
+    if (a.rows <= 0 || (!a.rect && a.r0 >= a.n) || (a.rect && a.n <= 0)) return cudaSuccess;
+    if (a.rect && !bops) return cudaErrorInvalidValue;
+    const ByteOperands& b = bops ? *bops : ops;
     if (kernel != TCH_KERNEL_TC_F8) return cudaErrorNotSupported;
     // one launch covers at most MAX_GROUPS raster groups of rows; a taller
     // stripe runs as consecutive sub-stripes writing into the same output
@@ -587,11 +606,12 @@ cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t*
         StripeArgs s = a;
         s.r0 = a.r0 + done;
         s.rows = std::min(max_rows, a.rows - done);
-        s.out = a.out + (size_t)done * a.ldo + (size_t)done;
+        const size_t col = a.rect ? 0 : (size_t)done;  // a triangle's columns start at its first row
+        s.out = a.out + (size_t)done * a.ldo + col;
         RareCSR rs = rare;
-        if (rare.dense) rs.dense = rare.dense + (size_t)done * rare.ldr + (size_t)done;
-        const cudaError_t e = cluster_size() == 2 ? launch_kind<KIND_F8, 2>(ops, ops.X, rs, s, num_sms, st)
-                                                  : launch_kind<KIND_F8, 1>(ops, ops.X, rs, s, num_sms, st);
+        if (rare.dense) rs.dense = rare.dense + (size_t)done * rare.ldr + col;
+        const cudaError_t e = cluster_size() == 2 ? launch_kind<KIND_F8, 2>(ops, b, rs, s, num_sms, st)
+                                                  : launch_kind<KIND_F8, 1>(ops, b, rs, s, num_sms, st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;

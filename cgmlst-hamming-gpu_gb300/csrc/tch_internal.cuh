@@ -7,6 +7,7 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "tch.h"
 
@@ -103,11 +104,15 @@ inline int chunk_width_for(int kb, size_t rows, size_t max_bytes) {
     return n > (size_t)kMaxKChunks ? 0 : (int)w;
 }
 
+// Upper triangle: rows [r0, r0 + rows) against columns [r0, n) of the same
+// set, out[(i - r0) * ldo + (j - r0)].  Rectangle (rect): rows [r0, r0 + rows)
+// of one set against columns [0, n) of another, out[(i - r0) * ldo + j].
 struct StripeArgs {
     int n = 0, r0 = 0, rows = 0;
     uint16_t* out = nullptr;
     size_t ldo = 0;
     int* err = nullptr;
+    bool rect = false;
 };
 
 // ---- k_popc.cu --------------------------------------------------------------------
@@ -134,7 +139,9 @@ cudaError_t launch_expand_bits_chunked(const BitOperands& bits, int n, size_t n_
 
 // ---- k_tc.cu ----------------------------------------------------------------------
 bool tc_kernel_compiled(int kernel);
-cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const uint8_t* Xneg, const RareCSR& rare,
+// ops: the rows' operand; bops: the columns' operand (nullptr = ops; required
+// for a rectangle, with the same K layout and chunking as ops).
+cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const ByteOperands* bops, const RareCSR& rare,
                              const StripeArgs& a, int num_sms, cudaStream_t st);
 
 // ---- k_encode.cu ------------------------------------------------------------------
@@ -164,6 +171,13 @@ struct RareGroups {
 // ~255), up to r0 + up(n - r0, 256); columns before that are left as they
 // are.  ldr >= up(n - r0, 256) and a multiple of 8; R 16-byte aligned.
 constexpr int kRareDenseAlign = 256;
+// Rank of an id that a profile set has never seen (new-profile encoding).
+constexpr uint32_t kNovelRank = 0xFFFFFFFFu;
+// R[r * ldr + j] = loci where new profile r (ranks xq, m x L u32 in the set's
+// numbering) and row j of the set share an allele that is rare in the set
+// (groups must include single-row groups), for j < n; 0 up to up(n, 256).
+cudaError_t launch_rare_query(const RareGroups& g, const uint32_t* xq, int m, uint16_t* R, size_t ldr, int sms,
+                              cudaStream_t st);
 cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R, size_t ldr, int sms,
                               cudaStream_t st);
 
@@ -184,11 +198,40 @@ struct DeviceEncoding {
     uint64_t* goff = nullptr;
     uint32_t* members = nullptr;
     uint32_t* mpos = nullptr;
+    // query maps (ENC_QUERY): ids in rank order per locus (slot cnt_off[k] + rank,
+    // ascending), frequent column of each slot (-1 = rare), per-locus column base
+    uint64_t* slot_ids = nullptr;
+    int32_t* col = nullptr;
+    uint32_t* base = nullptr;
     size_t bytes = 0;
 };
 
+// encode_on_device flags: ENC_DENSE keeps the rare groups (dense rare counts)
+// instead of building pair lists; ENC_QUERY (implies dense) also keeps
+// single-row groups and the maps that encode new profiles like these.
+enum EncodeFlags : int { ENC_DENSE = 1, ENC_QUERY = 2 };
+
+// Candidate taus of an encoding and their learned-model feature rows.
+struct TauTable {
+    std::vector<int> taus;
+    std::vector<float> feats;   // taus.size() x TCH_TAU_FEATURES
+    std::vector<double> est_s;  // analytic estimate per candidate
+};
+
+// With table != nullptr the encoder stops after the counts and fills it.
 int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_req, const TauModel& model,
-                     bool verbose, size_t max_chunk_bytes, bool dense_rare, DeviceEncoding* out, Err& e);
+                     bool verbose, size_t max_chunk_bytes, int flags, DeviceEncoding* out, Err& e,
+                     TauTable* table = nullptr);
 void free_device_encoding(DeviceEncoding* d);
+
+// ---- k_mlp.cu ----------------------------------------------------------------------
+constexpr int kMlpIn = TCH_TAU_FEATURES, kMlpHidden = TCH_MLP_HIDDEN, kMlpParams = TCH_MLP_PARAMS;
+// pred / loss / grad optional; y required for loss and grad.
+int mlp_run(int device, const float* w, const float* X, const float* y, int n, float* pred, float* loss,
+            float* grad, Err& e);
+int mlp_train(int device, float* w, const float* X, const float* y, int n, int steps, float lr, float* loss_out,
+              Err& e);
+// The model set by tch_set_tau_mlp, if any.
+bool tau_mlp_weights(float* out);
 
 }  // namespace tch

@@ -372,8 +372,8 @@ static int solver_from_calls(int device, int n, int L, const uint64_t* calls, in
     } else {
         TCH_CK(e, cudaMemset(d_calls, 0, std::max<size_t>((size_t)n, 1) * 8));
     }
-    if (encode_on_device(device, n, Le, d_calls, tau, g_tau_model, verbose, max_chunk_bytes(), rare_dense_default(),
-                         &enc, e))
+    if (encode_on_device(device, n, Le, d_calls, tau, g_tau_model, verbose, max_chunk_bytes(),
+                         rare_dense_default() ? ENC_DENSE : 0, &enc, e))
         goto fail;
     cudaFree(d_calls);
     d_calls = nullptr;
@@ -789,6 +789,35 @@ int tch_run_calls(int device, int n, int L, const uint64_t* calls, int tau, int 
     const int rc = n > 0 ? solver_run(s, S, cb, ctx, gpu_secs, e) : 0;
     solver_free(s);
     return rc;
+}
+
+int tch_tau_features(int device, int n, int L, const uint64_t* calls, int max_rows, int* taus, float* feats,
+                     double* est_s, int* rows, char* err, int errlen) {
+    Err e{err, errlen};
+    uint64_t* d_calls = nullptr;
+    DeviceEncoding enc;
+    TauTable table;
+    if (n < 2 || L < 1) return e.set("need n >= 2 profiles and L >= 1 loci (got n=%d, L=%d)", n, L);
+    if (L > 65535) return e.set("more than 65535 loci (u16 distances)");
+    if (!calls || !taus || !feats || !rows || max_rows < 0) return e.set("null buffer");
+    TCH_CK(e, cudaSetDevice(device));
+    TCH_CK(e, cudaMalloc(&d_calls, (size_t)n * L * 8));
+    TCH_CK(e, cudaMemcpy(d_calls, calls, (size_t)n * L * 8, cudaMemcpyHostToDevice));
+    if (encode_on_device(device, n, L, d_calls, 0, g_tau_model, false, 0, rare_dense_default() ? ENC_DENSE : 0, &enc,
+                         e, &table))
+        goto fail;
+    cudaFree(d_calls);
+    *rows = (int)std::min<size_t>(table.taus.size(), (size_t)max_rows);
+    for (int r = 0; r < *rows; r++) {
+        taus[r] = table.taus[r];
+        if (est_s) est_s[r] = table.est_s[r];
+        for (int f = 0; f < TCH_TAU_FEATURES; f++) feats[(size_t)r * TCH_TAU_FEATURES + f] =
+            table.feats[(size_t)r * TCH_TAU_FEATURES + f];
+    }
+    return 0;
+fail:
+    if (d_calls) cudaFree(d_calls);
+    return 1;
 }
 
 int tch_set_max_chunk_bytes(size_t bytes) {

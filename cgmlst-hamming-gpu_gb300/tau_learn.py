@@ -1,0 +1,217 @@
+"""Training data and training of the learned tau model.
+
+    python -m tau_learn sweep  [--datasets 240] [--out tau_sweep_gb300.npz]
+    python -m tau_learn train  [--sweep tau_sweep_gb300.npz] [--out tau_mlp_gb300.f32]
+
+(run from this directory, or ``python cgmlst-hamming-gpu_gb300/tau_learn.py``).
+
+sweep: seeded synthetic profile sets of varied shape (n log-uniform in
+[2 000, 63 005], L from the shapes the configs name, n x L <= 7.2e7; three in
+four Zipf (s in [1.0, 1.4], lognormal distinct-allele counts, 5 % 64-bit ids),
+one in four founder models (3-60 alleles per locus, 0.2-5 % mutations to new
+ids); 0-8 % missing).  For each set
+the library's own feature rows (tch_tau_features) and, for each candidate tau
+near the analytic pick, the measured device time of one whole-triangle solve
+(rare counts + tile pass, CUDA events, median of 3).
+
+train: the MLP of csrc/k_mlp.cu on ln(ms), trained on the GPU by the library's
+kernels (tch_mlp_train), every fifth profile set held out.  Feature
+standardisation is folded into the first layer, so the saved model takes the
+raw feature rows.  The report compares, on the held-out sets, the measured time
+at the learned pick, at the analytic pick and at the best swept tau.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+tch = importlib.import_module("cgmlst-hamming-gpu_gb300")
+synth = importlib.import_module("cgmlst-hamming-gpu_gb300.synth")
+
+SWEEP_PATH = os.path.join(HERE, "tau_sweep_gb300.npz")
+REPORT_PATH = os.path.join(HERE, "tau_mlp_gb300.json")
+LOCI = (500, 1142, 1343, 2000, 2794, 3016)
+
+
+def dataset_params(seed: int) -> dict:
+    """Shape and allele law of profile set `seed`: one in four is a founder
+    model (few alleles per locus, rare mutations), the rest Zipf."""
+    rng = np.random.default_rng(1000 + seed)
+    n = int(np.exp(rng.uniform(np.log(2000), np.log(63005))))
+    L = int(rng.choice(LOCI))
+    while n * L > 7.2e7:
+        L = int(rng.choice(LOCI[:3]))
+        if n * L > 7.2e7:
+            n = int(7.2e7 / L)
+    p = dict(seed=seed, n=n, L=L, miss=float(rng.uniform(0.0, 0.08)))
+    if rng.random() < 0.25:
+        p.update(kind="founders", founders=int(rng.integers(3, 60)), mut=float(np.exp(rng.uniform(np.log(0.002),
+                                                                                                 np.log(0.05)))))
+    else:
+        p.update(kind="zipf", s=float(rng.uniform(1.0, 1.4)), median=float(np.exp(rng.uniform(np.log(15), np.log(150)))),
+                 sigma=float(rng.uniform(0.8, 1.4)))
+    return p
+
+
+def make_dataset(p: dict) -> np.ndarray:
+    if p.get("kind") == "founders":
+        rng = np.random.default_rng(p["seed"])
+        n, L = p["n"], p["L"]
+        out = np.zeros((L, n), dtype=np.uint64)
+        for l in range(L):
+            f = rng.integers(1, 2**32, size=p["founders"], dtype=np.uint64)
+            col = f[rng.integers(0, p["founders"], n)]
+            mut = rng.random(n) < p["mut"]
+            col[mut] = rng.integers(2**32, 2**64 - 1, size=int(mut.sum()), dtype=np.uint64)
+            col[rng.random(n) < 2 * p["miss"] * rng.random()] = 0
+            out[l] = col
+        return np.ascontiguousarray(out.T)
+
+    def distinct(rng, L):
+        return np.clip(np.rint(rng.lognormal(np.log(p["median"]), p["sigma"], L)), 2, 3000).astype(np.int64)
+
+    def miss(rng, L):
+        return rng.uniform(0.0, 2 * p["miss"], L)
+
+    return synth.zipf_profiles(p["n"], p["L"], p["seed"], p["s"], distinct, miss, hashed_frac=0.05)
+
+
+def time_solve(A: np.ndarray, tau: int, reps: int = 3, device: int = 0) -> float:
+    """Median device ms of one whole-triangle stripe (rare counts + tile pass)."""
+    import torch
+
+    n = A.shape[0]
+    ldo = (n + 7) // 8 * 8
+    out = torch.empty((n, ldo), dtype=torch.int16, device=f"cuda:{device}")
+    stream = torch.cuda.current_stream(device).cuda_stream
+    with tch.Solver.from_calls(A, tau=tau, device=device) as s:
+        s.stripe(0, n, out.data_ptr(), ldo, stream)  # warm-up
+        times = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            s.stripe(0, n, out.data_ptr(), ldo, stream)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        s.check()
+    del out
+    return float(np.median(times))
+
+
+def sweep(n_datasets: int, out: str, span: int = 32, device: int = 0) -> None:
+    rows = dict(ds=[], tau=[], feats=[], est=[], ms=[])
+    params = []
+    t0 = time.time()
+    for d in range(n_datasets):
+        p = dataset_params(d)
+        A = make_dataset(p)
+        taus, feats, est = tch.tau_features(A, device)
+        analytic = int(taus[np.argmin(est)])
+        for t, f, e in zip(taus, feats, est):
+            if t < max(4, analytic // span) or t > analytic * span:
+                continue
+            ms = time_solve(A, int(t), device=device)
+            rows["ds"].append(d)
+            rows["tau"].append(int(t))
+            rows["feats"].append(f)
+            rows["est"].append(float(e))
+            rows["ms"].append(ms)
+        params.append(p)
+        print(f"[{time.time() - t0:6.1f}s] set {d}: {p['kind']} n={p['n']} L={p['L']} analytic tau={analytic}",
+              flush=True)
+    np.savez(out, ds=np.array(rows["ds"], np.int32), tau=np.array(rows["tau"], np.int32),
+             feats=np.array(rows["feats"], np.float32), est=np.array(rows["est"]), ms=np.array(rows["ms"]),
+             params=json.dumps(params))
+
+
+def holdout_mask(ds: np.ndarray) -> np.ndarray:
+    return ds % 5 == 4
+
+
+def fold_standardisation(w: np.ndarray, mu: np.ndarray, sd: np.ndarray) -> np.ndarray:
+    """Model on (x - mu) / sd -> the same model on raw x."""
+    F, H = tch.TAU_FEATURES, tch.MLP_HIDDEN
+    w = w.astype(np.float64).copy()
+    W1 = w[:F * H].reshape(F, H)
+    b1 = w[F * H:F * H + H]
+    b1 -= (mu / sd) @ W1
+    W1 /= sd[:, None]
+    w[:F * H] = W1.ravel()
+    w[F * H:F * H + H] = b1
+    return w.astype(np.float32)
+
+
+def evaluate(w: np.ndarray, data, device: int = 0) -> dict:
+    """Per held-out set: measured ms at the learned, analytic and best tau."""
+    ds, tau, X, est, ms = data["ds"], data["tau"], data["feats"], data["est"], data["ms"]
+    pred = tch.mlp_predict(w, X, device)
+    out = []
+    for d in np.unique(ds[holdout_mask(ds)]):
+        m = ds == d
+        i_l = np.argmin(np.where(m, pred, np.inf))
+        i_a = np.argmin(np.where(m, est, np.inf))
+        i_b = np.argmin(np.where(m, ms, np.inf))
+        out.append(dict(set=int(d), tau_learned=int(tau[i_l]), tau_analytic=int(tau[i_a]), tau_best=int(tau[i_b]),
+                        ms_learned=float(ms[i_l]), ms_analytic=float(ms[i_a]), ms_best=float(ms[i_b])))
+    tl = sum(r["ms_learned"] for r in out)
+    ta = sum(r["ms_analytic"] for r in out)
+    tb = sum(r["ms_best"] for r in out)
+    return dict(sets=out, total_ms_learned=tl, total_ms_analytic=ta, total_ms_best=tb,
+                learned_over_best=tl / tb, analytic_over_best=ta / tb,
+                mean_learned_over_best=float(np.mean([r["ms_learned"] / r["ms_best"] for r in out])),
+                mean_analytic_over_best=float(np.mean([r["ms_analytic"] / r["ms_best"] for r in out])))
+
+
+def train(sweep_path: str, out: str, steps: int = 6000, lr: float = 3e-3, seed: int = 7, device: int = 0) -> dict:
+    data = dict(np.load(sweep_path))
+    ds = data["ds"]
+    tr = ~holdout_mask(ds)
+    X = data["feats"].astype(np.float64)
+    y = np.log(data["ms"]).astype(np.float32)
+    mu = X[tr].mean(0)
+    sd = X[tr].std(0)
+    sd[sd < 1e-6] = 1.0
+    Xn = ((X - mu) / sd).astype(np.float32)
+    w = tch.mlp_init(seed)
+    t0 = time.time()
+    w, loss1 = tch.mlp_train(w, Xn[tr], y[tr], steps // 2, lr, device)
+    w, loss2 = tch.mlp_train(w, Xn[tr], y[tr], steps - steps // 2, lr / 5, device)
+    secs = time.time() - t0
+    w_raw = fold_standardisation(w, mu, sd)
+    rep = evaluate(w_raw, data, device)
+    rep.update(train_rows=int(tr.sum()), holdout_rows=int((~tr).sum()), steps=steps, final_train_mse=loss2,
+               train_seconds=secs)
+    w_raw.astype("<f4").tofile(out)
+    return rep
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("cmd", choices=["sweep", "train"])
+    ap.add_argument("--datasets", type=int, default=240)
+    ap.add_argument("--sweep", default=SWEEP_PATH)
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--steps", type=int, default=6000)
+    ap.add_argument("--device", type=int, default=0)
+    a = ap.parse_args()
+    if a.cmd == "sweep":
+        sweep(a.datasets, a.out or SWEEP_PATH, device=a.device)
+    else:
+        rep = train(a.sweep, a.out or tch.TAU_MLP_PATH, steps=a.steps, device=a.device)
+        with open(REPORT_PATH, "w") as f:
+            json.dump(rep, f, indent=1)
+        print(json.dumps({k: v for k, v in rep.items() if k != "sets"}, indent=1))
+
+
+if __name__ == "__main__":
+    main()

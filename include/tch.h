@@ -163,6 +163,77 @@ int tch_set_dense_rare_rate(double rate);
  * No reference counterpart (the reference always builds pair lists). */
 int tch_set_rare_term(int dense);
 
+/* ---- learned tau (no reference counterpart) --------------------------------
+ * A small MLP predicts ln(ms) of one whole-triangle solve for each candidate
+ * tau from TCH_TAU_FEATURES features; a solver built from calls with tau <= 0
+ * takes the candidate with the smallest prediction when a model is set
+ * (tch_set_tau_mlp), the analytic model's pick otherwise.  Feature row of a
+ * candidate: ln n, ln L, quantiles 0.25 / 0.5 / 0.9 of ln(1 + distinct alleles
+ * per locus), missing fraction, ln tau, ln(1 + frequent one-hot columns),
+ * ln(1 + rare pairs), ln(1 + rare cells), ln(pairs x operand bytes per row),
+ * ln(analytic estimate in seconds).  Network: F -> 32 -> 32 -> 1, ReLU, fp32,
+ * parameters W1[F][32] | b1[32] | W2[32][32] | b2[32] | w3[32] | b3. */
+#define TCH_TAU_FEATURES 12
+#define TCH_MLP_HIDDEN 32
+#define TCH_MLP_PARAMS                                                                             \
+    (TCH_TAU_FEATURES * TCH_MLP_HIDDEN + TCH_MLP_HIDDEN + TCH_MLP_HIDDEN * TCH_MLP_HIDDEN + \
+     TCH_MLP_HIDDEN + TCH_MLP_HIDDEN + 1)
+
+/* Candidate taus of a profile set (device encoder's counts; those whose
+ * encoding fits in free device memory) and their feature rows:
+ * taus[r], feats[r * TCH_TAU_FEATURES + f] for r < *rows <= max_rows.
+ * est_s[r] (may be NULL) receives the analytic model's estimate. */
+int tch_tau_features(int device, int n, int L, const uint64_t* calls, int max_rows, int* taus, float* feats,
+                     double* est_s, int* rows, char* err, int errlen);
+
+/* He-normal initial parameters from a seed (host). */
+int tch_mlp_init(float* w, uint64_t seed);
+/* Full-batch Adam on the GPU (the project's forward/backward kernels, one
+ * step captured as a CUDA graph): w updated in place, *loss = final MSE. */
+int tch_mlp_train(int device, float* w, const float* X, const float* y, int n, int steps, float lr, float* loss,
+                  char* err, int errlen);
+/* y[i] = f(X[i]) on the GPU. */
+int tch_mlp_predict(int device, const float* w, const float* X, int n, float* y, char* err, int errlen);
+/* Mean squared error of f(X) against y and its gradient (TCH_MLP_PARAMS floats). */
+int tch_mlp_loss_grad(int device, const float* w, const float* X, const float* y, int n, float* loss, float* grad,
+                      char* err, int errlen);
+/* Model used by tau <= 0 (copied; NULL = analytic model only). */
+int tch_set_tau_mlp(const float* w);
+
+/* ---- serving (no reference counterpart) ----------------------------------------
+ * A profile database resident on the device and batches of new profiles
+ * against it.  tch_db_query(db, m, q, qdb, qq, stream): q = m x L allele calls
+ * (host, u64, 0 = missing) in the database's locus order; writes (host,
+ * either may be NULL)
+ *   qdb[r * n + j] = distance of new profile r to database row j   (m x n)
+ *   qq[a * m + b]  = distance of new profiles a < b                 (m x m,
+ *                    upper triangle; other cells untouched)
+ * with the reference's semantics (ids compared for equality, 0 missing).  Runs
+ * on `stream` (NULL = legacy default) from a stream-ordered pool of the
+ * database and returns when the results are in host memory. */
+typedef struct tch_db tch_db;
+int tch_db_create(int device, int n, int L, const uint64_t* calls, int tau, tch_db** out, char* err, int errlen);
+void tch_db_destroy(tch_db* db);
+int tch_db_info(const tch_db* db, int* n, int* L, int* tau, size_t* d_onehot, size_t* device_bytes);
+/* Device bytes a query batch of m profiles takes while it runs. */
+size_t tch_db_query_bytes(const tch_db* db, int m);
+int tch_db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* qdb, uint16_t* qq, void* stream, char* err,
+                 int errlen);
+
+/* Continuous batching: `slots` worker threads, one stream each; a FIFO of
+ * requests, admitted when tch_db_query_bytes(m) fits in `budget` bytes next to
+ * the requests running (0 = half the free device memory; a request larger than
+ * the budget runs alone).  Host buffers of a request stay the caller's and
+ * must live until tch_server_wait returns for it. */
+typedef struct tch_server tch_server;
+int tch_server_create(tch_db* db, int slots, size_t budget, tch_server** out, char* err, int errlen);
+/* Returns a request id (> 0), or -1 on bad arguments. */
+int64_t tch_server_submit(tch_server* sv, int m, const uint64_t* qcalls, uint16_t* qdb, uint16_t* qq);
+/* Blocks until the request is done; *queued_s = submit -> start, *latency_s =
+ * submit -> results in host memory. */
+int tch_server_wait(tch_server* sv, int64_t id, double* queued_s, double* latency_s, char* err, int errlen);
+void tch_server_destroy(tch_server* sv);
+
 /* Fill *info. */
 int tch_solver_info(const tch_solver* s, tch_info* info);
 

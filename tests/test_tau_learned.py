@@ -1,0 +1,118 @@
+"""The learned tau model: its CUDA forward/backward/training kernels against
+the CPU oracle (oracle/oracle_mlp.py), the oracle against finite differences, the
+shipped model's gain over the analytic model on held-out sweep data, and
+exactness of a solve whose tau the model picked."""
+import importlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import oracle_mlp as omlp
+
+PKG = "cgmlst-hamming-gpu_gb300"
+
+
+def test_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    X = rng.normal(size=(64, omlp.F))
+    y = rng.normal(size=64)
+    w = omlp.init(3).astype(np.float64)
+    w[omlp.F * omlp.H:omlp.F * omlp.H + omlp.H] = 0.1  # biases away from the kinks
+    loss, g = omlp.loss_grad(w, X, y)
+    idx = rng.choice(omlp.NP, 80, replace=False)
+    num = omlp.numeric_grad(w, X, y, idx)
+    np.testing.assert_allclose(g[idx], num, rtol=1e-4, atol=1e-7)
+    assert loss == pytest.approx(np.mean((omlp.forward(w, X) - y) ** 2))
+
+
+def test_standardisation_fold_is_exact():
+    tl = importlib.import_module(PKG + ".tau_learn")
+    rng = np.random.default_rng(1)
+    X = rng.normal(3.0, 2.0, size=(50, omlp.F))
+    mu, sd = X.mean(0), X.std(0)
+    w = omlp.init(5)
+    folded = tl.fold_standardisation(w, mu, sd)
+    np.testing.assert_allclose(omlp.forward(folded, X), omlp.forward(w, (X - mu) / sd), rtol=1e-5, atol=1e-5)
+
+
+def test_shipped_model_files_present(pkg):
+    assert os.path.exists(pkg.TAU_MLP_PATH), "trained tau model missing"
+    w = np.fromfile(pkg.TAU_MLP_PATH, dtype="<f4")
+    assert w.size == pkg.MLP_PARAMS and np.all(np.isfinite(w))
+
+
+# ---------------------------------------------------------------------------- GPU
+
+@pytest.fixture(scope="module")
+def tch(pkg):
+    assert pkg.device_count() > 0, "no CUDA device visible"
+    yield pkg
+    pkg.set_tau_mlp(None)
+
+
+@pytest.mark.gpu
+def test_gpu_forward_and_gradient_match_oracle(tch):
+    rng = np.random.default_rng(2)
+    for n in (1, 37, 300, 1000):
+        X = rng.normal(size=(n, omlp.F)).astype(np.float32)
+        y = rng.normal(size=n).astype(np.float32)
+        w = tch.mlp_init(11 + n)
+        p = tch.mlp_predict(w, X)
+        np.testing.assert_allclose(p, omlp.forward(w, X), rtol=1e-4, atol=1e-4)
+        loss, g = tch.mlp_loss_grad(w, X, y)
+        lo, go = omlp.loss_grad(w, X, y)
+        assert loss == pytest.approx(lo, rel=1e-4)
+        scale = np.abs(go).max()
+        np.testing.assert_allclose(g, go, rtol=2e-3, atol=2e-5 * scale)
+
+
+@pytest.mark.gpu
+def test_gpu_training_follows_oracle_adam(tch):
+    rng = np.random.default_rng(4)
+    X = rng.normal(size=(400, omlp.F)).astype(np.float32)
+    y = (np.sin(X[:, 0]) + 0.5 * X[:, 1] * X[:, 2]).astype(np.float32)
+    w0 = tch.mlp_init(9)
+    l0, _ = omlp.loss_grad(w0, X, y)
+    w, loss = tch.mlp_train(w0, X, y, steps=60, lr=1e-2)
+    wo = omlp.adam_train(w0, X, y, steps=60, lr=1e-2)
+    lo, _ = omlp.loss_grad(wo, X, y)
+    assert loss < 0.5 * l0
+    assert loss == pytest.approx(lo, rel=0.05)
+    # longer training keeps improving
+    w2, loss2 = tch.mlp_train(w, X, y, steps=600, lr=3e-3)
+    assert loss2 < loss
+
+
+@pytest.mark.gpu
+def test_shipped_model_gains_over_analytic_on_heldout(tch):
+    """Held-out profile sets of the committed sweep: the measured time at the
+    learned pick is within 5% of the best swept tau overall and below the
+    analytic model's pick (the model is evaluated by the GPU kernel)."""
+    tl = importlib.import_module(PKG + ".tau_learn")
+    data = dict(np.load(tl.SWEEP_PATH))
+    w = np.fromfile(tch.TAU_MLP_PATH, dtype="<f4")
+    rep = tl.evaluate(w, data)
+    assert len(rep["sets"]) >= 8
+    assert rep["learned_over_best"] <= 1.05, rep
+    assert rep["total_ms_learned"] < rep["total_ms_analytic"], rep
+
+
+@pytest.mark.gpu
+def test_learned_tau_drives_the_solver_and_stays_exact(tch):
+    synth = importlib.import_module(PKG + ".synth")
+    A = synth.longtail(n=1500, L=300, seed=8)
+    w = tch.load_tau_mlp()
+    taus, feats, est = tch.tau_features(A)
+    pick = int(taus[np.argmin(tch.mlp_predict(w, feats))])
+    with tch.Solver.from_calls(A, tau=0) as s:
+        info = s.info()
+        H, _ = s.run(512)
+    assert info["tau"] == pick
+    x = oracle.dense_ranks(A)[0]
+    iu = np.triu_indices(1500, 1)
+    np.testing.assert_array_equal(H[iu], oracle.hamming(x)[iu])
+    tch.set_tau_mlp(None)
+    with tch.Solver.from_calls(A, tau=0) as s:
+        assert s.info()["tau"] == int(taus[np.argmin(est)])  # analytic model again
