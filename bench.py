@@ -162,6 +162,143 @@ def cpu_sample(x: np.ndarray, target_s: float, threads: int = 0):
     return pairs / dt, int(pairs), (rows, r1), dt
 
 
+def time_whole(tch, A, tau, device, out, ldo, stream, reps=3):
+    """(median device ms, tau used) of one whole-triangle solve of a fresh solver."""
+    import torch
+
+    n = A.shape[0]
+    with tch.Solver.from_calls(A, tau=tau, device=device) as s:
+        used = s.info()["tau"]
+        s.stripe(0, n, out.data_ptr(), ldo, stream.cuda_stream)
+        ms = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.stripe(0, n, out.data_ptr(), ldo, stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        s.check()
+    return statistics.median(ms), used
+
+
+def serving_bench(tch, synth, args, device):
+    """Resident database of n_db profiles x 1 142 loci (Zipf s = 1.2, 3 %
+    missing), Poisson query arrivals (mean 50/s) of batches log-uniform in
+    [1, 2 000] new profiles from the same generator, through tch_server."""
+    import threading
+
+    n_db, L, pool_rows = args.serve_db, 1142, 40000
+    t0 = time.perf_counter()
+
+    def distinct(rng, L):
+        return np.clip(np.rint(rng.lognormal(np.log(60.0), 1.26, L)), 2, 3000).astype(np.int64)
+
+    A = synth.zipf_profiles(n_db + pool_rows, L, 5, 1.2, distinct, lambda rng, L: np.full(L, 0.03),
+                            hashed_frac=0.05)
+    db_calls, pool = A[:n_db], A[n_db:]
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    db = tch.Database(db_calls, device=device)
+    build_s = time.perf_counter() - t0
+    dbi = db.info()
+    rng = np.random.default_rng(11)
+    R = args.serve_requests
+    sizes = np.minimum(2000, np.floor(np.exp(rng.uniform(0, np.log(2001), R)))).astype(int)
+    arrivals = np.cumsum(rng.exponential(1 / 50.0, R))
+    starts = rng.integers(0, pool_rows - 2000, R)
+    db.query(pool[:64])  # warm the pool and the kernels
+    slots = 4
+    sv = tch.Server(db, slots=slots)
+    rids = [None] * R
+    submit_delay = np.zeros(R)
+    tb = time.perf_counter() + 0.05
+
+    def submitter():
+        for k in range(R):
+            t = tb + arrivals[k]
+            d = t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            rids[k] = sv.submit(pool[starts[k]:starts[k] + sizes[k]])
+            submit_delay[k] = time.perf_counter() - t
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    lat = np.zeros(R)
+    queued = np.zeros(R)
+    for k in range(R):
+        while rids[k] is None:
+            time.sleep(0.0005)
+        _, _, q_s, l_s = sv.wait(rids[k])
+        lat[k] = submit_delay[k] + l_s  # from the request's arrival
+        queued[k] = q_s
+    th.join()
+    makespan = time.perf_counter() - tb
+    sv.close()
+    db.close()
+    pairs = int(sum(m * n_db + m * (m - 1) // 2 for m in sizes))
+    return {"db": f"{n_db} x {L} (Zipf s=1.2, lognormal distinct median 60, 3% missing, 5% 64-bit ids)",
+            "db_tau": dbi["tau"], "db_device_gb": dbi["device_bytes"] / 1e9, "db_build_s": build_s,
+            "requests": R, "arrival": "Poisson, mean 50/s", "batch": "log-uniform 1-2000 profiles",
+            "query_rows": int(sizes.sum()), "slots": slots,
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "mean_ms": float(lat.mean() * 1e3), "max_ms": float(lat.max() * 1e3),
+            "queued_p50_ms": float(np.percentile(queued, 50) * 1e3),
+            "pairs": pairs, "pairs_per_s": pairs / makespan, "makespan_s": makespan,
+            "note": "latency = arrival -> q x db and q x q distances in host memory; generation "
+                    f"{gen_s:.1f} s outside the timed region"}
+
+
+def batch_bench(tch, args, device):
+    """512 independent matrices, n log-uniform in [50, 5 000], L from {1 142,
+    1 343, 2 794, 3 016}, Zipf s in [1.0, 1.4] over lognormal distinct counts,
+    0-8 % missing: encoded once, then every upper triangle in one graph replay
+    with the autotuned schedule and tau chosen per matrix."""
+    import torch
+
+    rng = np.random.default_rng(21)
+    t0 = time.perf_counter()
+    b = tch.Batch(device=device)
+    pairs = 0
+    for _ in range(args.batch_count):
+        n = int(np.exp(rng.uniform(np.log(50), np.log(5000))))
+        L = int(rng.choice([1142, 1343, 2794, 3016]))
+        s = float(rng.uniform(1.0, 1.4))
+        k = np.clip(np.rint(rng.lognormal(np.log(40.0), 1.0, L)), 2, 500).astype(np.int64)
+        a = (rng.zipf(max(s, 1.01), size=(n, L)) - 1) % k[None, :]
+        A = (np.arange(L, dtype=np.uint64)[None, :] << np.uint64(20)) + a.astype(np.uint64) + np.uint64(1)
+        A[rng.random((n, L)) < rng.uniform(0.0, 0.08)] = 0
+        b.add(A)
+        pairs += n * (n - 1) // 2
+    build_s = time.perf_counter() - t0
+    off, ld = b.layout()
+    out = torch.empty(int(off[-1]) + 8, dtype=torch.int16, device=f"cuda:{device}")
+    stream = torch.cuda.Stream(device=device)
+    t0 = time.perf_counter()
+    tuned = b.tune(out.data_ptr(), stream.cuda_stream, reps=3)
+    tune_s = time.perf_counter() - t0
+    for _ in range(3):
+        b.run(out.data_ptr(), stream.cuda_stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record(stream)
+    for _ in range(reps):
+        b.run(out.data_ptr(), stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    b.check()
+    ms = e0.elapsed_time(e1) / reps
+    taus = b.info()["taus"]
+    b.close()
+    return {"matrices": args.batch_count, "pairs": pairs, "ms_per_batch": ms, "pairs_per_s": pairs / (ms / 1e3),
+            "schedule": tuned, "graph": "one CUDA graph per replay (fork/join over the tuned branch count)",
+            "tau_per_matrix": {"min": int(min(taus)), "median": int(np.median(taus)), "max": int(max(taus))},
+            "encode_s": build_s, "tune_s": tune_s}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -176,6 +313,13 @@ def main():
     ap.add_argument("--n", type=int, default=63005)
     ap.add_argument("--L", type=int, default=1142)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--analytic-tau", action="store_true", help="ignore the shipped learned tau model")
+    ap.add_argument("--no-tau-sweep", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--serve-db", type=int, default=200000)
+    ap.add_argument("--serve-requests", type=int, default=100)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -225,6 +369,14 @@ def main():
     torch.cuda.set_device(device)
     assert tch.device_count() > 0
 
+    # tau: the learned model shipped with the package picks it (the analytic
+    # model's pick is timed beside it below)
+    tau_pick = {}
+    if not args.tau and os.path.exists(tch.TAU_MLP_PATH) and not args.analytic_tau:
+        w_mlp = tch.load_tau_mlp()
+        taus_c, feats_c, est_c = tch.tau_features(A, device)
+        tau_pick = {"analytic": int(taus_c[int(np.argmin(est_c))]),
+                    "learned": int(taus_c[int(np.argmin(tch.mlp_predict(w_mlp, feats_c, device)))])}
     t0 = time.perf_counter()
     solver = tch.Solver.from_calls(A, tau=args.tau, kernel=args.kernel, device=device)  # device encoder
     info = solver.info()
@@ -331,6 +483,23 @@ def main():
 
     # e2e through the C ABI with host buffers: tch_run (the reference's entry
     # point, host-encoded operands) and tch_run_calls (allele calls, device encoder)
+    # learned vs analytic tau: whole-triangle device time at each pick and at
+    # a sweep of taus around them (fresh solvers)
+    tau_cmp = None
+    if rank == 0 and ws == 1 and not args.no_tau_sweep:
+        swept = {int(tau): ms_per_step}
+        cands = {512, 1024, 2048, 4096, 8192} | set(tau_pick.values())
+        for t in sorted(cands):
+            if t not in swept:
+                ms_t, used = time_whole(tch, A, t, device, out, ldo, stream)
+                swept[int(used)] = ms_t
+        best = min(swept, key=swept.get)
+        tau_cmp = {"used": int(tau), "swept_ms": {str(k): v for k, v in sorted(swept.items())},
+                   "best_swept": {"tau": best, "ms": swept[best]}}
+        for k, v in tau_pick.items():
+            tau_cmp[k] = {"tau": v, "ms": swept.get(v)}
+        log("tau comparison:", tau_cmp)
+
     e2e = None
     e2e_calls = None
     if rank == 0 and args.e2e_steps > 0:
@@ -381,6 +550,19 @@ def main():
                      "d2h_bytes_per_step": int(d2h), "seconds_per_step": ec, "tau": int(tu.value),
                      "path": "tch_run_calls: allele calls uploaded, device encoder, same stripes and copy-back"}
 
+    serving = None
+    batched = None
+    if rank == 0 and ws == 1 and not (args.no_serving and args.no_batch):
+        solver.close()
+        del out
+        torch.cuda.empty_cache()
+        if not args.no_batch:
+            batched = batch_bench(tch, args, device)
+            log("batched:", batched)
+        if not args.no_serving:
+            serving = serving_bench(tch, synth, args, device)
+            log("serving:", serving)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         rate, pairs, rows, dt = cpu_sample(x, args.cpu_seconds, 0)
@@ -396,11 +578,11 @@ def main():
                                                     parallelism=f"row shares x{ws}"),
                 "gpu_launches": args.steps * launches_per_step, "step_split": split,
                 "clocks": ck, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "e2e_device_encoder": e2e_calls,
+                "e2e_device_encoder": e2e_calls, "tau_choice": tau_cmp, "batched": batched, "serving": serving,
                 "peak_probe": peak_info}
         print(json.dumps(line), flush=True)
-    solver.close()
     if ws > 1:
+        solver.close()
         torch.distributed.destroy_process_group()
 
 

@@ -145,6 +145,22 @@ def lib():
         L.tch_server_wait.argtypes = [c_void, ctypes.c_int64, P(c_double), P(c_double), c_char_p, c_int]
         L.tch_server_wait.restype = c_int
         L.tch_server_destroy.argtypes, L.tch_server_destroy.restype = [c_void], None
+        L.tch_batch_create.argtypes = [c_int, c_int, c_void, c_void, c_void, c_void, P(c_void), c_char_p, c_int]
+        L.tch_batch_create.restype = c_int
+        L.tch_batch_add.argtypes = [c_void, c_int, c_int, c_void, c_int, c_char_p, c_int]
+        L.tch_batch_add.restype = c_int
+        L.tch_batch_layout.argtypes, L.tch_batch_layout.restype = [c_void, c_void, c_void], c_int
+        L.tch_batch_run.argtypes = [c_void, c_void, c_void, c_char_p, c_int]
+        L.tch_batch_run.restype = c_int
+        L.tch_batch_check.argtypes, L.tch_batch_check.restype = [c_void, c_char_p, c_int], c_int
+        L.tch_batch_tune.argtypes = [c_void, c_void, c_void, c_int, P(c_double), P(c_int), P(c_int), P(c_int),
+                                     c_char_p, c_int]
+        L.tch_batch_tune.restype = c_int
+        L.tch_batch_set_schedule.argtypes = [c_void, c_int, c_int, c_int]
+        L.tch_batch_set_schedule.restype = c_int
+        L.tch_batch_info.argtypes = [c_void, P(c_int), c_void, P(c_int), P(c_int), P(c_int)]
+        L.tch_batch_info.restype = c_int
+        L.tch_batch_destroy.argtypes, L.tch_batch_destroy.restype = [c_void], None
         _lib = L
     return _lib
 
@@ -509,7 +525,7 @@ class Database:
         m = q.shape[0]
         if q.shape[1] != self.L:
             raise TchError(f"queries have {q.shape[1]} loci, the database {self.L}")
-        qdb = np.zeros((m, self.n), np.uint16)
+        qdb = np.empty((m, self.n), np.uint16)  # every cell is written
         qq = np.zeros((m, m), np.uint16) if want_qq else None
         err = _errbuf()
         _check(lib().tch_db_query(self._h, m, _ptr(q), _ptr(qdb), _ptr(qq) if want_qq else None,
@@ -543,7 +559,7 @@ class Server:
     def submit(self, q: np.ndarray, want_qq: bool = True) -> int:
         q = np.ascontiguousarray(q, dtype=np.uint64)
         m = q.shape[0]
-        qdb = np.zeros((m, self.db.n), np.uint16)
+        qdb = np.empty((m, self.db.n), np.uint16)  # every cell is written
         qq = np.zeros((m, m), np.uint16) if want_qq else None
         rid = lib().tch_server_submit(self._h, m, _ptr(q), _ptr(qdb), _ptr(qq) if want_qq else None)
         if rid < 0:
@@ -563,6 +579,80 @@ class Server:
     def close(self):
         if self._h:
             lib().tch_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+# ---------------------------------------------------------------------------------------
+# batched solves under a CUDA graph
+# ---------------------------------------------------------------------------------------
+
+class Batch:
+    """Many profile sets solved together (tch_batch): every set's upper
+    triangle into one device buffer, launches captured as one CUDA graph."""
+
+    def __init__(self, sets=(), taus=None, device: int = 0):
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        _check(lib().tch_batch_create(device, 0, None, None, None, None, ctypes.byref(h), err, len(err)), err)
+        self._h = h
+        self.shapes = []
+        for k, A in enumerate(sets):
+            self.add(A, 0 if taus is None else taus[k])
+
+    def add(self, calls: np.ndarray, tau: int = 0):
+        calls = np.ascontiguousarray(calls, dtype=np.uint64)
+        n, L = calls.shape
+        err = _errbuf()
+        _check(lib().tch_batch_add(self._h, n, L, _ptr(calls), tau, err, len(err)), err)
+        self.shapes.append((n, L))
+
+    def layout(self):
+        c = len(self.shapes)
+        off = np.zeros(c + 1, np.uint64)
+        ld = np.zeros(max(c, 1), np.uint64)
+        lib().tch_batch_layout(self._h, _ptr(off), _ptr(ld))
+        return off.astype(np.int64), ld[:c].astype(np.int64)
+
+    def run(self, d_out: int, stream: int = 0):
+        err = _errbuf()
+        _check(lib().tch_batch_run(self._h, ctypes.c_void_p(d_out), ctypes.c_void_p(stream) if stream else None,
+                                   err, len(err)), err)
+
+    def check(self):
+        err = _errbuf()
+        _check(lib().tch_batch_check(self._h, err, len(err)), err)
+
+    def tune(self, d_out: int, stream: int = 0, reps: int = 3) -> dict:
+        ms = ctypes.c_double()
+        nb, cs, cl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        err = _errbuf()
+        _check(lib().tch_batch_tune(self._h, ctypes.c_void_p(d_out), ctypes.c_void_p(stream) if stream else None,
+                                    reps, ctypes.byref(ms), ctypes.byref(nb), ctypes.byref(cs), ctypes.byref(cl),
+                                    err, len(err)), err)
+        return dict(ms=ms.value, branches=nb.value, cluster_small=cs.value, cluster_large=cl.value)
+
+    def set_schedule(self, branches: int, cluster_small: int = 2, cluster_large: int = 2):
+        if lib().tch_batch_set_schedule(self._h, branches, cluster_small, cluster_large):
+            raise TchError("invalid schedule")
+
+    def info(self) -> dict:
+        c = ctypes.c_int()
+        taus = np.zeros(max(len(self.shapes), 1), np.int32)
+        nb, cs, cl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        lib().tch_batch_info(self._h, ctypes.byref(c), _ptr(taus), ctypes.byref(nb), ctypes.byref(cs),
+                             ctypes.byref(cl))
+        return dict(count=c.value, taus=taus[:c.value].tolist(), branches=nb.value, cluster_small=cs.value,
+                    cluster_large=cl.value)
+
+    def close(self):
+        if self._h:
+            lib().tch_batch_destroy(self._h)
             self._h = None
 
     def __enter__(self):

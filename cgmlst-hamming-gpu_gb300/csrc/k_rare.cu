@@ -266,8 +266,12 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
     const size_t width = up((size_t)(g.n - r0), kRareDenseAlign);
     if (ldr < width || (ldr & 7) || ((uintptr_t)R & 15)) return cudaErrorInvalidValue;
     const int smem = RD_SMEM;
-    cudaError_t e = cudaFuncSetAttribute(rare_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
+    static bool attr = false;  // once per process (also keeps it out of graph captures)
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(rare_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
     const int grid = std::max(1, std::min(rows, sms));
     rare_dense_kernel<<<grid, RD_THREADS, smem, st>>>(g, r0, rows, R, ldr, r0 + (int)width);
     return cudaGetLastError();
@@ -282,8 +286,12 @@ cudaError_t launch_rare_query(const RareGroups& g, const uint32_t* xq, int m, ui
     if (m <= 0) return cudaSuccess;
     const size_t width = up((size_t)std::max(g.n, 1), kRareDenseAlign);
     if (ldr < width || (ldr & 7) || ((uintptr_t)R & 15)) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(rare_query_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, RD_SMEM);
-    if (e != cudaSuccess) return e;
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(rare_query_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, RD_SMEM);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
     rare_query_kernel<<<std::max(1, std::min(m, sms)), RD_THREADS, RD_SMEM, st>>>(g, xq, m, R, ldr, (int)width);
     return cudaGetLastError();
 }

@@ -610,8 +610,9 @@ cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const ByteOper
         s.out = a.out + (size_t)done * a.ldo + col;
         RareCSR rs = rare;
         if (rare.dense) rs.dense = rare.dense + (size_t)done * rare.ldr + col;
-        const cudaError_t e = cluster_size() == 2 ? launch_kind<KIND_F8, 2>(ops, b, rs, s, num_sms, st)
-                                                  : launch_kind<KIND_F8, 1>(ops, b, rs, s, num_sms, st);
+        const int cm = (a.cluster == 1 || a.cluster == 2) ? a.cluster : cluster_size();
+        const cudaError_t e = cm == 2 ? launch_kind<KIND_F8, 2>(ops, b, rs, s, num_sms, st)
+                                      : launch_kind<KIND_F8, 1>(ops, b, rs, s, num_sms, st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;

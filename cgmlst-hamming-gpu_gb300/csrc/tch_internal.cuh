@@ -113,6 +113,7 @@ struct StripeArgs {
     size_t ldo = 0;
     int* err = nullptr;
     bool rect = false;
+    int cluster = 0;  // CTAs per cluster of the tile pass, 1 or 2 (0 = library default)
 };
 
 // ---- k_popc.cu --------------------------------------------------------------------
@@ -223,6 +224,19 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
                      bool verbose, size_t max_chunk_bytes, int flags, DeviceEncoding* out, Err& e,
                      TauTable* table = nullptr);
 void free_device_encoding(DeviceEncoding* d);
+
+// ---- tch_solver.cu (used by the batch runner) -----------------------------------------
+int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, bool verbose,
+                      tch_solver** out, Err& e);
+int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e,
+                  const int* unsorted_flag = nullptr);
+int solver_check(tch_solver* s, Err& e);
+void solver_free(tch_solver* s);
+void solver_set_cluster(tch_solver* s, int cm);
+int solver_stripe_counts(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, uint16_t* R, size_t ldr,
+                         cudaStream_t st, Err& e);
+double solver_work(const tch_solver* s);
+int solver_size(const tch_solver* s);
 
 // ---- k_mlp.cu ----------------------------------------------------------------------
 constexpr int kMlpIn = TCH_TAU_FEATURES, kMlpHidden = TCH_MLP_HIDDEN, kMlpParams = TCH_MLP_PARAMS;

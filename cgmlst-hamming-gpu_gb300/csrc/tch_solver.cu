@@ -160,6 +160,7 @@ struct tch_solver {
     uint32_t* gmembers = nullptr;
     uint32_t* gmpos = nullptr;
     int gL = 0;                      // loci of the rank rows (>= 1)
+    int cluster = 0;                 // CTAs per cluster of the tile pass (0 = library default)
     int* dErr = nullptr;
     int num_sms = 0;
     size_t bytes = 0;
@@ -173,7 +174,7 @@ static cudaError_t dmalloc(tch_solver* s, void** p, size_t bytes) {
     return e;
 }
 
-static void solver_free(tch_solver* s) {
+void solver_free(tch_solver* s) {
     if (!s) return;
     int cur = -1;
     cudaGetDevice(&cur);
@@ -343,7 +344,7 @@ static TauModel g_tau_model;
 
 // Operands on the device straight from allele calls (host buffer, n x L u64,
 // 0 = missing): the device encoder of k_encode.cu, then the tensor-core kernel.
-static int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, bool verbose,
+int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, bool verbose,
                              tch_solver** out, Err& e) {
     tch_solver* s = nullptr;
     uint64_t* d_calls = nullptr;
@@ -444,8 +445,8 @@ static cudaError_t launch_dense_stripe(tch_solver* s, const StripeArgs& a, const
     return launch_tc_stripe(s->kernel, byte_operands(s), nullptr, dr, a, s->num_sms, st);
 }
 
-static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e,
-                         const int* unsorted_flag = nullptr) {
+int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e,
+                         const int* unsorted_flag) {
     if (r0 < 0 || rows < 0 || r0 > s->n) return e.set("stripe out of range (r0=%d rows=%d n=%d)", r0, rows, s->n);
     if (s->defer_js && !unsorted_flag) return e.set("partner lists not uploaded (run the whole pipeline)");
     if (r0 + rows > s->n) rows = s->n - r0;
@@ -460,6 +461,7 @@ static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_
     a.out = d_out;
     a.ldo = ldo;
     a.err = s->dErr;
+    a.cluster = s->cluster;
     RareCSR rare;
     if (!s->rare_on_host) {
         rare.start = s->dStart;
@@ -499,7 +501,7 @@ static int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_
     return 0;
 }
 
-static int solver_check(tch_solver* s, Err& e) {
+int solver_check(tch_solver* s, Err& e) {
     int h = 0;
     TCH_CK(e, cudaSetDevice(s->device));
     TCH_CK(e, cudaDeviceSynchronize());
@@ -709,6 +711,39 @@ fail:
     if (t1) cudaEventDestroy(t1);
     return rc;
 }
+
+void solver_set_cluster(tch_solver* s, int cm) { s->cluster = cm; }
+
+// A stripe with the rare-count block in caller memory R (dense-rare solvers;
+// others take the ordinary path): no allocation, so it can be captured.
+int solver_stripe_counts(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, uint16_t* R, size_t ldr,
+                         cudaStream_t st, Err& e) {
+    if (!s->dense) return solver_stripe(s, r0, rows, d_out, ldo, st, e);
+    if (r0 < 0 || rows < 0 || r0 > s->n) return e.set("stripe out of range (r0=%d rows=%d n=%d)", r0, rows, s->n);
+    if (r0 + rows > s->n) rows = s->n - r0;
+    if (rows == 0) return 0;
+    if (ldo < (size_t)(s->n - r0) || (ldo & 1) || ((uintptr_t)d_out & 15))
+        return e.set("ldo must be even and >= n - r0, the output 16-byte aligned");
+    if (ldr < up((size_t)(s->n - r0), kRareDenseAlign) || (ldr & 7) || ((uintptr_t)R & 15))
+        return e.set("rare-count block too narrow or misaligned");
+    StripeArgs a;
+    a.n = s->n;
+    a.r0 = r0;
+    a.rows = rows;
+    a.out = d_out;
+    a.ldo = ldo;
+    a.err = s->dErr;
+    a.cluster = s->cluster;
+    cudaError_t ce = launch_rare_dense(rare_groups(s), r0, rows, R, ldr, s->num_sms, st);
+    if (ce == cudaSuccess) ce = launch_dense_stripe(s, a, R, ldr, st);
+    if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
+    return 0;
+}
+
+// Work of one whole-triangle solve, for scheduling: pairs x operand bytes per row.
+double solver_work(const tch_solver* s) { return (double)s->n * (double)(s->n - 1) / 2.0 * (double)s->kb; }
+
+int solver_size(const tch_solver* s) { return s->n; }
 
 }  // namespace tch
 

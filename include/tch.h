@@ -234,6 +234,31 @@ int64_t tch_server_submit(tch_server* sv, int m, const uint64_t* qcalls, uint16_
 int tch_server_wait(tch_server* sv, int64_t id, double* queued_s, double* latency_s, char* err, int errlen);
 void tch_server_destroy(tch_server* sv);
 
+/* ---- batched solves (no reference counterpart) -----------------------------------
+ * `count` independent profile sets (set s: n[s] x L[s] allele calls, host u64,
+ * 0 = missing; tau[s] <= 0 or tau == NULL: chosen per set) encoded on the
+ * device once.  tch_batch_run writes every set's whole upper triangle into one
+ * device buffer: set s at d_out + offsets[s], row stride ld[s] u16
+ * (tch_batch_layout; offsets[count] = total u16 elements), cell (i, j), i < j,
+ * at (i * ld[s] + j).  The launches of all sets are spread over parallel
+ * streams and captured once as a CUDA graph (per output buffer), replayed on
+ * every later run; tch_batch_tune times every schedule (branch streams x
+ * tile-pass cluster size for small and large sets) and keeps the fastest.
+ * Errors found on the device are reported by tch_batch_check. */
+typedef struct tch_batch tch_batch;
+int tch_batch_create(int device, int count, const int* n, const int* L, const uint64_t* const* calls, const int* tau,
+                     tch_batch** out, char* err, int errlen);
+/* Add one more set (encoded now); invalidates the captured graph. */
+int tch_batch_add(tch_batch* b, int n, int L, const uint64_t* calls, int tau, char* err, int errlen);
+int tch_batch_layout(const tch_batch* b, size_t* offsets, size_t* ld);
+int tch_batch_run(tch_batch* b, uint16_t* d_out, void* stream, char* err, int errlen);
+int tch_batch_check(tch_batch* b, char* err, int errlen);
+int tch_batch_tune(tch_batch* b, uint16_t* d_out, void* stream, int reps, double* best_ms, int* best_branches,
+                   int* best_cm_small, int* best_cm_large, char* err, int errlen);
+int tch_batch_set_schedule(tch_batch* b, int branches, int cm_small, int cm_large);
+int tch_batch_info(const tch_batch* b, int* count, int* taus, int* branches, int* cm_small, int* cm_large);
+void tch_batch_destroy(tch_batch* b);
+
 /* Fill *info. */
 int tch_solver_info(const tch_solver* s, tch_info* info);
 
