@@ -66,7 +66,7 @@ def row_shares(n: int, ws: int):
     total = cum[-1]
     bounds = [0]
     for r in range(1, ws):
-        bounds.append(int(np.searchsorted(cum, total * r / ws)) // 128 * 128)
+        bounds.append(int(np.searchsorted(cum, total * r / ws)))
     bounds.append(n)
     return [(bounds[i], bounds[i + 1]) for i in range(ws)]
 
