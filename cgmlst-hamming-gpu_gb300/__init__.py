@@ -21,6 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libtch.so")
 CLI_PATH = os.path.join(HERE, "bin", "cgmlst-hamming-gpu")
+RANKS_TOOL_PATH = os.path.join(HERE, "bin", "tch-ranks")
 
 KERNELS = {"auto": 0, "popc": 1, "mma_b1": 2, "tc_f8": 3, "tc_i8": 4, "tc_f16": 5}
 
@@ -161,6 +162,8 @@ def lib():
         L.tch_batch_info.argtypes = [c_void, P(c_int), c_void, P(c_int), P(c_int), P(c_int)]
         L.tch_batch_info.restype = c_int
         L.tch_batch_destroy.argtypes, L.tch_batch_destroy.restype = [c_void], None
+        L.tch_solver_from_ranks.argtypes = [c_int, c_int, c_int, c_void, c_int, c_int, P(c_void), c_char_p, c_int]
+        L.tch_solver_from_ranks.restype = c_int
         _lib = L
     return _lib
 
@@ -430,6 +433,17 @@ class Solver:
         return cls(h)
 
     @classmethod
+    def from_ranks(cls, ranks: np.ndarray, tau: int = 0, kernel="auto", device: int = 0):
+        """Device encoding of dense per-locus ranks (n x L u16, 0 = missing)."""
+        ranks = np.ascontiguousarray(ranks, dtype=np.uint16)
+        n, L = ranks.shape
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        _check(lib().tch_solver_from_ranks(device, n, L, _ptr(ranks), tau, kernel_id(kernel), ctypes.byref(h), err,
+                                           len(err)), err)
+        return cls(h)
+
+    @classmethod
     def from_calls(cls, calls: np.ndarray, tau: int = 0, kernel="auto", device: int = 0):
         """Device encoding of allele calls (n x L u64, 0 = missing), tau <= 0 automatic."""
         calls = np.ascontiguousarray(calls, dtype=np.uint64)
@@ -660,3 +674,23 @@ class Batch:
 
     def __exit__(self, *a):
         self.close()
+
+
+# ---------------------------------------------------------------------------------------
+# ranks files (tensorcore/to_ranks.py: int32 n, int32 L, then n x L u16, 0 = missing)
+# ---------------------------------------------------------------------------------------
+
+def write_ranks(path: str, x: np.ndarray) -> None:
+    x = np.ascontiguousarray(x, dtype="<u2")
+    with open(path, "wb") as f:
+        np.array(x.shape, dtype="<i4").tofile(f)
+        x.tofile(f)
+
+
+def read_ranks(path: str) -> np.ndarray:
+    with open(path, "rb") as f:
+        n, L = np.fromfile(f, dtype="<i4", count=2)
+        x = np.fromfile(f, dtype="<u2", count=int(n) * int(L))
+    if x.size != int(n) * int(L):
+        raise TchError(f"{path}: truncated ranks file")
+    return x.reshape(int(n), int(L))

@@ -6,7 +6,8 @@ nvcc compiles each translation unit in parallel with
 ``-gencode arch=compute_103a,code=sm_103a -lineinfo -O3``; the objects are
 linked into ``lib/libtch.so`` (static CUDA runtime, so the library needs only
 the driver).  The CLI (``host/cgmlst_hamming_gpu.cpp``) is compiled with g++
-into ``bin/cgmlst-hamming-gpu`` and linked against ``lib/libtch.so``.
+into ``bin/cgmlst-hamming-gpu`` and linked against ``lib/libtch.so``, and the
+ranks-file front end (``host/ranks_tool.cpp``) into ``bin/tch-ranks``.
 Nothing is installed outside this directory.
 """
 from __future__ import annotations
@@ -108,6 +109,23 @@ def build_cli(verbose: bool = False) -> str | None:
     return out
 
 
+def build_ranks_tool(verbose: bool = False) -> str | None:
+    """bin/tch-ranks: the ranks-file front end (host/ranks_tool.cpp)."""
+    src = os.path.join(HOST, "ranks_tool.cpp")
+    if not os.path.exists(src):
+        return None
+    os.makedirs(BIN, exist_ok=True)
+    out = os.path.join(BIN, "tch-ranks")
+    lib = os.path.join(LIB, LIBNAME)
+    if not _newer(out, [src, lib, os.path.join(INCLUDE, "tch.h")]):
+        _run(["g++", "-O3", "-std=c++17", "-I", INCLUDE, src, "-o", out + ".tmp", "-L", LIB, "-ltch",
+              "-Wl,-rpath,$ORIGIN/../lib"])
+        os.replace(out + ".tmp", out)
+    if verbose:
+        print("built", out)
+    return out
+
+
 def build_peak(verbose: bool = False) -> str:
     """bin/tch-peak: the instruction-throughput probe (csrc/peak.cu)."""
     src = os.path.join(CSRC, "peak.cu")
@@ -126,6 +144,7 @@ def build(verbose: bool = False):
         fpeak = ex.submit(build_peak, verbose)
         lib = build_lib(verbose)
         cli = build_cli(verbose)
+        build_ranks_tool(verbose)
         fpeak.result()
     return lib, cli
 

@@ -344,15 +344,23 @@ static TauModel g_tau_model;
 
 // Operands on the device straight from allele calls (host buffer, n x L u64,
 // 0 = missing): the device encoder of k_encode.cu, then the tensor-core kernel.
-int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, bool verbose,
-                             tch_solver** out, Err& e) {
+// Ranks (u16, 0 = missing) as allele ids: equal ranks are equal alleles.
+__global__ void widen_ranks_kernel(const uint16_t* __restrict__ x, size_t count, uint64_t* calls) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < count; t += (size_t)gridDim.x * blockDim.x)
+        calls[t] = x[t];
+}
+
+// calls: host u64 allele ids, or (ranks != nullptr) host u16 ranks.
+static int solver_from_input(int device, int n, int L, const uint64_t* calls, const uint16_t* ranks, int tau,
+                             int kernel, bool verbose, tch_solver** out, Err& e) {
     tch_solver* s = nullptr;
     uint64_t* d_calls = nullptr;
+    uint16_t* d_ranks = nullptr;
     DeviceEncoding enc;
     *out = nullptr;
     if (n < 0 || L < 0) return e.set("negative size (n=%d, L=%d)", n, L);
     if (L > 65535) return e.set("more than 65535 loci (u16 distances)");
-    if ((size_t)n * L && !calls) return e.set("null input buffer");
+    if ((size_t)n * L && !calls && !ranks) return e.set("null input buffer");
     kernel = resolve_kernel(kernel);
     if (kernel != TCH_KERNEL_TC_F8 || !kernel_compiled(kernel))
         return e.set("the device encoder feeds the tensor-core kernel (tc_f8); kernel %s is not supported here",
@@ -368,7 +376,18 @@ int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, 
     TCH_CK(e, dmalloc(s, (void**)&s->dErr, sizeof(int)));
     TCH_CK(e, cudaMemset(s->dErr, 0, sizeof(int)));
     TCH_CK(e, cudaMalloc(&d_calls, std::max<size_t>((size_t)n * Le, 1) * 8));
-    if (L) {
+    if (L && ranks) {
+        const size_t count = (size_t)n * L;
+        TCH_CK(e, cudaMalloc(&d_ranks, std::max<size_t>(count, 1) * 2));
+        if (count) {
+            TCH_CK(e, cudaMemcpy(d_ranks, ranks, count * 2, cudaMemcpyHostToDevice));
+            widen_ranks_kernel<<<(int)std::min<size_t>((count + 255) / 256, (size_t)s->num_sms * 32), 256>>>(
+                d_ranks, count, d_calls);
+            TCH_CK(e, cudaGetLastError());
+        }
+        cudaFree(d_ranks);
+        d_ranks = nullptr;
+    } else if (L) {
         if ((size_t)n * L) TCH_CK(e, cudaMemcpy(d_calls, calls, (size_t)n * L * 8, cudaMemcpyHostToDevice));
     } else {
         TCH_CK(e, cudaMemset(d_calls, 0, std::max<size_t>((size_t)n, 1) * 8));
@@ -409,8 +428,14 @@ int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, 
     return 0;
 fail:
     if (d_calls) cudaFree(d_calls);
+    if (d_ranks) cudaFree(d_ranks);
     solver_free(s);
     return 1;
+}
+
+int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, bool verbose,
+                      tch_solver** out, Err& e) {
+    return solver_from_input(device, n, L, calls, nullptr, tau, kernel, verbose, out, e);
 }
 
 static RareGroups rare_groups(const tch_solver* s) {
@@ -811,6 +836,14 @@ int tch_solver_from_calls(int device, int n, int L, const uint64_t* calls, int t
     Err e{err, errlen};
     if (!out) return e.set("null output handle");
     return solver_from_calls(device, n, L, calls, tau, kernel, false, out, e);
+}
+
+int tch_solver_from_ranks(int device, int n, int L, const uint16_t* ranks, int tau, int kernel, tch_solver** out,
+                          char* err, int errlen) {
+    Err e{err, errlen};
+    if (!out) return e.set("null output handle");
+    if ((size_t)n * L && !ranks) return e.set("null input buffer");
+    return solver_from_input(device, n, L, nullptr, ranks, tau, kernel, false, out, e);
 }
 
 int tch_run_calls(int device, int n, int L, const uint64_t* calls, int tau, int S, tch_cb cb, void* ctx,

@@ -142,6 +142,12 @@ int tch_solver_from_bits(int device, int n, size_t n_pad, const uint8_t* O, size
 int tch_solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, tch_solver** out,
                           char* err, int errlen);
 
+/* The same from dense per-locus ranks (u16, 0 = missing; equal ranks are equal
+ * alleles), the payload of the reference prototype's ranks file
+ * (tensorcore/to_ranks.py: int32 n, int32 L, then n x L u16 row-major). */
+int tch_solver_from_ranks(int device, int n, int L, const uint16_t* ranks, int tau, int kernel, tch_solver** out,
+                          char* err, int errlen);
+
 /* tch_run's stripe/callback contract on allele calls: device encoding, then
  * the whole upper triangle through the callback.  *tau_used (may be NULL)
  * receives the tau that was used.  TCH_VERBOSE=1 prints the tau table. */
