@@ -33,6 +33,10 @@ CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.
                       ctypes.POINTER(ctypes.c_uint16))
 
 
+TEXT_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_char), ctypes.c_size_t)
+LAYOUTS = {"full": 0, "lower-tri": 1, "upper-tri": 2}
+
+
 class TchError(RuntimeError):
     pass
 
@@ -137,6 +141,8 @@ def lib():
         L.tch_db_info.argtypes = [c_void, P(c_int), P(c_int), P(c_int), P(c_size), P(c_size)]
         L.tch_db_info.restype = c_int
         L.tch_db_query_bytes.argtypes, L.tch_db_query_bytes.restype = [c_void, c_int], c_size
+        L.tch_host_alloc.argtypes, L.tch_host_alloc.restype = [c_size], c_void
+        L.tch_host_free.argtypes, L.tch_host_free.restype = [c_void], None
         L.tch_db_query.argtypes = [c_void, c_int, c_void, c_void, c_void, c_void, c_char_p, c_int]
         L.tch_db_query.restype = c_int
         L.tch_server_create.argtypes = [c_void, c_int, c_size, P(c_void), c_char_p, c_int]
@@ -164,6 +170,9 @@ def lib():
         L.tch_batch_destroy.argtypes, L.tch_batch_destroy.restype = [c_void], None
         L.tch_solver_from_ranks.argtypes = [c_int, c_int, c_int, c_void, c_int, c_int, P(c_void), c_char_p, c_int]
         L.tch_solver_from_ranks.restype = c_int
+        L.tch_solver_write_tsv.argtypes = [c_void, P(c_char_p), c_char_p, c_char_p, c_int, c_int, c_int, TEXT_CB,
+                                           c_void, c_char_p, c_int]
+        L.tch_solver_write_tsv.restype = c_int
         _lib = L
     return _lib
 
@@ -482,6 +491,26 @@ class Solver:
         err = _errbuf()
         _check(lib().tch_solver_check(self._h, err, len(err)), err)
 
+    def write_tsv(self, ids, osep: str = "\t", index_name: str = "cgmlst-hamming-gpu", layout: str = "full",
+                  cap: int = 0, block_rows: int = 0, sink=None) -> str | None:
+        """The reference's TSV matrix, formatted on the GPU; returns the text,
+        or hands each chunk (bytes) to sink(chunk) when given."""
+        parts = []
+
+        def take(ctx, p, n):
+            chunk = ctypes.string_at(p, n)
+            if sink is not None:
+                sink(chunk)
+            else:
+                parts.append(chunk)
+
+        cb = TEXT_CB(take)
+        arr = (ctypes.c_char_p * max(len(ids), 1))(*[i.encode() for i in ids])
+        err = _errbuf()
+        _check(lib().tch_solver_write_tsv(self._h, arr, osep.encode(), index_name.encode(), LAYOUTS[layout], cap,
+                                          block_rows, cb, None, err, len(err)), err)
+        return None if sink is not None else b"".join(parts).decode()
+
     def run(self, stripe: int = 512, sink: StripeSink | None = None):
         sink = sink or StripeSink(self.info()["n"])
         cb = CB(sink)
@@ -511,6 +540,21 @@ class Solver:
 # ---------------------------------------------------------------------------------------
 # serving: resident database, query batches, continuous batching
 # ---------------------------------------------------------------------------------------
+
+def pinned_empty(shape, dtype=np.uint16) -> np.ndarray:
+    """A numpy array in page-locked host memory (freed with the array)."""
+    import weakref
+
+    dtype = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dtype.itemsize
+    p = lib().tch_host_alloc(nbytes)
+    if not p:
+        raise TchError(f"could not page-lock {nbytes} bytes")
+    buf = (ctypes.c_char * max(nbytes, 1)).from_address(p)
+    a = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+    weakref.finalize(buf, lib().tch_host_free, p)
+    return a
+
 
 class Database:
     """A profile database resident on the device (tch_db)."""
@@ -570,11 +614,16 @@ class Server:
         self.db = db
         self._live = {}
 
-    def submit(self, q: np.ndarray, want_qq: bool = True) -> int:
+    def submit(self, q: np.ndarray, want_qq: bool = True, out: np.ndarray | None = None,
+               out_qq: np.ndarray | None = None) -> int:
+        """out / out_qq: caller buffers for the results (m x n and m x m u16;
+        page-locked ones, see pinned_empty, arrive fastest)."""
         q = np.ascontiguousarray(q, dtype=np.uint64)
         m = q.shape[0]
-        qdb = np.empty((m, self.db.n), np.uint16)  # every cell is written
-        qq = np.zeros((m, m), np.uint16) if want_qq else None
+        qdb = out if out is not None else np.empty((m, self.db.n), np.uint16)  # every cell is written
+        if qdb.shape != (m, self.db.n) or qdb.dtype != np.uint16 or not qdb.flags.c_contiguous:
+            raise TchError("out must be a C-contiguous m x n uint16 array")
+        qq = (out_qq if out_qq is not None else np.zeros((m, m), np.uint16)) if want_qq else None
         rid = lib().tch_server_submit(self._h, m, _ptr(q), _ptr(qdb), _ptr(qq) if want_qq else None)
         if rid < 0:
             raise TchError("request rejected")

@@ -78,12 +78,13 @@ __global__ void insert_kernel(const uint64_t* __restrict__ calls, int n, int L, 
 __global__ void rank_kernel(int k0, const unsigned long long* keys, const uint32_t* cnts, int logC,
                             const uint32_t* nd, const uint64_t* cnt_off, uint32_t* cnt_flat, uint16_t* rank_slot,
                             unsigned long long* list_keys, uint32_t* list_slots, unsigned long long* slot_ids,
-                            int* err) {
+                            uint32_t lcap, int* err) {
     const int kk = blockIdx.x;
     const size_t C = (size_t)1 << logC;
     const unsigned long long* kt = keys + kk * C;
-    unsigned long long* lk = list_keys + (size_t)kk * kMaxDistinct;
-    uint32_t* ls = list_slots + (size_t)kk * kMaxDistinct;
+    // a locus has at most min(n, kMaxDistinct) distinct ids: lcap entries per list
+    unsigned long long* lk = list_keys + (size_t)kk * lcap;
+    uint32_t* ls = list_slots + (size_t)kk * lcap;
     __shared__ uint32_t m;
     __shared__ unsigned long long tile[2048];
     if (threadIdx.x == 0) m = 0;
@@ -92,7 +93,7 @@ __global__ void rank_kernel(int k0, const unsigned long long* keys, const uint32
         const unsigned long long v = kt[s];
         if (v) {
             const uint32_t idx = atomicAdd(&m, 1u);
-            if (idx < kMaxDistinct) {
+            if (idx < lcap) {
                 lk[idx] = v;
                 ls[idx] = s;
             }
@@ -100,7 +101,7 @@ __global__ void rank_kernel(int k0, const unsigned long long* keys, const uint32
     }
     __syncthreads();
     const uint32_t mm = m;
-    if (mm > kMaxDistinct || mm != nd[k0 + kk]) {
+    if (mm > lcap || mm != nd[k0 + kk]) {
         if (threadIdx.x == 0) atomicOr(err, DEVERR_TOO_MANY_ALLELES);
         return;
     }
@@ -476,7 +477,8 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
     while (((size_t)1 << logC) < 2 * (size_t)std::min<int>(std::max(n, 1), (int)kMaxDistinct)) logC++;
     const size_t C = (size_t)1 << logC;
     // loci per batch: hash tables + id lists within ~2 GB
-    const size_t per_locus = C * (8 + 4 + 2) + (size_t)kMaxDistinct * 12;
+    const uint32_t lcap = (uint32_t)std::min<int>(std::max(n, 1), (int)kMaxDistinct);
+    const size_t per_locus = C * (8 + 4 + 2) + (size_t)lcap * 12;
     const int nk_max = (int)std::max<size_t>(1, std::min<size_t>((size_t)L, ((size_t)2 << 30) / per_locus));
     unsigned long long* keys = nullptr;
     uint32_t *cnts = nullptr, *nd = nullptr, *list_slots = nullptr, *cnt_flat = nullptr, *gfill = nullptr;
@@ -513,8 +515,8 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
     TCH_CK(e, dalloc(&keys, C * nk_max, &tmp_bytes));
     TCH_CK(e, dalloc(&cnts, C * nk_max, &tmp_bytes));
     TCH_CK(e, dalloc(&rank_slot, C * nk_max, &tmp_bytes));
-    TCH_CK(e, dalloc(&list_keys, (size_t)kMaxDistinct * nk_max, &tmp_bytes));
-    TCH_CK(e, dalloc(&list_slots, (size_t)kMaxDistinct * nk_max, &tmp_bytes));
+    TCH_CK(e, dalloc(&list_keys, (size_t)lcap * nk_max, &tmp_bytes));
+    TCH_CK(e, dalloc(&list_slots, (size_t)lcap * nk_max, &tmp_bytes));
     TCH_CK(e, dalloc(&cnt_off_d, (size_t)L + 1, nullptr));
 
     // ---- 1-3: ranks and counts, batch by batch
@@ -557,7 +559,7 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
                 TCH_CK(e, cudaGetLastError());
             }
             rank_kernel<<<nk, 512>>>(k0, keys, cnts, logC, nd, cnt_off_d, cnt_flat, rank_slot, list_keys, list_slots,
-                                     slot_ids, err_d);
+                                     slot_ids, lcap, err_d);
             TCH_CK(e, cudaGetLastError());
             cell_rank_kernel<<<grid_for((size_t)n * nk, sms), 256>>>(d_calls, n, L, k0, nk, keys, rank_slot, logC,
                                                                       out->x, err_d);

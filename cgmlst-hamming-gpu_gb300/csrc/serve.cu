@@ -138,6 +138,14 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
     KChunks X = enc.X;  // same K layout as the database's rows, m rows
     for (int c = 0; c < kMaxKChunks; c++) X.p[c] = nullptr;
     cudaError_t ce = cudaSuccess;
+    // TCH_VERBOSE=1: device time of each phase on stderr
+    const char* vb = getenv("TCH_VERBOSE");
+    const bool verbose = vb && vb[0] == '1';
+    cudaEvent_t ev[8] = {};
+    int nev = 0;
+    auto mark = [&]() {
+        if (verbose && nev < 8 && cudaEventCreate(&ev[nev]) == cudaSuccess) cudaEventRecord(ev[nev++], st);
+    };
     auto alloc = [&](void** p, size_t bytes) {
         if (ce == cudaSuccess) ce = cudaMallocFromPoolAsync(p, std::max<size_t>(bytes, 16), db->pool, st);
     };
@@ -154,6 +162,7 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
     }
     if (h_qq && m > 1) alloc((void**)&qq, (size_t)m * ldq * 2);
     if (ce != cudaSuccess) goto done;
+    mark();
     ce = cudaMemcpyAsync(dq, qcalls, (size_t)m * L * 8, cudaMemcpyHostToDevice, st);
     if (ce == cudaSuccess) ce = cudaMemsetAsync(derr, 0, 4, st);
     if (ce != cudaSuccess) goto done;
@@ -163,6 +172,7 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
             for (int c = 0; c < X.n && ce == cudaSuccess; c++)
                 ce = cudaMemsetAsync(X.p[c], 0, mr * (size_t)X.width_of(c), st);
             if (ce != cudaSuccess) goto done;
+            mark();
             query_rank_kernel<<<grid, 256, 0, st>>>(dq, m, L, enc.cnt_off, enc.slot_ids, xq);
             query_pack_kernel<<<grid, 256, 0, st>>>(xq, m, L, enc.cnt_off, enc.col, enc.base, X, enc.kp, 0x38);
             ce = cudaGetLastError();
@@ -175,7 +185,9 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
             g.mpos = enc.mpos;
             g.n = n;
             g.L = L;
+            mark();
             ce = launch_rare_query(g, xq, m, R, ldr, db->sms, st);
+            mark();
             if (ce != cudaSuccess) goto done;
             ByteOperands qa, dbb;
             qa.X = X.p[0];
@@ -202,6 +214,7 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
             a.rect = true;
             ce = launch_tc_stripe(TCH_KERNEL_TC_F8, qa, &dbb, dr, a, db->sms, st);
             if (ce != cudaSuccess) goto done;
+            mark();
             ce = cudaMemcpy2DAsync(h_qdb, (size_t)n * 2, out, ldo * 2, (size_t)n * 2, m, cudaMemcpyDeviceToHost, st);
             if (ce != cudaSuccess) goto done;
         }
@@ -222,8 +235,20 @@ done:
             if (p) cudaFreeAsync(p, st);
         for (int c = 0; c < X.n; c++)
             if (X.p[c]) cudaFreeAsync(X.p[c], st);
+        mark();
         const cudaError_t se = cudaStreamSynchronize(st);
         if (ce == cudaSuccess) ce = se;
+        if (nev > 1) {
+            static const char* names[] = {"h2d", "rank+pack", "rare counts", "tile pass", "d2h + q x q", "", "", ""};
+            fprintf(stderr, "tch query m=%d:", m);
+            for (int k = 0; k + 1 < nev; k++) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+                fprintf(stderr, " %s %.2f ms", names[k], ms);
+            }
+            fprintf(stderr, "\n");
+        }
+        for (int k = 0; k < nev; k++) cudaEventDestroy(ev[k]);
         if (ce != cudaSuccess) return e.set("query batch: %s", cudaGetErrorString(ce));
         if (herr) return e.set("query batch: device reported error 0x%x", herr);
     }
@@ -350,6 +375,15 @@ fail:
         delete db;
     }
     return 1;
+}
+
+void* tch_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    return cudaMallocHost(&p, std::max<size_t>(bytes, 16)) == cudaSuccess ? p : nullptr;
+}
+
+void tch_host_free(void* p) {
+    if (p) cudaFreeHost(p);
 }
 
 void tch_db_destroy(tch_db* db) {

@@ -14,7 +14,8 @@
 //
 // Differences that do not change any output byte: the automatic tau uses rates
 // measured on GB300 instead of the L4 constants of main.rs:170-171, and the
-// writer formats and writes with a thread pool instead of rayon.
+// writer formats on the GPU (tch_solver_write_tsv; --host-format: a thread
+// pool on the CPU) instead of with rayon.
 
 #include <dlfcn.h>
 #include <errno.h>
@@ -84,6 +85,7 @@ struct Args {
     size_t device = 0;
     bool silent = false;
     bool host_encode = false;
+    bool host_format = false;
 };
 
 const char* kUsage =
@@ -110,6 +112,7 @@ const char* kUsage =
     "      --device <DEVICE>                    CUDA device [default: 0]\n"
     "  -s, --silent                             Suppress progress/log messages on stderr\n"
     "      --host-encode                        Encode on the host and call tch_run (the reference's path)\n"
+    "      --host-format                        Format the matrix text on the CPU (default: on the GPU)\n"
     "  -h, --help                               Print help\n"
     "  -V, --version                            Print version\n";
 
@@ -154,7 +157,7 @@ Args parse_args(int argc, char** argv) {
                                {"z", "gzip", false},         {"X", "max-dist", true},
                                {nullptr, "tau", true},       {nullptr, "stripe", true},
                                {nullptr, "device", true},    {"s", "silent", false},
-                               {nullptr, "host-encode", false},
+                               {nullptr, "host-encode", false},     {nullptr, "host-format", false},
                                {"h", "help", false},         {"V", "version", false}};
     for (int k = 1; k < argc; k++) {
         std::string arg = argv[k];
@@ -242,6 +245,8 @@ Args parse_args(int argc, char** argv) {
             a.silent = true;
         } else if (name == "host-encode") {
             a.host_encode = true;
+        } else if (name == "host-format") {
+            a.host_format = true;
         }
     }
     if (!have_input) usage_error("the following required arguments were not provided:\n  --input <INPUT>");
@@ -473,6 +478,12 @@ struct FileOut {
     }
 };
 
+// tch_text_cb into a writer.
+template <class W>
+void text_to(void* ctx, const char* text, size_t len) {
+    static_cast<W*>(ctx)->write(text, len);
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -575,6 +586,23 @@ int main(int argc, char** argv) {
     }
     if (L > 65535) die("more than 65535 loci (u16 distances)");
 
+    // ---- output (main.rs:472-490): a file or stdout, gzip level 3 with -z or *.gz
+    const bool gz = args.gzip || (args.has_output && args.output.size() >= 3 &&
+                                  args.output.compare(args.output.size() - 3, 3, ".gz") == 0);
+    auto open_out = [&]() {
+        FILE* f = stdout;
+        if (args.has_output) {
+            f = fopen(args.output.c_str(), "wb");
+            if (!f) die(fmt("creating %s: %s", args.output.c_str(), strerror(errno)));
+        }
+        setvbuf(f, nullptr, _IOFBF, 16 << 20);
+        return f;
+    };
+    auto close_out = [&](FILE* f) {
+        if (fflush(f) != 0) die(fmt("writing output: %s", strerror(errno)));
+        if (f != stdout) fclose(f);
+    };
+
     // ---- encode (main.rs:353-445) and GPU (main.rs:447-465)
     t = now();
     char err[512] = {0};
@@ -594,6 +622,31 @@ int main(int argc, char** argv) {
         log(fmt("Encoded in %.2fs: tau=%d, one-hot cols=%zu, rare equal pairs=%zu", now() - t, info.tau,
                 info.d_onehot, info.n_rare));
         t = now();
+        if (!args.host_format) {
+            // the matrix stays in HBM and is formatted there; text blocks come back in order
+            std::vector<const char*> idp(n);
+            for (size_t i = 0; i < n; i++) idp[i] = ids[i].c_str();
+            const int lay = args.layout == Layout::Full ? 0 : args.layout == Layout::LowerTri ? 1 : 2;
+            FILE* f = open_out();
+            FileOut fo{f};
+            int rc;
+            if (gz) {
+                tch_host::GzipWriter<FileOut> z(fo, 3);
+                rc = tch_solver_write_tsv(solver, idp.data(), args.output_sep.c_str(), args.index_name.c_str(), lay,
+                                          args.max_dist, 0, text_to<tch_host::GzipWriter<FileOut>>, &z, err,
+                                          sizeof err);
+                if (!rc) z.finish();
+            } else {
+                rc = tch_solver_write_tsv(solver, idp.data(), args.output_sep.c_str(), args.index_name.c_str(), lay,
+                                          args.max_dist, 0, text_to<FileOut>, &fo, err, sizeof err);
+            }
+            tch_solver_destroy(solver);
+            if (rc) die(fmt("CUDA: %s", err));
+            close_out(f);
+            log(fmt("Computed and wrote the %zu x %zu matrix (tensor cores, text formatted on the GPU) in %.2fs. "
+                    "Total %.2fs", n, n, now() - t, now() - t_start));
+            return 0;
+        }
         Sink sink{&upper, threads};
         const int rc = tch_solver_run(solver, (int)stripe, on_stripe, &sink, &gpu_secs, err, sizeof err);
         tch_solver_destroy(solver);
@@ -638,14 +691,7 @@ int main(int argc, char** argv) {
 
     // ---- write (main.rs:472-490)
     t = now();
-    const bool gz = args.gzip || (args.has_output && args.output.size() >= 3 &&
-                                  args.output.compare(args.output.size() - 3, 3, ".gz") == 0);
-    FILE* f = stdout;
-    if (args.has_output) {
-        f = fopen(args.output.c_str(), "wb");
-        if (!f) die(fmt("creating %s: %s", args.output.c_str(), strerror(errno)));
-    }
-    setvbuf(f, nullptr, _IOFBF, 16 << 20);
+    FILE* f = open_out();
     FileOut fo{f};
     if (gz) {
         tch_host::GzipWriter<FileOut> z(fo, 3);
@@ -654,8 +700,7 @@ int main(int argc, char** argv) {
     } else {
         write_matrix(fo, ids, upper, args.output_sep, args.index_name, args.layout, args.max_dist, threads);
     }
-    if (fflush(f) != 0) die(fmt("writing output: %s", strerror(errno)));
-    if (f != stdout) fclose(f);
+    close_out(f);
     log(fmt("Wrote output in %.2fs. Total %.2fs", now() - t, now() - t_start));
     return 0;
 }

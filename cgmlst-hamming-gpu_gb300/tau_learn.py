@@ -1,12 +1,12 @@
 """Training data and training of the learned tau model.
 
-    python -m tau_learn sweep  [--datasets 240] [--out tau_sweep_gb300.npz]
+    python -m tau_learn sweep  [--datasets 200] [--out tau_sweep_gb300.npz]
     python -m tau_learn train  [--sweep tau_sweep_gb300.npz] [--out tau_mlp_gb300.f32]
 
 (run from this directory, or ``python cgmlst-hamming-gpu_gb300/tau_learn.py``).
 
 sweep: seeded synthetic profile sets of varied shape (n log-uniform in
-[2 000, 63 005], L from the shapes the configs name, n x L <= 7.2e7; three in
+[50, 63 005], L from the shapes the configs name, n x L <= 7.2e7; three in
 four Zipf (s in [1.0, 1.4], lognormal distinct-allele counts, 5 % 64-bit ids),
 one in four founder models (3-60 alleles per locus, 0.2-5 % mutations to new
 ids); 0-8 % missing).  For each set
@@ -45,7 +45,7 @@ def dataset_params(seed: int) -> dict:
     """Shape and allele law of profile set `seed`: one in four is a founder
     model (few alleles per locus, rare mutations), the rest Zipf."""
     rng = np.random.default_rng(1000 + seed)
-    n = int(np.exp(rng.uniform(np.log(2000), np.log(63005))))
+    n = int(np.exp(rng.uniform(np.log(50), np.log(63005))))
     L = int(rng.choice(LOCI))
     while n * L > 7.2e7:
         L = int(rng.choice(LOCI[:3]))
@@ -198,7 +198,7 @@ def train(sweep_path: str, out: str, steps: int = 6000, lr: float = 3e-3, seed: 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("cmd", choices=["sweep", "train"])
-    ap.add_argument("--datasets", type=int, default=240)
+    ap.add_argument("--datasets", type=int, default=200)
     ap.add_argument("--sweep", default=SWEEP_PATH)
     ap.add_argument("--out", default=None)
     ap.add_argument("--steps", type=int, default=6000)

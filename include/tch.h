@@ -226,6 +226,11 @@ size_t tch_db_query_bytes(const tch_db* db, int m);
 int tch_db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* qdb, uint16_t* qq, void* stream, char* err,
                  int errlen);
 
+/* Page-locked host memory (results copied into it reach the host at the
+ * link's speed; pageable buffers go through a staging copy). */
+void* tch_host_alloc(size_t bytes);
+void tch_host_free(void* p);
+
 /* Continuous batching: `slots` worker threads, one stream each; a FIFO of
  * requests, admitted when tch_db_query_bytes(m) fits in `budget` bytes next to
  * the requests running (0 = half the free device memory; a request larger than
@@ -291,6 +296,18 @@ int tch_solver_rare_counts(tch_solver* s, int r0, int rows, uint16_t* d_R, size_
                            int errlen);
 int tch_solver_stripe_counts(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, const uint16_t* d_R,
                              size_t ldr, void* stream, char* err, int errlen);
+
+/* The whole matrix as the reference's TSV (tensorcore/rs/src/main.rs:224-265:
+ * header `index_name{osep id}*`, then per sample `id{osep value}*`, newline;
+ * layout 0 full, 1 lower-tri, 2 upper-tri (masked cells print 0, the diagonal
+ * 0), then cap > 0 caps every value), formatted on the GPU: the upper triangle
+ * is computed into device memory, mirrored, and formatted in blocks of
+ * block_rows rows (0 = 2048); cb receives the header, then every block's text,
+ * in order, on the calling thread.  No reference counterpart as an entry
+ * point (the reference formats on the CPU). */
+typedef void (*tch_text_cb)(void* ctx, const char* text, size_t len);
+int tch_solver_write_tsv(tch_solver* s, const char* const* ids, const char* osep, const char* index_name, int layout,
+                         int cap, int block_rows, tch_text_cb cb, void* ctx, char* err, int errlen);
 
 /* Synchronise the device and report any error recorded by earlier stripes. */
 int tch_solver_check(tch_solver* s, char* err, int errlen);

@@ -73,14 +73,18 @@ def case_files(tmp_path_factory, golden):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("encoder", ["device", "host"])
+@pytest.mark.parametrize("encoder", ["device", "device-hostformat", "host"])
 @pytest.mark.parametrize("case_idx", [0, 1, 2])
 @pytest.mark.parametrize("flags_idx", range(len(refgen.CHECKPY_FLAGSETS)))
 def test_checkpy_matrix(pkg, case_files, encoder, case_idx, flags_idx):
+    """device: device encoder + text formatted on the GPU; device-hostformat:
+    device encoder + the CPU writer; host: the reference's path (tch_run)."""
     c, path, A = case_files[case_idx]
     args, kind = refgen.CHECKPY_FLAGSETS[flags_idx]
     if encoder == "host":
         args = args + ["--host-encode"]
+    elif encoder == "device-hostformat":
+        args = args + ["--host-format"]
     r = run(pkg, ["-s", "-i", path, *args])
     assert r.returncode == 0, r.stderr
     got = parse(r.stdout, "," if "-D" in args else "\t")
@@ -100,10 +104,12 @@ def test_full_text_equals_oracle(pkg, tmp_path):
     p.write_text(text)
     ids, x, cnt, H = oracle.distances_from_text(text)
     for args, kw in [([], {}), (["-m", "lower-tri", "-D", ";"], dict(mode="lower-tri", osep=";")),
-                     (["-m", "upper-tri", "-X", "1", "-x", "ID"], dict(mode="upper-tri", cap=1, index_name="ID"))]:
-        r = run(pkg, ["-s", "-i", str(p), *args])
-        assert r.returncode == 0, r.stderr
-        assert r.stdout == oracle.write_matrix(ids, H, **kw)
+                     (["-m", "upper-tri", "-X", "1", "-x", "ID"], dict(mode="upper-tri", cap=1, index_name="ID")),
+                     (["-D", "::"], dict(osep="::"))]:
+        for fmt in ([], ["--host-format"], ["--host-encode"]):
+            r = run(pkg, ["-s", "-i", str(p), *args, *fmt])
+            assert r.returncode == 0, r.stderr
+            assert r.stdout == oracle.write_matrix(ids, H, **kw), fmt
 
 
 @pytest.mark.gpu
@@ -169,3 +175,20 @@ def test_edge_inputs(pkg, tmp_path):
     assert r.returncode == 0 and r.stdout == "cgmlst-hamming-gpu\tA\tB\nA\t0\t0\nB\t0\t0\n"
     r = go("F\tL0\n")  # header only
     assert r.returncode == 0 and r.stdout == "cgmlst-hamming-gpu\n"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("layout,osep,cap,block", [("full", "\t", 0, 7), ("lower-tri", ",", 3, 64),
+                                                   ("upper-tri", "\t", 0, 1), ("full", " | ", 40, 0)])
+def test_gpu_tsv_writer_blocks(pkg, layout, osep, cap, block):
+    """tch_solver_write_tsv over several blocks of rows equals the oracle's text."""
+    rng = np.random.default_rng(11)
+    n, L = 300, 120
+    A = rng.integers(0, 30, size=(n, L)).astype(np.uint64)
+    A[:, :10] = rng.integers(0, 2000, size=(n, 10))
+    x = oracle.dense_ranks(A)[0]
+    H = oracle.hamming(x)
+    ids = [f"s{i}" * (1 + i % 3) for i in range(n)]
+    with pkg.Solver.from_calls(A) as s:
+        text = s.write_tsv(ids, osep=osep, index_name="IDX", layout=layout, cap=cap, block_rows=block)
+    assert text == oracle.write_matrix(ids, H, osep=osep, index_name="IDX", mode=layout, cap=cap)
