@@ -332,6 +332,7 @@ def main():
     ap.add_argument("--no-tau-sweep", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-tsv", action="store_true")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--serve-db", type=int, default=200000)
     ap.add_argument("--serve-requests", type=int, default=100)
@@ -565,6 +566,35 @@ def main():
                      "d2h_bytes_per_step": int(d2h), "seconds_per_step": ec, "tau": int(tu.value),
                      "path": "tch_run_calls: allele calls uploaded, device encoder, same stripes and copy-back"}
 
+    # the reference's TSV writer (main.rs:224-265) on the GPU: the full matrix
+    # as text, delivered block by block to a callback that discards it
+    tsv = None
+    if rank == 0 and ws == 1 and not args.no_tsv:
+        import ctypes
+
+        nbytes = [0]
+
+        def take(ctx, p, n):
+            nbytes[0] += n
+
+        cb = tch.TEXT_CB(take)
+        ids = (ctypes.c_char_p * n)(*[f"sample{i:05d}".encode() for i in range(n)])
+        err = ctypes.create_string_buffer(512)
+        times = []
+        for _ in range(2):
+            nbytes[0] = 0
+            t = time.perf_counter()
+            rc = tch.lib().tch_solver_write_tsv(solver._h, ids, b"\t", b"cgmlst-hamming-gpu", 0, 0, 0, cb, None,
+                                                err, len(err))
+            times.append(time.perf_counter() - t)
+            if rc:
+                raise RuntimeError(err.value.decode())
+        tsv = {"bytes": nbytes[0], "seconds": min(times), "gb_per_s": nbytes[0] / min(times) / 1e9,
+               "pairs_per_s": pairs_total / min(times),
+               "path": "tch_solver_write_tsv: whole triangle computed, mirrored, formatted on the GPU in blocks of "
+                       "2048 rows, copied to pinned host memory, handed to a callback (full layout, tab)"}
+        log("tsv writer:", tsv)
+
     serving = None
     batched = None
     if rank == 0 and ws == 1 and not (args.no_serving and args.no_batch):
@@ -593,7 +623,7 @@ def main():
                                                     parallelism=f"row shares x{ws}"),
                 "gpu_launches": args.steps * launches_per_step, "step_split": split,
                 "clocks": ck, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "e2e_device_encoder": e2e_calls, "tau_choice": tau_cmp, "batched": batched, "serving": serving,
+                "e2e_device_encoder": e2e_calls, "tau_choice": tau_cmp, "tsv_writer": tsv, "batched": batched, "serving": serving,
                 "peak_probe": peak_info}
         print(json.dumps(line), flush=True)
     if ws > 1:

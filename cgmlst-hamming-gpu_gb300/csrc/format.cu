@@ -13,6 +13,7 @@
 
 #include <string.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -132,6 +133,38 @@ __global__ void row_write_kernel(const uint16_t* H, size_t ld, int n, int r0, in
     }
 }
 
+// Page-locked text buffers cost far more to allocate than to fill, so the pair
+// of the previous call is kept for the next (one pair per process; a call that
+// finds it in use allocates its own).
+std::mutex g_text_mu;
+char* g_text[2] = {nullptr, nullptr};
+size_t g_text_bytes = 0;
+bool g_text_busy = false;
+
+bool text_acquire(size_t bytes, char* out[2]) {
+    std::lock_guard<std::mutex> lk(g_text_mu);
+    if (g_text_busy) return false;
+    if (g_text_bytes < bytes) {
+        for (int b = 0; b < 2; b++) {
+            if (g_text[b]) cudaFreeHost(g_text[b]);
+            g_text[b] = nullptr;
+        }
+        g_text_bytes = 0;
+        for (int b = 0; b < 2; b++)
+            if (cudaMallocHost(&g_text[b], bytes) != cudaSuccess) return false;
+        g_text_bytes = bytes;
+    }
+    g_text_busy = true;
+    out[0] = g_text[0];
+    out[1] = g_text[1];
+    return true;
+}
+
+void text_release() {
+    std::lock_guard<std::mutex> lk(g_text_mu);
+    g_text_busy = false;
+}
+
 }  // namespace
 }  // namespace tch
 
@@ -152,6 +185,7 @@ extern "C" int tch_solver_write_tsv(tch_solver* s, const char* const* ids, const
     std::string head;
     size_t cap_bytes = 0;
     int prev = -1;
+    bool pooled = false;
     uint64_t prev_len = 0, lens[2] = {0, 0};
     if (!s || !ids || !osep || !index_name || !cb) return e.set("null argument");
     if (layout < 0 || layout > 2) return e.set("layout must be 0 (full), 1 (lower-tri) or 2 (upper-tri)");
@@ -205,10 +239,11 @@ extern "C" int tch_solver_write_tsv(tch_solver* s, const char* const* ids, const
         cap_bytes = (size_t)block_rows * (maxid + (size_t)n * (seplen + 5) + 1);
     }
     TCH_CK(e, cudaMalloc(&d_len, (size_t)block_rows * 8));
+    pooled = text_acquire(cap_bytes, h_text);
     for (int b = 0; b < 2; b++) {
         TCH_CK(e, cudaMalloc(&d_off[b], ((size_t)block_rows + 1) * 8));
         TCH_CK(e, cudaMalloc(&d_text[b], cap_bytes));
-        TCH_CK(e, cudaMallocHost(&h_text[b], cap_bytes));
+        if (!pooled) TCH_CK(e, cudaMallocHost(&h_text[b], cap_bytes));
         TCH_CK(e, cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming));
     }
     for (int r0 = 0;; r0 += block_rows) {
@@ -245,9 +280,10 @@ fail:
     for (int b = 0; b < 2; b++) {
         cudaFree(d_off[b]);
         cudaFree(d_text[b]);
-        if (h_text[b]) cudaFreeHost(h_text[b]);
+        if (h_text[b] && !pooled) cudaFreeHost(h_text[b]);
         if (done[b]) cudaEventDestroy(done[b]);
     }
     if (st) cudaStreamDestroy(st);
+    if (pooled) text_release();
     return rc;
 }
