@@ -577,14 +577,16 @@ class Database:
     def query_bytes(self, m: int) -> int:
         return lib().tch_db_query_bytes(self._h, m)
 
-    def query(self, q: np.ndarray, want_qq: bool = True, stream: int = 0):
-        """(q x database distances [m x n], q x q upper triangle [m x m] or None)."""
+    def query(self, q: np.ndarray, want_qq: bool = True, stream: int = 0, out: np.ndarray | None = None,
+              out_qq: np.ndarray | None = None):
+        """(q x database distances [m x n], q x q upper triangle [m x m] or None);
+        out / out_qq: caller buffers (page-locked ones arrive fastest)."""
         q = np.ascontiguousarray(q, dtype=np.uint64)
         m = q.shape[0]
         if q.shape[1] != self.L:
             raise TchError(f"queries have {q.shape[1]} loci, the database {self.L}")
-        qdb = np.empty((m, self.n), np.uint16)  # every cell is written
-        qq = np.zeros((m, m), np.uint16) if want_qq else None
+        qdb = out if out is not None else np.empty((m, self.n), np.uint16)  # every cell is written
+        qq = (out_qq if out_qq is not None else np.zeros((m, m), np.uint16)) if want_qq else None
         err = _errbuf()
         _check(lib().tch_db_query(self._h, m, _ptr(q), _ptr(qdb), _ptr(qq) if want_qq else None,
                                   ctypes.c_void_p(stream) if stream else None, err, len(err)), err)

@@ -348,6 +348,7 @@ struct TauRow {
     int tau = 0;
     size_t d = 0;             // frequent one-hot columns
     double r = 0, cells = 0;  // rare pairs, cells in rare groups
+    double sq = 0;            // sum of squared counts of the alleles that are not frequent
     double kb = 0, mem = 0, t = 0;
     bool fits = false;
 };
@@ -370,9 +371,12 @@ std::vector<TauRow> tau_rows(const std::vector<uint32_t>& cnt_flat, const std::v
         w.tau = tau;
         for (double v : cs) {
             if (v >= tau) w.d++;
-            else if (v >= 2) {
-                w.r += v * (v - 1.0) / 2.0;
-                w.cells += v;
+            else {
+                w.sq += v * v;
+                if (v >= 2) {
+                    w.r += v * (v - 1.0) / 2.0;
+                    w.cells += v;
+                }
             }
         }
         w.kb = (double)(kp + up(w.d, 128));
@@ -433,6 +437,26 @@ void tau_features(const std::vector<TauRow>& rows, const std::vector<uint32_t>& 
     }
 }
 
+// A database that serves new profiles (ENC_QUERY): tau minimising the time of
+// one new profile against all n rows -- the contraction over n rows of kb
+// bytes, plus the rare counts, sum over its loci of the group size it hits
+// (expected sum of c^2 / n over the alleles that are not frequent).
+int choose_tau_query(const std::vector<TauRow>& rows, int n, const TauModel& m, bool verbose) {
+    int best = 0;
+    double best_t = 1e300;
+    for (const TauRow& w : rows) {
+        const double t = (double)n * w.kb / m.gemm_rate + w.sq / std::max(n, 1) / m.dense_rate;
+        if (verbose)
+            fprintf(stderr, "  tau=%5d  one-hot=%8zu  rare items per query %.0f  est %.3f us per query%s\n", w.tau, w.d,
+                    w.sq / std::max(n, 1), t * 1e6, w.fits ? "" : "  (does not fit)");
+        if (w.fits && t < best_t) {
+            best = w.tau;
+            best_t = t;
+        }
+    }
+    return best;
+}
+
 // tau <= 0: the learned model's pick when one is set, else the analytic one.
 int choose_tau_gb300(int device, const std::vector<uint32_t>& cnt_flat, const std::vector<uint64_t>& off, int n,
                      int L, size_t free_bytes, const TauModel& m, bool dense, bool verbose) {
@@ -462,6 +486,19 @@ int choose_tau_gb300(int device, const std::vector<uint32_t>& cnt_flat, const st
             fprintf(stderr, "\n");
         }
         fprintf(stderr, "  tau: analytic %d, learned %d\n", analytic, learned);
+    }
+    // the analytic model is the fallback: a learned pick it rates more than 1.5x
+    // slower than its own is outside what the network was trained on
+    if (learned && analytic) {
+        double t_l = 0, t_a = 0;
+        for (const TauRow& r : rows) {
+            if (r.tau == learned) t_l = r.t;
+            if (r.tau == analytic) t_a = r.t;
+        }
+        if (t_l > 1.5 * t_a) {
+            if (verbose) fprintf(stderr, "  learned pick %d rated %.1fx the analytic one: analytic\n", learned, t_l / t_a);
+            learned = 0;
+        }
     }
     return learned ? learned : analytic;
 }
@@ -587,7 +624,8 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
             goto done;
         }
         if (tau <= 0) {
-            tau = choose_tau_gb300(device, cnt_h, off_h, n, L, freeb, model, dense_rare, verbose);
+            tau = query_maps ? choose_tau_query(tau_rows(cnt_h, off_h, n, L, freeb, model, true), n, model, verbose)
+                             : choose_tau_gb300(device, cnt_h, off_h, n, L, freeb, model, dense_rare, verbose);
             if (!tau) { e.set("no tau fits in %.2f GB of free device memory", freeb / 1e9); goto fail; }
         }
         out->tau = tau;

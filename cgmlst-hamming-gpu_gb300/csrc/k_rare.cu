@@ -24,11 +24,14 @@
 namespace tch {
 namespace {
 
-constexpr int RD_THREADS = 1024;
 constexpr int RD_WORDS = 32768;          // u32 counter words in shared memory (128 KB)
 constexpr int RD_COLS = 2 * RD_WORDS;    // columns per pass
-constexpr int RD_LOCI = 2 * RD_THREADS;  // loci laid out per scan
-constexpr int RD_SMEM = RD_WORDS * 4 + (RD_LOCI + 1) * 4 + RD_LOCI * 4 + 32 * 4;
+
+// Counter words a launch needs (a narrow stripe takes less shared memory, so
+// more CTAs fit on an SM when several solves run side by side).
+inline int counter_words(size_t width) { return (int)std::min<size_t>(RD_WORDS, width / 2); }
+template <int T>
+inline int rd_smem(int cwords) { return cwords * 4 + (2 * T + 1) * 4 + 2 * T * 4 + 32 * 4; }
 constexpr unsigned FULL = 0xFFFFFFFFu;
 
 __device__ __forceinline__ uint64_t lower_bound_m(const uint32_t* __restrict__ m, uint64_t lo, uint64_t hi,
@@ -84,11 +87,12 @@ __device__ __forceinline__ void count_col(uint32_t* cnt, uint32_t c) {
 // members[lo1]) end to end with every other thread's by a block-wide scan, cuts
 // the total into one equal part per warp and counts every partner j at column
 // j - wb.  Called by all threads of the CTA (it synchronises them).
+template <int T>
 __device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_t* run, uint32_t* wsum, uint32_t l0,
                                            uint32_t lo0, uint32_t l1, uint32_t lo1,
                                            const uint32_t* __restrict__ members, int wb) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr int NWARPS = RD_THREADS / 32;
+    constexpr int NWARPS = T / 32, LOCI = 2 * T;
     const uint32_t mine = l0 + l1;
     uint32_t inc = mine;
 #pragma unroll
@@ -99,15 +103,15 @@ __device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_
     if (lane == 31) wsum[warp] = inc;
     __syncthreads();  // also orders the counter zeroing and the previous chunk's readers
     if (warp == 0) {
-        const uint32_t v = wsum[lane];
+        const uint32_t v = lane < NWARPS ? wsum[lane] : 0u;
         uint32_t x = v;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
             const uint32_t t = __shfl_up_sync(FULL, x, d);
             if (lane >= d) x += t;
         }
-        wsum[lane] = x - v;
-        if (lane == 31) pre[RD_LOCI] = x;
+        if (lane < NWARPS) wsum[lane] = x - v;
+        if (lane == 31) pre[LOCI] = x;
     }
     __syncthreads();
     const uint32_t ex = wsum[warp] + inc - mine;
@@ -116,14 +120,14 @@ __device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_
     run[2 * tid] = lo0;
     run[2 * tid + 1] = lo1;
     __syncthreads();
-    const uint32_t total = pre[RD_LOCI];
+    const uint32_t total = pre[LOCI];
     // warp w takes the items [w * part, (w + 1) * part) and walks them run
     // by run, its 32 lanes on consecutive members of a run
     const uint32_t part = (total + NWARPS - 1) / NWARPS;
     uint32_t e = min(total, (uint32_t)warp * part);
     const uint32_t e_end = min(total, e + part);
     if (e < e_end) {
-        int lo = 0, hi = RD_LOCI;  // the run holding item e: the last p with pre[p] <= e
+        int lo = 0, hi = LOCI;  // the run holding item e: the last p with pre[p] <= e
         while (hi - lo > 1) {
             const int m = (lo + hi) >> 1;
             if (pre[m] <= e) lo = m; else hi = m;
@@ -155,19 +159,21 @@ __device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_
     }
 }
 
-__global__ void __launch_bounds__(RD_THREADS, 1)
-    rare_dense_kernel(const RareGroups g, int r0, int rows, uint16_t* __restrict__ R, size_t ldr, int cend) {
+template <int T>
+__global__ void __launch_bounds__(T, 1024 / T)
+    rare_dense_kernel(const RareGroups g, int r0, int rows, uint16_t* __restrict__ R, size_t ldr, int cend,
+                      int cwords) {
     extern __shared__ uint4 smem_rd[];
     uint32_t* cnt = reinterpret_cast<uint32_t*>(smem_rd);
-    uint32_t* pre = cnt + RD_WORDS;        // RD_LOCI + 1: exclusive prefix of the run lengths
-    uint32_t* run = pre + RD_LOCI + 1;     // RD_LOCI: first member index of each run
-    uint32_t* wsum = run + RD_LOCI;        // 32: per-warp totals of the scan
+    uint32_t* pre = cnt + cwords;          // 2T + 1: exclusive prefix of the run lengths
+    uint32_t* run = pre + (2 * T) + 1;     // 2T: first member index of each run
+    uint32_t* wsum = run + (2 * T);        // 32: per-warp totals of the scan
     const int tid = threadIdx.x;
     const int n = g.n, L = g.L;
-    // with every locus in one scan (L <= RD_LOCI) a thread keeps the same two
+    // with every locus in one scan (L <= 2T) a thread keeps the same two
     // loci for all rows: their count offsets stay in registers and the next
     // row's ranks and positions are fetched while this row is counted
-    const bool one_chunk = L <= RD_LOCI;
+    const bool one_chunk = L <= (2 * T);
     uint64_t co0 = 0, co1 = 0;
     if (one_chunk) {
         if (2 * tid < L) co0 = g.cnt_off[2 * tid];
@@ -181,12 +187,12 @@ __global__ void __launch_bounds__(RD_THREADS, 1)
         if (one_chunk && r + (int)gridDim.x < rows) next = load_cells(g, i + (int)gridDim.x, 2 * tid);
         const int cbeg = r0 + (r & ~(kRareDenseAlign - 1));  // first column of the row's diagonal tile
         uint4* Rrow = reinterpret_cast<uint4*>(R + (size_t)r * ldr + (size_t)(cbeg - r0));
-        for (int wb = cbeg; wb < cend; wb += RD_COLS) {
-            const int we = min(cend, wb + RD_COLS);
+        for (int wb = cbeg; wb < cend; wb += 2 * cwords) {
+            const int we = min(cend, wb + 2 * cwords);
             const int nq = (we - wb) >> 3;  // uint4 of counters (8 columns each); we - wb is a multiple of 256
-            for (int w = tid; w < nq; w += RD_THREADS) smem_rd[w] = make_uint4(0, 0, 0, 0);
+            for (int w = tid; w < nq; w += T) smem_rd[w] = make_uint4(0, 0, 0, 0);
             const uint32_t jlo = (uint32_t)max(wb, i + 1), jhi = (uint32_t)min(we, n);
-            for (int kc = 0; jlo < jhi && kc < L; kc += RD_LOCI) {
+            for (int kc = 0; jlo < jhi && kc < L; kc += (2 * T)) {
                 // this thread's two loci, then a block-wide exclusive scan of the run lengths
                 const int k0 = kc + 2 * tid;
                 uint32_t lo0 = 0, lo1 = 0, l0 = 0, l1 = 0;
@@ -198,11 +204,11 @@ __global__ void __launch_bounds__(RD_THREADS, 1)
                     if (k0 < L) l0 = partner_run(g, i, c.a0, c.m0, g.cnt_off[k0], jlo, jhi, &lo0);
                     if (k0 + 1 < L) l1 = partner_run(g, i, c.a1, c.m1, g.cnt_off[k0 + 1], jlo, jhi, &lo1);
                 }
-                count_runs(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, wb);
+                count_runs<T>(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, wb);
             }
             __syncthreads();
             uint4* dst = Rrow + ((wb - cbeg) >> 3);
-            for (int w = tid; w < nq; w += RD_THREADS) dst[w] = smem_rd[w];
+            for (int w = tid; w < nq; w += T) dst[w] = smem_rd[w];
             __syncthreads();
         }
     }
@@ -226,33 +232,34 @@ __device__ __forceinline__ uint32_t group_run(const RareGroups& g, uint32_t a, u
 // Rare counts of m new profiles against every row of the set:
 // R[r * ldr + j] = loci where new profile r and row j share an allele that is
 // rare in the set, for j < n (0 up to cend).  Same counting as rare_dense_kernel.
-__global__ void __launch_bounds__(RD_THREADS, 1)
+template <int T>
+__global__ void __launch_bounds__(T, 1024 / T)
     rare_query_kernel(const RareGroups g, const uint32_t* __restrict__ xq, int m, uint16_t* __restrict__ R,
-                      size_t ldr, int cend) {
+                      size_t ldr, int cend, int cwords) {
     extern __shared__ uint4 smem_rd[];
     uint32_t* cnt = reinterpret_cast<uint32_t*>(smem_rd);
-    uint32_t* pre = cnt + RD_WORDS;
-    uint32_t* run = pre + RD_LOCI + 1;
-    uint32_t* wsum = run + RD_LOCI;
+    uint32_t* pre = cnt + cwords;
+    uint32_t* run = pre + (2 * T) + 1;
+    uint32_t* wsum = run + (2 * T);
     const int tid = threadIdx.x;
     const int n = g.n, L = g.L;
     for (int r = blockIdx.x; r < m; r += gridDim.x) {
         uint4* Rrow = reinterpret_cast<uint4*>(R + (size_t)r * ldr);
-        for (int wb = 0; wb < cend; wb += RD_COLS) {
-            const int we = min(cend, wb + RD_COLS);
+        for (int wb = 0; wb < cend; wb += 2 * cwords) {
+            const int we = min(cend, wb + 2 * cwords);
             const int nq = (we - wb) >> 3;
-            for (int w = tid; w < nq; w += RD_THREADS) smem_rd[w] = make_uint4(0, 0, 0, 0);
+            for (int w = tid; w < nq; w += T) smem_rd[w] = make_uint4(0, 0, 0, 0);
             const uint32_t jlo = (uint32_t)wb, jhi = (uint32_t)min(we, n);
-            for (int kc = 0; jlo < jhi && kc < L; kc += RD_LOCI) {
+            for (int kc = 0; jlo < jhi && kc < L; kc += (2 * T)) {
                 const int k0 = kc + 2 * tid;
                 uint32_t lo0 = 0, lo1 = 0, l0 = 0, l1 = 0;
                 if (k0 < L) l0 = group_run(g, xq[(size_t)r * L + k0], g.cnt_off[k0], jlo, jhi, &lo0);
                 if (k0 + 1 < L) l1 = group_run(g, xq[(size_t)r * L + k0 + 1], g.cnt_off[k0 + 1], jlo, jhi, &lo1);
-                count_runs(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, wb);
+                count_runs<T>(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, wb);
             }
             __syncthreads();
             uint4* dst = Rrow + (wb >> 3);
-            for (int w = tid; w < nq; w += RD_THREADS) dst[w] = smem_rd[w];
+            for (int w = tid; w < nq; w += T) dst[w] = smem_rd[w];
             __syncthreads();
         }
     }
@@ -265,15 +272,27 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
     if (rows <= 0) return cudaSuccess;
     const size_t width = up((size_t)(g.n - r0), kRareDenseAlign);
     if (ldr < width || (ldr & 7) || ((uintptr_t)R & 15)) return cudaErrorInvalidValue;
-    const int smem = RD_SMEM;
     static bool attr = false;  // once per process (also keeps it out of graph captures)
     if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(rare_dense_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaError_t e = cudaFuncSetAttribute(rare_dense_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             rd_smem<1024>(RD_WORDS));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(rare_dense_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     rd_smem<256>(RD_WORDS));
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    const int grid = std::max(1, std::min(rows, sms));
-    rare_dense_kernel<<<grid, RD_THREADS, smem, st>>>(g, r0, rows, R, ldr, r0 + (int)width);
+    const int cwords = counter_words(width);
+    // a small stripe (few rows, narrow) takes CTAs of 256 threads: four fit on an SM,
+    // so solves that run side by side share the SMs
+    if (rows < 2 * sms && width <= 8192) {
+        rare_dense_kernel<256><<<std::max(1, rows), 256, rd_smem<256>(cwords), st>>>(g, r0, rows, R, ldr,
+                                                                                   r0 + (int)width, cwords);
+    } else {
+        const int grid = std::max(1, std::min(rows, sms));
+        rare_dense_kernel<1024><<<grid, 1024, rd_smem<1024>(cwords), st>>>(g, r0, rows, R, ldr, r0 + (int)width,
+                                                                            cwords);
+    }
     return cudaGetLastError();
 }
 
@@ -288,11 +307,15 @@ cudaError_t launch_rare_query(const RareGroups& g, const uint32_t* xq, int m, ui
     if (ldr < width || (ldr & 7) || ((uintptr_t)R & 15)) return cudaErrorInvalidValue;
     static bool attr = false;
     if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(rare_query_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, RD_SMEM);
+        const cudaError_t e = cudaFuncSetAttribute(rare_query_kernel<1024>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   rd_smem<1024>(RD_WORDS));
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    rare_query_kernel<<<std::max(1, std::min(m, sms)), RD_THREADS, RD_SMEM, st>>>(g, xq, m, R, ldr, (int)width);
+    const int cwords = counter_words(width);
+    rare_query_kernel<1024><<<std::max(1, std::min(m, sms)), 1024, rd_smem<1024>(cwords), st>>>(g, xq, m, R, ldr,
+                                                                                               (int)width, cwords);
     return cudaGetLastError();
 }
 

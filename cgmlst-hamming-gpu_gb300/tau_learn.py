@@ -6,10 +6,10 @@
 (run from this directory, or ``python cgmlst-hamming-gpu_gb300/tau_learn.py``).
 
 sweep: seeded synthetic profile sets of varied shape (n log-uniform in
-[50, 63 005], L from the shapes the configs name, n x L <= 7.2e7; three in
-four Zipf (s in [1.0, 1.4], lognormal distinct-allele counts, 5 % 64-bit ids),
-one in four founder models (3-60 alleles per locus, 0.2-5 % mutations to new
-ids); 0-8 % missing).  For each set
+[50, 63 005], L from the shapes the configs name, n x L <= 7.2e7): 60 % Zipf
+(s in [1.0, 1.4], lognormal distinct-allele counts, 5 % 64-bit ids), 20 %
+founder models (3-60 alleles per locus, 0.2-5 % mutations to new ids), 20 % the
+batched config's law (n <= 5 000); 0-8 % missing.  For each set
 the library's own feature rows (tch_tau_features) and, for each candidate tau
 near the analytic pick, the measured device time of one whole-triangle solve
 (rare counts + tile pass, CUDA events, median of 3).
@@ -42,8 +42,7 @@ LOCI = (500, 1142, 1343, 2000, 2794, 3016)
 
 
 def dataset_params(seed: int) -> dict:
-    """Shape and allele law of profile set `seed`: one in four is a founder
-    model (few alleles per locus, rare mutations), the rest Zipf."""
+    """Shape and allele law of profile set `seed`."""
     rng = np.random.default_rng(1000 + seed)
     n = int(np.exp(rng.uniform(np.log(50), np.log(63005))))
     L = int(rng.choice(LOCI))
@@ -52,7 +51,10 @@ def dataset_params(seed: int) -> dict:
         if n * L > 7.2e7:
             n = int(7.2e7 / L)
     p = dict(seed=seed, n=n, L=L, miss=float(rng.uniform(0.0, 0.08)))
-    if rng.random() < 0.25:
+    kind = rng.random()
+    if kind < 0.2:  # the batched config's law: Zipf over lognormal(40) distinct ids, n up to 5 000
+        p.update(kind="batch", n=min(n, 5000), L=int(rng.choice(LOCI[1:])), s=float(rng.uniform(1.0, 1.4)))
+    elif kind < 0.4:
         p.update(kind="founders", founders=int(rng.integers(3, 60)), mut=float(np.exp(rng.uniform(np.log(0.002),
                                                                                                  np.log(0.05)))))
     else:
@@ -62,6 +64,14 @@ def dataset_params(seed: int) -> dict:
 
 
 def make_dataset(p: dict) -> np.ndarray:
+    if p.get("kind") == "batch":
+        rng = np.random.default_rng(p["seed"])
+        n, L = p["n"], p["L"]
+        k = np.clip(np.rint(rng.lognormal(np.log(40.0), 1.0, L)), 2, 500).astype(np.int64)
+        a = (rng.zipf(max(p["s"], 1.01), size=(n, L)) - 1) % k[None, :]
+        A = (np.arange(L, dtype=np.uint64)[None, :] << np.uint64(20)) + a.astype(np.uint64) + np.uint64(1)
+        A[rng.random((n, L)) < p["miss"]] = 0
+        return A
     if p.get("kind") == "founders":
         rng = np.random.default_rng(p["seed"])
         n, L = p["n"], p["L"]
