@@ -31,7 +31,7 @@ constexpr int RD_COLS = 2 * RD_WORDS;    // columns per pass
 // more CTAs fit on an SM when several solves run side by side).
 inline int counter_words(size_t width) { return (int)std::min<size_t>(RD_WORDS, width / 2); }
 template <int T>
-inline int rd_smem(int cwords) { return cwords * 4 + (2 * T + 1) * 4 + 2 * T * 4 + 32 * 4; }
+inline int rd_smem(int cwords) { return cwords * 4 + (2 * T + 1) * 4 + 2 * T * 4 + 64 * 4; }
 constexpr unsigned FULL = 0xFFFFFFFFu;
 
 __device__ __forceinline__ uint64_t lower_bound_m(const uint32_t* __restrict__ m, uint64_t lo, uint64_t hi,
@@ -79,63 +79,87 @@ __device__ __forceinline__ CellPair load_cells(const RareGroups& g, int i, int k
     return c;
 }
 
+// A part whose runs hold this many items on average is walked run by run
+// (measured on the long-tail profiles: 256 beats 0, 64, 1024 and never).
+constexpr uint32_t kWalkMin = 256;
+
 __device__ __forceinline__ void count_col(uint32_t* cnt, uint32_t c) {
     atomicAdd(cnt + (c >> 1), 1u << ((c & 1u) * 16u));
 }
 
 // Lays this thread's two runs (l0 partners from members[lo0], l1 from
-// members[lo1]) end to end with every other thread's by a block-wide scan, cuts
-// the total into one equal part per warp and counts every partner j at column
-// j - wb.  Called by all threads of the CTA (it synchronises them).
+// members[lo1]) end to end with every other thread's non-empty runs (a block
+// scan of item and run counts compacts them), cuts the items into one equal
+// part per warp, and counts every partner j at column j - wb.  A part of long
+// runs (kWalkMin items or more on average) is walked run by run, the lanes on
+// consecutive members; otherwise 256 items at a time, lane l on items
+// e + l + 32 u, several short runs in one pass, each lane keeping its current
+// run (start, end, first member) in registers.  Called by all threads of the
+// CTA (it synchronises them).
 template <int T>
 __device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_t* run, uint32_t* wsum, uint32_t l0,
                                            uint32_t lo0, uint32_t l1, uint32_t lo1,
                                            const uint32_t* __restrict__ members, int wb) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr int NWARPS = T / 32, LOCI = 2 * T;
-    const uint32_t mine = l0 + l1;
-    uint32_t inc = mine;
+    constexpr int NWARPS = T / 32;
+    __shared__ uint32_t tot[2];  // items, runs
+    const uint32_t mi = l0 + l1, mc = (l0 ? 1u : 0u) + (l1 ? 1u : 0u);
+    uint32_t ii = mi, ic = mc;  // inclusive warp scans of items and runs
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t t = __shfl_up_sync(FULL, inc, d);
-        if (lane >= d) inc += t;
+        const uint32_t ti = __shfl_up_sync(FULL, ii, d), tc = __shfl_up_sync(FULL, ic, d);
+        if (lane >= d) ii += ti, ic += tc;
     }
-    if (lane == 31) wsum[warp] = inc;
+    if (lane == 31) wsum[warp] = ii, wsum[32 + warp] = ic;
     __syncthreads();  // also orders the counter zeroing and the previous chunk's readers
     if (warp == 0) {
-        const uint32_t v = lane < NWARPS ? wsum[lane] : 0u;
-        uint32_t x = v;
+        const uint32_t vi = lane < NWARPS ? wsum[lane] : 0u, vc = lane < NWARPS ? wsum[32 + lane] : 0u;
+        uint32_t xi = vi, xc = vc;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t t = __shfl_up_sync(FULL, x, d);
-            if (lane >= d) x += t;
+            const uint32_t ti = __shfl_up_sync(FULL, xi, d), tc = __shfl_up_sync(FULL, xc, d);
+            if (lane >= d) xi += ti, xc += tc;
         }
-        if (lane < NWARPS) wsum[lane] = x - v;
-        if (lane == 31) pre[LOCI] = x;
+        if (lane < NWARPS) wsum[lane] = xi - vi, wsum[32 + lane] = xc - vc;
+        if (lane == 31) tot[0] = xi, tot[1] = xc;
     }
     __syncthreads();
-    const uint32_t ex = wsum[warp] + inc - mine;
-    pre[2 * tid] = ex;
-    pre[2 * tid + 1] = ex + l0;
-    run[2 * tid] = lo0;
-    run[2 * tid + 1] = lo1;
+    {
+        const uint32_t ei = wsum[warp] + ii - mi;        // items before this thread's runs
+        uint32_t q = wsum[32 + warp] + ic - mc;          // their places among the non-empty runs
+        if (l0) pre[q] = ei, run[q] = lo0, q++;
+        if (l1) pre[q] = ei + l0, run[q] = lo1;
+        if (tid == 0) pre[tot[1]] = tot[0];
+    }
     __syncthreads();
-    const uint32_t total = pre[LOCI];
-    // warp w takes the items [w * part, (w + 1) * part) and walks them run
-    // by run, its 32 lanes on consecutive members of a run
+    const uint32_t total = tot[0];
+    const int nr = (int)tot[1];
     const uint32_t part = (total + NWARPS - 1) / NWARPS;
-    uint32_t e = min(total, (uint32_t)warp * part);
-    const uint32_t e_end = min(total, e + part);
-    if (e < e_end) {
-        int lo = 0, hi = LOCI;  // the run holding item e: the last p with pre[p] <= e
-        while (hi - lo > 1) {
-            const int m = (lo + hi) >> 1;
-            if (pre[m] <= e) lo = m; else hi = m;
+    const uint32_t e_begin = min(total, (uint32_t)warp * part), e_end = min(total, e_begin + part);
+    if (e_begin >= e_end) return;
+    int p = 0;  // the run holding e_begin: the last p with pre[p] <= e_begin
+    {
+        int hi = nr;
+        while (hi - p > 1) {
+            const int m = (p + hi) >> 1;
+            if (pre[m] <= e_begin) p = m; else hi = m;
         }
-        for (int p = lo; e < e_end; p++) {
-            const uint32_t stop = min(pre[p + 1], e_end);
-            if (stop <= e) continue;  // an empty run
-            const uint32_t* src = members + run[p] + (e - pre[p]);
+    }
+    // long runs on average: walk run by run, the lanes on consecutive members
+    // with no per-item bookkeeping
+    int pe = p;  // the run holding e_end - 1
+    {
+        int hi = nr;
+        while (hi - pe > 1) {
+            const int m = (pe + hi) >> 1;
+            if (pre[m] <= e_end - 1) pe = m; else hi = m;
+        }
+    }
+    if ((e_end - e_begin) >= kWalkMin * (uint32_t)(pe - p + 1)) {
+        uint32_t e = e_begin;
+        for (int q = p; e < e_end; q++) {
+            const uint32_t stop = min(pre[q + 1], e_end);
+            const uint32_t* src = members + run[q] + (e - pre[q]);
             const uint32_t c = stop - e;
             uint32_t k = (uint32_t)lane;
             for (; k + 224 < c; k += 256) {  // eight loads in flight per lane
@@ -156,6 +180,31 @@ __device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_
             for (; k < c; k += 32) count_col(cnt, __ldg(src + k) - (uint32_t)wb);
             e = stop;
         }
+        return;
+    }
+    uint32_t a = pre[p], b = pre[p + 1], r = run[p];  // this lane's current run
+    for (uint32_t e0 = e_begin; e0 < e_end; e0 += 256) {
+        uint32_t idx[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const uint32_t e = e0 + (uint32_t)(u * 32 + lane);
+            idx[u] = 0xFFFFFFFFu;
+            if (e < e_end) {
+                while (e >= b) {  // next run (pre[nr] = total > e bounds it)
+                    ++p;
+                    a = b;
+                    b = pre[p + 1];
+                    r = run[p];
+                }
+                idx[u] = r + (e - a);
+            }
+        }
+        uint32_t j[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) j[u] = idx[u] != 0xFFFFFFFFu ? __ldg(members + idx[u]) : 0u;
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (idx[u] != 0xFFFFFFFFu) count_col(cnt, j[u] - (uint32_t)wb);
     }
 }
 
@@ -167,7 +216,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
     uint32_t* cnt = reinterpret_cast<uint32_t*>(smem_rd);
     uint32_t* pre = cnt + cwords;          // 2T + 1: exclusive prefix of the run lengths
     uint32_t* run = pre + (2 * T) + 1;     // 2T: first member index of each run
-    uint32_t* wsum = run + (2 * T);        // 32: per-warp totals of the scan
+    uint32_t* wsum = run + (2 * T);        // 64: per-warp totals of the scans
     const int tid = threadIdx.x;
     const int n = g.n, L = g.L;
     // with every locus in one scan (L <= 2T) a thread keeps the same two
