@@ -263,6 +263,8 @@ def serving_bench(tch, synth, args, device):
             "query_rows": int(sizes.sum()), "slots": slots,
             "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
             "mean_ms": float(lat.mean() * 1e3), "max_ms": float(lat.max() * 1e3),
+            "slowest": [{"m": int(sizes[k]), "ms": float(lat[k] * 1e3), "queued_ms": float(queued[k] * 1e3),
+                         "submit_delay_ms": float(submit_delay[k] * 1e3)} for k in np.argsort(-lat)[:4]],
             "queued_p50_ms": float(np.percentile(queued, 50) * 1e3),
             "pairs": pairs, "pairs_per_s": pairs / makespan, "makespan_s": makespan,
             "note": "latency = arrival -> q x db and q x q distances in (page-locked, reused) host memory; "
