@@ -334,9 +334,12 @@ bool parse_allele(const std::string& s, size_t b, size_t e, bool skip_repl, cons
     return true;
 }
 
-bool valid_utf8(const std::string& s) {
-    size_t i = 0, n = s.size();
-    while (i < n) {
+// UTF-8 check of s[b, e): every sequence that starts there is complete and
+// well formed (it may read up to 3 bytes past e to finish one).
+bool valid_utf8_range(const std::string& s, size_t b, size_t e) {
+    size_t i = b;
+    const size_t n = s.size();
+    while (i < e) {
         const unsigned char c = (unsigned char)s[i];
         size_t len;
         uint32_t cp;
@@ -359,43 +362,93 @@ bool valid_utf8(const std::string& s) {
     return true;
 }
 
-bool read_all(const std::string& path, std::string& buf, std::string& err) {
+// The whole buffer, in parallel chunks; a chunk starts at a byte that begins a
+// sequence (continuation bytes at a chunk's start belong to the previous one).
+bool valid_utf8(const std::string& s, size_t threads) {
+    const size_t n = s.size(), parts = std::max<size_t>(1, std::min<size_t>(threads * 4, n / (1 << 20) + 1));
+    std::vector<size_t> cut(parts + 1, n);
+    cut[0] = 0;
+    for (size_t k = 1; k < parts; k++) {
+        size_t c = n * k / parts;
+        for (int back = 0; back < 3 && c > 0 && ((unsigned char)s[c] & 0xC0) == 0x80; back++) c--;
+        cut[k] = std::max(c, cut[k - 1]);
+    }
+    std::atomic<bool> ok{true};
+    parallel_for(threads, parts, 1, [&](size_t a, size_t b) {
+        for (size_t k = a; k < b; k++)
+            if (!valid_utf8_range(s, cut[k], cut[k + 1])) ok = false;
+    });
+    return ok;
+}
+
+bool read_all(const std::string& path, std::string& buf, std::string& err, size_t threads) {
     FILE* f = path == "-" ? stdin : fopen(path.c_str(), "rb");
     if (!f) {
         err = strerror(errno);
         return false;
     }
-    char tmp[1 << 16];
-    size_t r;
-    while ((r = fread(tmp, 1, sizeof tmp, f)) > 0) buf.append(tmp, r);
-    const bool bad = ferror(f);
+    bool bad = false;
+    if (f != stdin && fseek(f, 0, SEEK_END) == 0) {  // a regular file: one read of its size
+        const long size = ftell(f);
+        if (size >= 0 && fseek(f, 0, SEEK_SET) == 0) {
+            buf.resize((size_t)size);
+            if (size && fread(&buf[0], 1, (size_t)size, f) != (size_t)size) bad = true;
+            char extra;
+            if (!bad && fread(&extra, 1, 1, f) == 1) {  // grew meanwhile: read the rest
+                buf.push_back(extra);
+                char tmp[1 << 16];
+                size_t r;
+                while ((r = fread(tmp, 1, sizeof tmp, f)) > 0) buf.append(tmp, r);
+            }
+        } else {
+            bad = true;
+        }
+    } else {
+        char tmp[1 << 16];
+        size_t r;
+        while ((r = fread(tmp, 1, sizeof tmp, f)) > 0) buf.append(tmp, r);
+    }
+    bad = bad || ferror(f);
     if (f != stdin) fclose(f);
     if (bad) {
         err = "read error";
         return false;
     }
-    if (!valid_utf8(buf)) {
+    if (!valid_utf8(buf, threads)) {
         err = "stream did not contain valid UTF-8";
         return false;
     }
     return true;
 }
 
-// str::lines: (begin, end) of every line, '\n' and one '\r' before it removed.
-std::vector<std::pair<size_t, size_t>> rust_lines(const std::string& t) {
+// str::lines: (begin, end) of every line, '\n' and one '\r' before it removed;
+// the newlines are found in parallel chunks.
+std::vector<std::pair<size_t, size_t>> rust_lines(const std::string& t, size_t threads) {
+    const size_t n = t.size(), parts = std::max<size_t>(1, std::min<size_t>(threads * 4, n / (1 << 20) + 1));
+    std::vector<std::vector<size_t>> nl(parts);
+    parallel_for(threads, parts, 1, [&](size_t a, size_t b) {
+        for (size_t k = a; k < b; k++) {
+            const size_t lo = n * k / parts, hi = n * (k + 1) / parts;
+            const char* p = t.data() + lo;
+            const char* e = t.data() + hi;
+            while (p < e) {
+                const char* q = (const char*)memchr(p, '\n', (size_t)(e - p));
+                if (!q) break;
+                nl[k].push_back((size_t)(q - t.data()));
+                p = q + 1;
+            }
+        }
+    });
     std::vector<std::pair<size_t, size_t>> out;
     size_t b = 0;
-    while (b < t.size()) {
-        size_t nl = t.find('\n', b);
-        if (nl == std::string::npos) {
-            out.push_back({b, t.size()});
-            break;
+    for (auto& v : nl)
+        for (size_t q : v) {
+            size_t e = q;
+            if (e > b && t[e - 1] == '\r') e--;
+            out.push_back({b, e});
+            b = q + 1;
         }
-        size_t e = nl;
-        if (e > b && t[e - 1] == '\r') e--;
-        out.push_back({b, e});
-        b = nl + 1;
-    }
+    if (b < n) out.push_back({b, n});
     return out;
 }
 
@@ -500,8 +553,8 @@ int main(int argc, char** argv) {
     // ---- load (main.rs:286-311)
     double t = now();
     std::string text, rerr;
-    if (!read_all(args.input, text, rerr)) die(fmt("reading %s: %s", args.input.c_str(), rerr.c_str()));
-    auto lines = rust_lines(text);
+    if (!read_all(args.input, text, rerr, threads)) die(fmt("reading %s: %s", args.input.c_str(), rerr.c_str()));
+    auto lines = rust_lines(text, threads);
     if (lines.empty()) die("empty input");
     size_t L = 1;
     for (size_t p = lines[0].first; p < lines[0].second; p++) L += text[p] == sep;
