@@ -208,10 +208,6 @@ def serving_bench(tch, synth, args, device):
     sizes = np.minimum(2000, np.floor(np.exp(rng.uniform(0, np.log(2001), R)))).astype(int)
     arrivals = np.cumsum(rng.exponential(1 / 50.0, R))
     starts = rng.integers(0, pool_rows - 2000, R)
-    # warm the kernels and grow the stream-ordered pool to the largest batch
-    warm = tch.pinned_empty((2000, n_db))
-    db.query(pool[:2000], out=warm)
-    del warm
     slots = 4
     # results go to page-locked buffers, reused: a request waits for a free one
     # (that wait counts in its latency)
@@ -223,6 +219,11 @@ def serving_bench(tch, synth, args, device):
     for k in range(nbuf):
         free.put(k)
     sv = tch.Server(db, slots=slots)
+    # warm the kernels and grow the database's stream-ordered pool to `slots`
+    # concurrent batches of the largest size
+    warm = [sv.submit(pool[:2000], out=bufs[k][0], out_qq=bufs[k][1].reshape(2000, 2000)) for k in range(slots)]
+    for w in warm:
+        sv.wait(w)
     rids = [None] * R
     bslot = [None] * R
     submit_delay = np.zeros(R)
@@ -342,12 +343,16 @@ def main():
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--serve-db", type=int, default=200000)
     ap.add_argument("--serve-requests", type=int, default=100)
+    ap.add_argument("--serving-only", action="store_true", help="run the serving leg alone and print its JSON")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
     ws, rank, local = dist_env()
     tch = importlib.import_module(PKG)
     synth = importlib.import_module(PKG + ".synth")
+    if args.serving_only:  # a service runs in its own process
+        print(json.dumps(serving_bench(tch, synth, args, local)), flush=True)
+        return
 
     t0 = time.perf_counter()
     A = synth.longtail(n=args.n, L=args.L)
@@ -610,8 +615,14 @@ def main():
         if not args.no_batch:
             batched = batch_bench(tch, args, device)
             log("batched:", batched)
-        if not args.no_serving:
-            serving = serving_bench(tch, synth, args, device)
+        if not args.no_serving:  # in a process of its own, as a service would run
+            r = subprocess.run([sys.executable, os.path.abspath(__file__), "--serving-only",
+                                "--serve-db", str(args.serve_db), "--serve-requests", str(args.serve_requests)],
+                               capture_output=True, text=True, env=dict(os.environ, CUDA_VISIBLE_DEVICES=str(device)))
+            if r.returncode:
+                raise RuntimeError("serving leg failed: " + r.stderr[-2000:])
+            serving = json.loads(r.stdout.strip().splitlines()[-1])
+            serving["process"] = "separate (bench.py --serving-only)"
             log("serving:", serving)
 
     cpu = None

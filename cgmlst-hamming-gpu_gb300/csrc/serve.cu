@@ -219,6 +219,7 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
             if (ce != cudaSuccess) goto done;
         }
         if (qq) {
+            mark();
             const dim3 blk(QQ_T, QQ_T), grd((m + QQ_T - 1) / QQ_T, (m + QQ_T - 1) / QQ_T);
             qq_kernel<<<grd, blk, 0, st>>>(dq, m, L, qq, ldq);
             ce = cudaGetLastError();
@@ -239,7 +240,8 @@ done:
         const cudaError_t se = cudaStreamSynchronize(st);
         if (ce == cudaSuccess) ce = se;
         if (nev > 1) {
-            static const char* names[] = {"h2d", "rank+pack", "rare counts", "tile pass", "d2h + q x q", "", "", ""};
+            static const char* names[] = {"h2d", "rank+pack", "rare counts", "tile pass", "d2h", "q x q + d2h", "",
+                                          ""};
             fprintf(stderr, "tch query m=%d:", m);
             for (int k = 0; k + 1 < nev; k++) {
                 float ms = 0;
