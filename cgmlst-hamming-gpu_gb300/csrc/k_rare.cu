@@ -321,7 +321,8 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
     if (rows <= 0) return cudaSuccess;
     const size_t width = up((size_t)(g.n - r0), kRareDenseAlign);
     if (ldr < width || (ldr & 7) || ((uintptr_t)R & 15)) return cudaErrorInvalidValue;
-    static bool attr = false;  // once per process (also keeps it out of graph captures)
+    static bool attrs[kMaxDevices] = {};  // once per device (also keeps it out of graph captures)
+    bool& attr = attrs[current_device()];
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(rare_dense_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              rd_smem<1024>(RD_WORDS));
@@ -354,7 +355,8 @@ cudaError_t launch_rare_query(const RareGroups& g, const uint32_t* xq, int m, ui
     if (m <= 0) return cudaSuccess;
     const size_t width = up((size_t)std::max(g.n, 1), kRareDenseAlign);
     if (ldr < width || (ldr & 7) || ((uintptr_t)R & 15)) return cudaErrorInvalidValue;
-    static bool attr = false;
+    static bool attrs[kMaxDevices] = {};
+    bool& attr = attrs[current_device()];
     if (!attr) {
         const cudaError_t e = cudaFuncSetAttribute(rare_query_kernel<1024>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,

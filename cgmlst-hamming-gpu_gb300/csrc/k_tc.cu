@@ -489,8 +489,11 @@ KChunks chunks_of(const ByteOperands& ops) {
 template <int KIND, int CM>
 cudaError_t launch_kind(const ByteOperands& ops, const ByteOperands& bops, const RareCSR& rare, const StripeArgs& a,
                         int num_sms, cudaStream_t st) {
-    static bool attr = false;
-    static int max_clusters = 0;
+    static bool attrs[kMaxDevices] = {};
+    static int max_clusters_of[kMaxDevices] = {};
+    const int dev = current_device();
+    bool& attr = attrs[dev];
+    int& max_clusters = max_clusters_of[dev];
     auto kern = tc_stripe_kernel<KIND, CM>;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute lattr[1];

@@ -32,6 +32,14 @@ struct Err {
 
 inline size_t up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 
+// Per-device one-time set-up flags (kernel attributes are set per device).
+constexpr int kMaxDevices = 64;
+inline int current_device() {
+    int d = 0;
+    cudaGetDevice(&d);
+    return d >= 0 && d < kMaxDevices ? d : 0;
+}
+
 // Bits reported through the device error word.
 enum DevErr : int {
     DEVERR_RARE_PAIR = 1,  // a rare partner j outside (i, n)
