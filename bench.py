@@ -510,6 +510,19 @@ def main():
 
     # e2e through the C ABI with host buffers: tch_run (the reference's entry
     # point, host-encoded operands) and tch_run_calls (allele calls, device encoder)
+    # serving: in a process of its own, as a service would run, and before the
+    # legs that churn host memory (its large copies slow down after them)
+    serving = None
+    if rank == 0 and ws == 1 and not args.no_serving:
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--serving-only",
+                            "--serve-db", str(args.serve_db), "--serve-requests", str(args.serve_requests)],
+                           capture_output=True, text=True, env=dict(os.environ, CUDA_VISIBLE_DEVICES=str(device)))
+        if r.returncode:
+            raise RuntimeError("serving leg failed: " + r.stderr[-2000:])
+        serving = json.loads(r.stdout.strip().splitlines()[-1])
+        serving["process"] = "separate (bench.py --serving-only)"
+        log("serving:", serving)
+
     # learned vs analytic tau: whole-triangle device time at each pick and at
     # a sweep of taus around them (fresh solvers)
     tau_cmp = None
@@ -606,24 +619,13 @@ def main():
                        "2048 rows, copied to pinned host memory, handed to a callback (full layout, tab)"}
         log("tsv writer:", tsv)
 
-    serving = None
     batched = None
-    if rank == 0 and ws == 1 and not (args.no_serving and args.no_batch):
+    if rank == 0 and ws == 1 and not args.no_batch:
         solver.close()
         del out
         torch.cuda.empty_cache()
-        if not args.no_batch:
-            batched = batch_bench(tch, args, device)
-            log("batched:", batched)
-        if not args.no_serving:  # in a process of its own, as a service would run
-            r = subprocess.run([sys.executable, os.path.abspath(__file__), "--serving-only",
-                                "--serve-db", str(args.serve_db), "--serve-requests", str(args.serve_requests)],
-                               capture_output=True, text=True, env=dict(os.environ, CUDA_VISIBLE_DEVICES=str(device)))
-            if r.returncode:
-                raise RuntimeError("serving leg failed: " + r.stderr[-2000:])
-            serving = json.loads(r.stdout.strip().splitlines()[-1])
-            serving["process"] = "separate (bench.py --serving-only)"
-            log("serving:", serving)
+        batched = batch_bench(tch, args, device)
+        log("batched:", batched)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
