@@ -576,7 +576,7 @@ def main():
             dt_calls = time.perf_counter() - t
             if rc:
                 raise RuntimeError(err.value.decode())
-            if k > 0:  # the first round warms the context and the pinned stripe buffers
+            if k > 0:  # the first pass warms the context and the pinned stripe buffers
                 times.append(dt)
                 times_calls.append(dt_calls)
         os.environ.pop("TCH_VERBOSE", None)

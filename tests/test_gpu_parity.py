@@ -217,8 +217,9 @@ def test_device_stripe_api(tch):
 
 
 def test_k_chunked_operand(tch):
-    """The operand rows split along K into several allocations (spec K
-    tiling): same distances as one allocation, for both solver builds."""
+    """The operand rows split along K into several allocations (K tiling of
+    the one-hot matrix): same distances as one allocation, for both solver
+    builds."""
     rng = np.random.default_rng(17)
     n, L = 900, 300
     A = rng.integers(1, 60, size=(n, L)).astype(np.uint64)
