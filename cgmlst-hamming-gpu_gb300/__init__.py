@@ -138,7 +138,7 @@ def lib():
         L.tch_db_create.argtypes = [c_int, c_int, c_int, c_void, c_int, P(c_void), c_char_p, c_int]
         L.tch_db_create.restype = c_int
         L.tch_db_destroy.argtypes, L.tch_db_destroy.restype = [c_void], None
-        L.tch_db_info.argtypes = [c_void, P(c_int), P(c_int), P(c_int), P(c_size), P(c_size)]
+        L.tch_db_info.argtypes = [c_void, P(c_int), P(c_int), P(c_int), P(c_size), P(c_size), P(c_int)]
         L.tch_db_info.restype = c_int
         L.tch_db_query_bytes.argtypes, L.tch_db_query_bytes.restype = [c_void, c_int], c_size
         L.tch_host_alloc.argtypes, L.tch_host_alloc.restype = [c_size], c_void
@@ -568,11 +568,11 @@ class Database:
         self._h = h
 
     def info(self) -> dict:
-        n, L, tau = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        n, L, tau, kc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         d, b = ctypes.c_size_t(), ctypes.c_size_t()
         lib().tch_db_info(self._h, ctypes.byref(n), ctypes.byref(L), ctypes.byref(tau), ctypes.byref(d),
-                          ctypes.byref(b))
-        return dict(n=n.value, L=L.value, tau=tau.value, d_onehot=d.value, device_bytes=b.value)
+                          ctypes.byref(b), ctypes.byref(kc))
+        return dict(n=n.value, L=L.value, tau=tau.value, d_onehot=d.value, device_bytes=b.value, k_chunks=kc.value)
 
     def query_bytes(self, m: int) -> int:
         return lib().tch_db_query_bytes(self._h, m)

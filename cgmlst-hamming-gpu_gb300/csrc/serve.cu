@@ -359,7 +359,8 @@ int tch_db_create(int device, int n, int L, const uint64_t* calls, int tau, tch_
     TCH_CK(e, cudaMemcpy(d_calls, calls, (size_t)n * L * 8, cudaMemcpyHostToDevice));
     {
         TauModel model;
-        if (encode_on_device(device, n, L, d_calls, tau, model, false, 0, ENC_QUERY, &db->enc, e)) goto fail;
+        if (encode_on_device(device, n, L, d_calls, tau, model, false, max_chunk_bytes(), ENC_QUERY, &db->enc, e))
+            goto fail;
     }
     cudaFree(d_calls);
     // the database's own triangle is not served: drop its ranks and positions
@@ -397,8 +398,9 @@ void tch_db_destroy(tch_db* db) {
     delete db;
 }
 
-int tch_db_info(const tch_db* db, int* n, int* L, int* tau, size_t* d_onehot, size_t* device_bytes) {
+int tch_db_info(const tch_db* db, int* n, int* L, int* tau, size_t* d_onehot, size_t* device_bytes, int* k_chunks) {
     if (!db) return 1;
+    if (k_chunks) *k_chunks = db->enc.X.n;
     if (n) *n = db->n;
     if (L) *L = db->L;
     if (tau) *tau = db->enc.tau;

@@ -233,7 +233,9 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
                      TauTable* table = nullptr);
 void free_device_encoding(DeviceEncoding* d);
 
-// ---- tch_solver.cu (used by the batch runner) -----------------------------------------
+// ---- tch_solver.cu (used by the batch runner and the database) ------------------------
+// Largest single allocation of operand rows (tch_set_max_chunk_bytes; 0 = one).
+size_t max_chunk_bytes();
 int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, bool verbose,
                       tch_solver** out, Err& e);
 int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e,

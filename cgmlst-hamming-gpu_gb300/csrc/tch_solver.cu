@@ -45,7 +45,7 @@ static int g_kernel = -1;  // process default, resolved lazily
 // Set by tch_set_max_chunk_bytes or TCH_MAX_CHUNK_BYTES.
 static long long g_max_chunk = -1;
 
-static size_t max_chunk_bytes() {
+size_t max_chunk_bytes() {
     if (g_max_chunk < 0) {
         const char* v = getenv("TCH_MAX_CHUNK_BYTES");
         g_max_chunk = v ? atoll(v) : 0;

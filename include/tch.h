@@ -220,7 +220,7 @@ int tch_set_tau_mlp(const float* w);
 typedef struct tch_db tch_db;
 int tch_db_create(int device, int n, int L, const uint64_t* calls, int tau, tch_db** out, char* err, int errlen);
 void tch_db_destroy(tch_db* db);
-int tch_db_info(const tch_db* db, int* n, int* L, int* tau, size_t* d_onehot, size_t* device_bytes);
+int tch_db_info(const tch_db* db, int* n, int* L, int* tau, size_t* d_onehot, size_t* device_bytes, int* k_chunks);
 /* Device bytes a query batch of m profiles takes while it runs. */
 size_t tch_db_query_bytes(const tch_db* db, int m);
 int tch_db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* qdb, uint16_t* qq, void* stream, char* err,

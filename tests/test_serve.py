@@ -122,3 +122,18 @@ def test_query_errors(tch):
     with tch.Database(A[:200]) as db:
         with pytest.raises(tch.TchError):
             db.query(A[200:, :40])  # wrong locus count
+
+
+def test_query_against_k_chunked_database(tch):
+    """A database whose operand rows are split along K into several
+    allocations: the new profiles' rows follow the same split."""
+    A = profiles(600, 300, seed=9, alleles=120)
+    try:
+        tch.set_max_chunk_bytes(1024 * 512)  # rows padded to 512 -> chunks of 1 KB of K
+        with tch.Database(A[:500], tau=8) as db:
+            assert db.info()["k_chunks"] > 1
+            qdb, qq = db.query(A[500:])
+    finally:
+        tch.set_max_chunk_bytes(0)
+    exp_qdb, exp_qq = expected(A[:500], A[500:])
+    check(qdb, qq, exp_qdb, exp_qq)
