@@ -183,6 +183,30 @@ def time_whole(tch, A, tau, device, out, ldo, stream, reps=3):
     return statistics.median(ms), used
 
 
+def host_link(device, mib=512, reps=3):
+    """Page-locked copy rates (GB/s) of the host link at this moment: the e2e
+    and serving figures move with it (other jobs on the host share it)."""
+    import torch
+
+    h = torch.empty(mib << 20, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(mib << 20, dtype=torch.uint8, device=f"cuda:{device}")
+    st = torch.cuda.Stream(device=device)
+    res = {}
+    with torch.cuda.stream(st):
+        for name, dst, src in (("d2h", h, d), ("h2d", d, h)):
+            dst.copy_(src, non_blocking=True)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                dst.copy_(src, non_blocking=True)
+            e1.record(st)
+            st.synchronize()
+            res[name + "_gbs"] = round(reps * h.numel() / (e0.elapsed_time(e1) * 1e-3) / 1e9, 1)
+    del h, d
+    return res
+
+
 def serving_bench(tch, synth, args, device):
     """Resident database of n_db profiles x 1 142 loci (Zipf s = 1.2, 3 %
     missing), Poisson query arrivals (mean 50/s) of batches log-uniform in
@@ -242,6 +266,7 @@ def serving_bench(tch, synth, args, device):
                                 out_qq=bufs[j][1][:m * m].reshape(m, m))
             submit_delay[k] = time.perf_counter() - t
 
+    link_before = host_link(device)
     th = threading.Thread(target=submitter)
     th.start()
     lat = np.zeros(R)
@@ -255,6 +280,7 @@ def serving_bench(tch, synth, args, device):
         queued[k] = q_s
     th.join()
     makespan = time.perf_counter() - tb
+    link_after = host_link(device)
     sv.close()
     db.close()
     pairs = int(sum(m * n_db + m * (m - 1) // 2 for m in sizes))
@@ -268,6 +294,7 @@ def serving_bench(tch, synth, args, device):
                          "submit_delay_ms": float(submit_delay[k] * 1e3)} for k in np.argsort(-lat)[:4]],
             "queued_p50_ms": float(np.percentile(queued, 50) * 1e3),
             "pairs": pairs, "pairs_per_s": pairs / makespan, "makespan_s": makespan,
+            "host_link_gbs": {"before": link_before, "after": link_after},
             "note": "latency = arrival -> q x db and q x q distances in (page-locked, reused) host memory; "
                     f"generation {gen_s:.1f} s outside the timed region"}
 
@@ -330,7 +357,7 @@ def main():
     ap.add_argument("--kernel", default="tc_f8")
     ap.add_argument("--tau", type=int, default=0, help="0 = the analytic GB300 model's choice")
     ap.add_argument("--stripe", type=int, default=4096, help="rows per stripe of the e2e tch_run call")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5, help="timed e2e passes; the median is reported")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--n", type=int, default=63005)
     ap.add_argument("--L", type=int, default=1142)
@@ -557,6 +584,7 @@ def main():
             pass
 
         cb = tch.CB(nop)
+        link_before = host_link(device)
         times, times_calls = [], []
         for k in range(args.e2e_steps + 1):
             secs = ctypes.c_double(0)
@@ -580,14 +608,17 @@ def main():
                 times.append(dt)
                 times_calls.append(dt_calls)
         os.environ.pop("TCH_VERBOSE", None)
+        link = {"before": link_before, "after": host_link(device)}
         e2e_s = statistics.median(times)
         e2e = {"value": pairs_total / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_s, "tau": tau_host,
+               "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_s, "tau": tau_host, "host_link_gbs": link,
+               "samples_s": [round(t, 5) for t in times],
                "path": f"tch_run (the reference's C ABI): host O/P bits + rare CSR uploaded, stripes of "
                        f"{args.stripe} rows copied back, no-op callback"}
         ec = statistics.median(times_calls)
         e2e_calls = {"value": pairs_total / ec, "unit": UNIT, "h2d_bytes_per_step": int(A.nbytes),
-                     "d2h_bytes_per_step": int(d2h), "seconds_per_step": ec, "tau": int(tu.value),
+                     "d2h_bytes_per_step": int(d2h), "seconds_per_step": ec, "tau": int(tu.value), "host_link_gbs": link,
+                     "samples_s": [round(t, 5) for t in times_calls],
                      "path": "tch_run_calls: allele calls uploaded, device encoder, same stripes and copy-back"}
 
     # the reference's TSV writer (main.rs:224-265) on the GPU: the full matrix

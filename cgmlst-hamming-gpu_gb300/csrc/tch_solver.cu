@@ -22,7 +22,9 @@
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "tch_internal.cuh"
@@ -623,6 +625,106 @@ static cudaError_t upload_u32(uint32_t* dst, const uint32_t* src, size_t count, 
     return cudaGetLastError();
 }
 
+// Row ranges whose partner lists are uploaded, checked and computed as one
+// unit: the first stripe in sub-stripes of a quarter (multiples of 128 rows,
+// so every sub-stripe's output starts 16-byte aligned), so that its tile pass
+// starts after the first quarter's lists rather than the whole stripe's;
+// every later stripe whole (its lists arrive while earlier stripes compute).
+struct RowChunk {
+    int r0, rows;
+};
+
+static std::vector<RowChunk> row_chunks(int n, int S) {
+    std::vector<RowChunk> c;
+    const int first = std::min(S, n);
+    const int sub = S >= 1024 ? (int)up((size_t)S / 4, 128) : std::max(first, 1);
+    for (int a = 0; a < first; a += sub) c.push_back({a, std::min(sub, first - a)});
+    for (int r0 = S; r0 < n; r0 += S) c.push_back({r0, std::min(S, n - r0)});
+    return c;
+}
+
+// Uploads every chunk's partner lists ahead of the pipeline, in row order, on
+// a stream of its own, from a helper thread.  The device holds the whole
+// partner array, so the copies reuse no buffer and only wait for the link; a
+// copy from pageable host memory returns only once it has finished, so issued
+// from the pipeline's own thread it would hold back the next stripe's launch
+// and the previous stripe's callback.  A stripe stream waits for its chunks'
+// events.
+struct ListUploader {
+    std::thread th;
+    std::mutex mu;
+    std::condition_variable cv;
+    int issued = 0;  // stripes whose copy is issued and whose event is recorded
+    cudaError_t err = cudaSuccess;
+    bool stop = false;
+    cudaStream_t st = nullptr;
+    std::vector<cudaEvent_t> ev;
+    double seconds = 0;  // from the first copy issued to the last one returned
+
+    cudaError_t start(const tch_solver* s, const std::vector<RowChunk>& chunks, bool pull);
+
+    // chunk k's event once its copy is issued, or the uploader's error
+    cudaError_t ready(int k, cudaEvent_t* out) {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [&] { return issued > k || err != cudaSuccess; });
+        if (issued > k) {
+            *out = ev[k];
+            return cudaSuccess;
+        }
+        return err;
+    }
+
+    ~ListUploader() {
+        if (th.joinable()) {
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                stop = true;
+            }
+            th.join();
+        }
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+    }
+};
+
+cudaError_t ListUploader::start(const tch_solver* s, const std::vector<RowChunk>& chunks, bool pull) {
+    const int ns = (int)chunks.size();
+    cudaError_t ce = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) return ce;
+    ev.assign(ns, nullptr);
+    for (cudaEvent_t& x : ev)
+        if ((ce = cudaEventCreateWithFlags(&x, cudaEventDisableTiming)) != cudaSuccess) return ce;
+    th = std::thread([this, s, chunks, ns, pull] {
+        const auto t0 = std::chrono::steady_clock::now();
+        cudaError_t ce = cudaSetDevice(s->device);
+        for (int k = 0; k < ns && ce == cudaSuccess; k++) {
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                if (stop) return;
+            }
+            const size_t pa = s->defer_start[chunks[k].r0], pb = s->defer_start[chunks[k].r0 + chunks[k].rows];
+            ce = upload_u32(s->dJs + pa, s->defer_js + pa, pb - pa, pull, s->num_sms, st);
+            if (ce == cudaSuccess) ce = cudaEventRecord(ev[k], st);
+            if (ce == cudaSuccess) {
+                std::lock_guard<std::mutex> lk(mu);
+                issued = k + 1;
+                seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+                cv.notify_all();
+            }
+        }
+        if (ce != cudaSuccess) {
+            std::lock_guard<std::mutex> lk(mu);
+            err = ce;
+            cv.notify_all();
+        }
+    });
+    return cudaSuccess;
+}
+
 static double wall() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -638,9 +740,12 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
     uint16_t* dU[2] = {nullptr, nullptr};
     uint16_t* hU[2] = {nullptr, nullptr};
     bool pooled = false;
-    int* dflags = nullptr;  // per stripe: its partner lists are not ascending (1) / invalid (2)
+    int* dflags = nullptr;  // per row chunk: its partner lists are not ascending (1) / invalid (2)
     std::vector<int> hflags;
+    std::vector<RowChunk> chunks;
+    int ci = 0;             // next row chunk
     const bool pull = s->defer_js && host_pages_visible(s->device);
+    ListUploader up;
     cudaStream_t st[2] = {nullptr, nullptr};
     cudaEvent_t done[2] = {nullptr, nullptr}, t0 = nullptr, t1 = nullptr;
     int rc = 1, prev = -1;
@@ -657,9 +762,12 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
         TCH_CK(e, cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming));
     }
     if (s->defer_js) {
-        hflags.assign((size_t)(n + S - 1) / S, 0);
+        chunks = row_chunks(n, S);
+        hflags.assign(chunks.size(), 0);
         TCH_CK(e, cudaMalloc(&dflags, hflags.size() * sizeof(int)));
-        TCH_CK(e, cudaMemset(dflags, 0, hflags.size() * sizeof(int)));
+        // on stripe stream 0 before the start event, which stream 1 also waits for
+        TCH_CK(e, cudaMemsetAsync(dflags, 0, hflags.size() * sizeof(int), st[0]));
+        TCH_CK(e, up.start(s, chunks, pull));
     }
     w_setup = wall() - w0;
     TCH_CK(e, cudaEventCreate(&t0));
@@ -670,21 +778,28 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
         if (r0 < n) {
             const int rows = std::min(S, n - r0), b = (r0 / S) & 1;
             const size_t w = (size_t)(n - r0);
-            const int* flag = nullptr;
             if (s->defer_js) {
-                // this stripe's partner lists: uploaded while the previous stripe
-                // computes, then checked on the device; the stripe kernel and the
-                // atomic pass read the verdict from the flag
-                const size_t pa = s->defer_start[r0], pb = s->defer_start[r0 + rows];
-                TCH_CK(e, upload_u32(s->dJs + pa, s->defer_js + pa, pb - pa, pull, s->num_sms, st[b]));
-                RareCSR rc;
-                rc.start = s->dStart;
-                rc.js = s->dJs;
-                rc.n_rare = s->n_rare;
-                TCH_CK(e, launch_rare_check_sorted(rc, n, dflags + r0 / S, st[b], r0, r0 + rows));
-                flag = dflags + r0 / S;
+                // each row chunk of this stripe: its partner lists, uploaded
+                // ahead by the uploader, are checked on the device; its tile pass
+                // and atomic pass read the verdict from the chunk's flag and
+                // write rows and columns from the chunk's first row on (the
+                // stripe's cells below the diagonal are not part of the output)
+                for (; ci < (int)chunks.size() && chunks[ci].r0 < r0 + rows; ci++) {
+                    cudaEvent_t uploaded = nullptr;
+                    TCH_CK(e, up.ready(ci, &uploaded));
+                    TCH_CK(e, cudaStreamWaitEvent(st[b], uploaded, 0));
+                    RareCSR rc;
+                    rc.start = s->dStart;
+                    rc.js = s->dJs;
+                    rc.n_rare = s->n_rare;
+                    const int ca = chunks[ci].r0, cr = chunks[ci].rows;
+                    TCH_CK(e, launch_rare_check_sorted(rc, n, dflags + ci, st[b], ca, ca + cr));
+                    const size_t off = (size_t)(ca - r0);
+                    if (solver_stripe(s, ca, cr, dU[b] + off * ldo + off, ldo, st[b], e, dflags + ci)) goto fail;
+                }
+            } else if (solver_stripe(s, r0, rows, dU[b], ldo, st[b], e, nullptr)) {
+                goto fail;
             }
-            if (solver_stripe(s, r0, rows, dU[b], ldo, st[b], e, flag)) goto fail;
             TCH_CK(e, cudaMemcpy2DAsync(hU[b], w * 2, dU[b], ldo * 2, w * 2, rows, cudaMemcpyDeviceToHost, st[b]));
             TCH_CK(e, cudaEventRecord(done[b], st[b]));
         }
@@ -719,9 +834,17 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
                 goto fail;
             }
     }
-    if (verbose())
-        fprintf(stderr, "tch: stripes %d rows: setup %.1f ms, pipeline %.1f ms (device %.1f ms, callbacks %.1f ms)\n",
-                S, w_setup * 1e3, (wall() - w0 - w_setup) * 1e3, ms, w_cb * 1e3);
+    if (verbose()) {
+        double up_s;
+        {
+            std::lock_guard<std::mutex> lk(up.mu);
+            up_s = up.seconds;
+        }
+        fprintf(stderr,
+                "tch: stripes %d rows: setup %.1f ms, pipeline %.1f ms (device %.1f ms, callbacks %.1f ms, "
+                "partner uploads %.1f ms)\n",
+                S, w_setup * 1e3, (wall() - w0 - w_setup) * 1e3, ms, w_cb * 1e3, up_s * 1e3);
+    }
     rc = 0;
 fail:
     for (int b = 0; b < 2; b++) {
@@ -802,8 +925,13 @@ int tch_run(int device, int n, size_t n_pad, const uint8_t* O, size_t K1, const 
         fprintf(stderr, "tch: operands on the device in %.1f ms (%.2f GB uploaded)\n", (wall() - w0) * 1e3,
                 (double)(n_pad * (K1 + K2) / 8 + (n_rare + (size_t)n + 1) * 4) / 1e9);
     if (rare_on_gpu) *rare_on_gpu = s->rare_on_host ? 0 : 1;
+    const double w1 = wall();
     const int rc = solver_run(s, S, cb, ctx, gpu_secs, e);
+    const double w2 = wall();
     solver_free(s);
+    if (verbose())
+        fprintf(stderr, "tch: tch_run %.1f ms: operands %.1f, stripes %.1f, release %.1f\n", (wall() - w0) * 1e3,
+                (w1 - w0) * 1e3, (w2 - w1) * 1e3, (wall() - w2) * 1e3);
     return rc;
 }
 

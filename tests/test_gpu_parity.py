@@ -91,11 +91,15 @@ def test_host_rare_fallback(tch, checkpy_inputs):
     upper_equal(H, ref)
 
 
+@pytest.mark.parametrize("stripe", [136, 1024, 1030])
 @pytest.mark.parametrize("pull", ["1", "0"])
-def test_tch_run_partner_upload_paths(tch, checkpy_inputs, pull):
-    """tch_run uploads each stripe's partner lists while the previous stripe
-    computes: staged by cudaMemcpyAsync, or read by the GPU from host memory
-    (TCH_HOST_PULL=1, where the platform allows it).  Both in any order."""
+def test_tch_run_partner_upload_paths(tch, checkpy_inputs, pull, stripe):
+    """tch_run uploads the partner lists ahead of the stripes that use them:
+    copied by cudaMemcpyAsync, or read by the GPU from host memory
+    (TCH_HOST_PULL=1, where the platform allows it).  Both in any order.
+    Stripes of 1 024 rows and more start with their first stripe in
+    sub-stripes of a quarter (multiples of 128 rows): 1 024 -> 4 x 256,
+    1 030 -> 384 + 384 + 262, then 1 024 + 476 / 470 rows."""
     c, A, x, ref = checkpy_inputs[2]
     xr, nd = tch.dense_ranks(A.astype(np.uint64))
     enc = tch.encode_host(xr, nd, 64)
@@ -105,11 +109,28 @@ def test_tch_run_partner_upload_paths(tch, checkpy_inputs, pull):
         rng.shuffle(seg)
     os.environ["TCH_HOST_PULL"] = pull
     try:
-        H, _, rare_gpu, _ = tch.run(enc, stripe=136)
+        H, _, rare_gpu, sink = tch.run(enc, stripe=stripe)
     finally:
         del os.environ["TCH_HOST_PULL"]
     assert rare_gpu == 1
+    assert [c[0] for c in sink.calls] == list(range(0, enc.n, stripe))
     upper_equal(H, ref)
+
+
+@pytest.mark.parametrize("row", [300, 700, 1200])
+def test_invalid_rare_pair_in_a_sub_stripe(tch, row):
+    """An invalid partner in a sub-stripe of the first stripe (rows 256-511,
+    512-767 of a 1 024-row stripe) or in a later stripe is still an error."""
+    rng = np.random.default_rng(8)
+    A = rng.integers(0, 400, size=(1400, 12)).astype(np.uint64)
+    x, nd = tch.dense_ranks(A)
+    enc = tch.encode_host(x, nd, 1000)
+    a, b = int(enc.start[row]), int(enc.start[row + 1])
+    assert b > a
+    enc.js = enc.js.copy()
+    enc.js[a] = row  # j == i
+    with pytest.raises(tch.TchError, match="rare"):
+        tch.run(enc, stripe=1024)
 
 
 def test_unsorted_partner_lists(tch, checkpy_inputs):
