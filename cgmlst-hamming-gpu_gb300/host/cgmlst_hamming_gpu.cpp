@@ -26,11 +26,18 @@
 #include <string.h>
 #include <unistd.h>
 
+#include <fcntl.h>
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <memory>
+#include <new>
 #include <string>
+#include <string_view>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "tch.h"
@@ -45,8 +52,17 @@ namespace {
 constexpr double kGemmRateGB300 = 1.6e15;
 constexpr double kRareRateGB300 = 1.0e11;
 
+// Set while a helper thread creates the CUDA context (during the input's
+// load): an error exit then skips the runtime's teardown, which must not run
+// while another thread is inside its initialisation.
+std::atomic<bool> g_cuda_starting{false};
+
 [[noreturn]] void die(const std::string& msg) {
     fprintf(stderr, "error: %s\n", msg.c_str());
+    if (g_cuda_starting) {
+        fflush(nullptr);
+        _exit(1);
+    }
     exit(1);
 }
 
@@ -62,6 +78,29 @@ std::string fmt(const char* f, ...) {
 double now() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
+
+// An allocator whose value-less construct leaves trivial elements
+// uninitialised: a vector of n elements is allocated without being zero-filled
+// on one core, and its pages are first touched by the threads that fill them.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = NoInitAlloc<U>;
+    };
+    NoInitAlloc() = default;
+    template <class U>
+    NoInitAlloc(const NoInitAlloc<U>&) noexcept {}
+    template <class U>
+    void construct(U* p) noexcept {
+        ::new ((void*)p) U;
+    }
+    template <class U, class... A>
+    void construct(U* p, A&&... a) {
+        ::new ((void*)p) U(std::forward<A>(a)...);
+    }
+};
+using CallMatrix = std::vector<uint64_t, NoInitAlloc<uint64_t>>;
 
 enum class Layout { Full, LowerTri, UpperTri };
 
@@ -275,7 +314,7 @@ void parallel_for(size_t threads, size_t count, size_t chunk, F&& f) {
 // ---- text semantics ---------------------------------------------------------------
 
 // Decodes the UTF-8 code point starting at s[i] (input already validated).
-uint32_t cp_at(const std::string& s, size_t i, size_t* len) {
+uint32_t cp_at(std::string_view s, size_t i, size_t* len) {
     const unsigned char c = (unsigned char)s[i];
     if (c < 0x80) { *len = 1; return c; }
     if ((c >> 5) == 6) { *len = 2; return ((c & 0x1F) << 6) | (s[i + 1] & 0x3F); }
@@ -291,7 +330,7 @@ bool is_ws(uint32_t c) {
 }
 
 // [b, e) of the trimmed cell inside s.
-void trim(const std::string& s, size_t& b, size_t& e) {
+void trim(std::string_view s, size_t& b, size_t& e) {
     while (b < e) {
         size_t len;
         const uint32_t c = cp_at(s, b, &len);
@@ -309,7 +348,7 @@ void trim(const std::string& s, size_t& b, size_t& e) {
 }
 
 // parse_allele (main.rs:98-113): 0 = missing; returns false on u64 overflow.
-bool parse_allele(const std::string& s, size_t b, size_t e, bool skip_repl, const std::string& missing,
+bool parse_allele(std::string_view s, size_t b, size_t e, bool skip_repl, const std::string& missing,
                   uint64_t* out) {
     trim(s, b, e);
     if (!skip_repl && e - b >= 4 && s.compare(b, 4, "INF-") == 0) b += 4;
@@ -336,7 +375,7 @@ bool parse_allele(const std::string& s, size_t b, size_t e, bool skip_repl, cons
 
 // UTF-8 check of s[b, e): every sequence that starts there is complete and
 // well formed (it may read up to 3 bytes past e to finish one).
-bool valid_utf8_range(const std::string& s, size_t b, size_t e) {
+bool valid_utf8_range(std::string_view s, size_t b, size_t e) {
     size_t i = b;
     const size_t n = s.size();
     while (i < e) {
@@ -364,7 +403,7 @@ bool valid_utf8_range(const std::string& s, size_t b, size_t e) {
 
 // The whole buffer, in parallel chunks; a chunk starts at a byte that begins a
 // sequence (continuation bytes at a chunk's start belong to the previous one).
-bool valid_utf8(const std::string& s, size_t threads) {
+bool valid_utf8(std::string_view s, size_t threads) {
     const size_t n = s.size(), parts = std::max<size_t>(1, std::min<size_t>(threads * 4, n / (1 << 20) + 1));
     std::vector<size_t> cut(parts + 1, n);
     cut[0] = 0;
@@ -381,40 +420,82 @@ bool valid_utf8(const std::string& s, size_t threads) {
     return ok;
 }
 
-bool read_all(const std::string& path, std::string& buf, std::string& err, size_t threads) {
-    FILE* f = path == "-" ? stdin : fopen(path.c_str(), "rb");
-    if (!f) {
+// The input's bytes.  A regular file is read into one allocation that is not
+// zero-filled, by parallel preads: each thread faults in and fills its own
+// range, so neither the page faults nor the copy out of the page cache run on
+// one core.  A pipe (or "-") is read sequentially.
+struct InputText {
+    std::unique_ptr<char[]> raw;
+    std::string piped;
+    std::string_view view;
+};
+
+bool read_all(const std::string& path, InputText& in, std::string& err, size_t threads) {
+    bool bad = false;
+    int fd = -1;
+    struct stat st;
+    if (path != "-" && (fd = open(path.c_str(), O_RDONLY)) < 0) {
         err = strerror(errno);
         return false;
     }
-    bool bad = false;
-    if (f != stdin && fseek(f, 0, SEEK_END) == 0) {  // a regular file: one read of its size
-        const long size = ftell(f);
-        if (size >= 0 && fseek(f, 0, SEEK_SET) == 0) {
-            buf.resize((size_t)size);
-            if (size && fread(&buf[0], 1, (size_t)size, f) != (size_t)size) bad = true;
-            char extra;
-            if (!bad && fread(&extra, 1, 1, f) == 1) {  // grew meanwhile: read the rest
-                buf.push_back(extra);
-                char tmp[1 << 16];
-                size_t r;
-                while ((r = fread(tmp, 1, sizeof tmp, f)) > 0) buf.append(tmp, r);
+    if (fd >= 0 && fstat(fd, &st) == 0 && S_ISREG(st.st_mode)) {
+        const size_t size = (size_t)st.st_size;
+        in.raw.reset(new char[std::max<size_t>(size, 1)]);
+        char* base = in.raw.get();
+        const size_t parts = std::max<size_t>(1, std::min<size_t>(threads, size >> 22));
+        std::atomic<bool> short_read{false};
+        parallel_for(threads, parts, 1, [&](size_t a, size_t b) {
+            for (size_t k = a; k < b; k++) {
+                size_t off = size * k / parts;
+                const size_t end = size * (k + 1) / parts;
+                while (off < end) {
+                    const ssize_t r = pread(fd, base + off, end - off, (off_t)off);
+                    if (r <= 0) {
+                        short_read = true;
+                        break;
+                    }
+                    off += (size_t)r;
+                }
             }
+        });
+        bad = short_read;
+        char extra;
+        if (!bad && pread(fd, &extra, 1, (off_t)size) == 1) {  // grew meanwhile: read the rest
+            in.piped.assign(base, size);
+            in.raw.reset();
+            char tmp[1 << 16];
+            ssize_t r;
+            off_t off = (off_t)size;
+            while ((r = pread(fd, tmp, sizeof tmp, off)) > 0) {
+                in.piped.append(tmp, (size_t)r);
+                off += r;
+            }
+            if (r < 0) bad = true;
+            in.view = in.piped;
         } else {
-            bad = true;
+            in.view = std::string_view(base, size);
         }
     } else {
+        FILE* f = fd >= 0 ? fdopen(fd, "rb") : stdin;
+        if (!f) {
+            err = strerror(errno);
+            close(fd);
+            return false;
+        }
         char tmp[1 << 16];
         size_t r;
-        while ((r = fread(tmp, 1, sizeof tmp, f)) > 0) buf.append(tmp, r);
+        while ((r = fread(tmp, 1, sizeof tmp, f)) > 0) in.piped.append(tmp, r);
+        bad = ferror(f) != 0;
+        if (f != stdin) fclose(f);
+        fd = -1;
+        in.view = in.piped;
     }
-    bad = bad || ferror(f);
-    if (f != stdin) fclose(f);
+    if (fd >= 0) close(fd);
     if (bad) {
         err = "read error";
         return false;
     }
-    if (!valid_utf8(buf, threads)) {
+    if (!valid_utf8(in.view, threads)) {
         err = "stream did not contain valid UTF-8";
         return false;
     }
@@ -423,7 +504,7 @@ bool read_all(const std::string& path, std::string& buf, std::string& err, size_
 
 // str::lines: (begin, end) of every line, '\n' and one '\r' before it removed;
 // the newlines are found in parallel chunks.
-std::vector<std::pair<size_t, size_t>> rust_lines(const std::string& t, size_t threads) {
+std::vector<std::pair<size_t, size_t>> rust_lines(std::string_view t, size_t threads) {
     const size_t n = t.size(), parts = std::max<size_t>(1, std::min<size_t>(threads * 4, n / (1 << 20) + 1));
     std::vector<std::vector<size_t>> nl(parts);
     parallel_for(threads, parts, 1, [&](size_t a, size_t b) {
@@ -550,10 +631,16 @@ int main(int argc, char** argv) {
     const char sep = args.input_sep[0];
     if ((size_t)tch_device_count() <= args.device) die(fmt("CUDA device %zu not available", args.device));
 
+    // the CUDA context (~0.1 s) is created while the input is read and parsed
+    g_cuda_starting = true;
+    std::thread cuda_start([&] { tch_free_vram((int)args.device); });
+
     // ---- load (main.rs:286-311)
     double t = now();
-    std::string text, rerr;
-    if (!read_all(args.input, text, rerr, threads)) die(fmt("reading %s: %s", args.input.c_str(), rerr.c_str()));
+    InputText in;
+    std::string rerr;
+    if (!read_all(args.input, in, rerr, threads)) die(fmt("reading %s: %s", args.input.c_str(), rerr.c_str()));
+    const std::string_view text = in.view;
     auto lines = rust_lines(text, threads);
     if (lines.empty()) die("empty input");
     size_t L = 1;
@@ -564,7 +651,7 @@ int main(int argc, char** argv) {
         if (lines[k].second > lines[k].first) data.push_back(lines[k]);
     size_t n = data.size();
     std::vector<std::string> ids(n);
-    std::vector<uint64_t> calls(n * L, 0);
+    CallMatrix calls(n * L);  // every cell written by the parse below
     std::atomic<long> bad_row{-1};
     std::vector<std::string> bad_cell(1);
     std::atomic<bool> bad_taken{false};
@@ -572,20 +659,20 @@ int main(int argc, char** argv) {
         for (size_t i = a; i < b; i++) {
             size_t p = data[i].first, e = data[i].second;
             size_t f = text.find(sep, p);
-            if (f == std::string::npos || f > e) f = e;
-            ids[i] = text.substr(p, f - p);
+            if (f == std::string_view::npos || f > e) f = e;
+            ids[i] = std::string(text.substr(p, f - p));
             size_t k = 0;
             while (f < e) {
                 const size_t cb = f + 1;
                 size_t ce = text.find(sep, cb);
-                if (ce == std::string::npos || ce > e) ce = e;
+                if (ce == std::string_view::npos || ce > e) ce = e;
                 uint64_t v;
                 if (!parse_allele(text, cb, ce, args.skip_repl, args.missing, &v)) {
                     bool expect = false;
                     if (bad_taken.compare_exchange_strong(expect, true)) {
                         size_t tb = cb, te = ce;
                         trim(text, tb, te);
-                        bad_cell[0] = text.substr(tb, te - tb);
+                        bad_cell[0] = std::string(text.substr(tb, te - tb));
                         bad_row = (long)i;
                     }
                     v = 0;
@@ -594,10 +681,11 @@ int main(int argc, char** argv) {
                 k++;
                 f = ce;
             }
+            for (; k < L; k++) calls[i * L + k] = 0;  // a short row: missing to the end
         }
     });
     if (bad_row >= 0) die(fmt("sample %s: allele '%s' too large", ids[bad_row].c_str(), bad_cell[0].c_str()));
-    std::string().swap(text);
+    in = InputText();
     log(fmt("Loaded %zu samples x %zu loci in %.2fs", n, L, now() - t));
 
     // ---- completeness filters (main.rs:313-348)
@@ -609,7 +697,7 @@ int main(int argc, char** argv) {
             if (((double)c / (double)n) * 100.0 >= args.locus_pct) keep.push_back(k);
         }
         if (keep.size() != L) {
-            std::vector<uint64_t> nc(n * keep.size());
+            CallMatrix nc(n * keep.size());
             for (size_t i = 0; i < n; i++)
                 for (size_t d = 0; d < keep.size(); d++) nc[i * keep.size() + d] = calls[i * L + keep[d]];
             calls.swap(nc);
@@ -625,7 +713,7 @@ int main(int argc, char** argv) {
             if (((double)c / (double)L) * 100.0 >= args.sample_pct) keep.push_back(i);
         }
         if (keep.size() != n) {
-            std::vector<uint64_t> nc(keep.size() * L);
+            CallMatrix nc(keep.size() * L);
             std::vector<std::string> nids;
             for (size_t d = 0; d < keep.size(); d++) {
                 std::copy(calls.begin() + keep[d] * L, calls.begin() + (keep[d] + 1) * L, nc.begin() + d * L);
@@ -657,6 +745,8 @@ int main(int argc, char** argv) {
     };
 
     // ---- encode (main.rs:353-445) and GPU (main.rs:447-465)
+    cuda_start.join();
+    g_cuda_starting = false;
     t = now();
     char err[512] = {0};
     std::vector<std::vector<uint16_t>> upper(n);
@@ -669,7 +759,7 @@ int main(int argc, char** argv) {
         if (tch_solver_from_calls((int)args.device, (int)n, (int)L, calls.data(), (int)args.tau, TCH_KERNEL_AUTO,
                                   &solver, err, sizeof err))
             die(err);
-        std::vector<uint64_t>().swap(calls);
+        CallMatrix().swap(calls);
         tch_info info;
         tch_solver_info(solver, &info);
         log(fmt("Encoded in %.2fs: tau=%d, one-hot cols=%zu, rare equal pairs=%zu", now() - t, info.tau,
@@ -712,7 +802,7 @@ int main(int argc, char** argv) {
         std::vector<uint32_t> nd(L);
         if (tch_dense_ranks(calls.data(), (int)n, (int)L, x.data(), nd.data(), (int)threads, err, sizeof err))
             die(err);
-        std::vector<uint64_t>().swap(calls);
+        CallMatrix().swap(calls);
         const size_t stripe = std::max<size_t>(args.stripe, 8) / 8 * 8;
         int tau = (int)args.tau;
         if (tau <= 0 &&
