@@ -19,13 +19,14 @@
 // with its lanes on consecutive members (coalesced loads, up to eight in
 // flight per lane).
 
+#include <climits>
+
 #include "tch_internal.cuh"
 
 namespace tch {
 namespace {
 
-constexpr int RD_WORDS = 32768;          // u32 counter words in shared memory (128 KB)
-constexpr int RD_COLS = 2 * RD_WORDS;    // columns per pass
+constexpr int RD_WORDS = 32768;          // u32 counter words in shared memory (128 KB): 65 536 columns per pass
 
 // Counter words a launch needs (a narrow stripe takes less shared memory, so
 // more CTAs fit on an SM when several solves run side by side).
@@ -333,9 +334,18 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
         attr = true;
     }
     const int cwords = counter_words(width);
-    // a small stripe (few rows, narrow) takes CTAs of 256 threads: four fit on an SM,
-    // so solves that run side by side share the SMs
-    if (rows < 2 * sms && width <= 8192) {
+    // a narrow stripe takes CTAs of 256 threads, one row each: four fit on an SM,
+    // so four rows' lookup chains (rank -> group -> partner search) overlap, and
+    // solves that run side by side share the SMs.  Narrow rows carry little
+    // counting work, so their time is those chains: on 512 sets of 50-5 000
+    // profiles (one graph) the batch took 36.5 ms this way and 46.4 ms when only
+    // stripes under 304 rows did.  TCH_RARE_SMALL_ROWS sets a row limit for it.
+    static int small_rows = -1;
+    if (small_rows < 0) {
+        const char* v = getenv("TCH_RARE_SMALL_ROWS");
+        small_rows = v ? std::max(0, atoi(v)) : INT_MAX;
+    }
+    if (rows < small_rows && width <= 8192) {
         rare_dense_kernel<256><<<std::max(1, rows), 256, rd_smem<256>(cwords), st>>>(g, r0, rows, R, ldr,
                                                                                    r0 + (int)width, cwords);
     } else {

@@ -139,6 +139,30 @@ def test_options_and_streams(pkg, tmp_path, case_files):
 
 
 @pytest.mark.gpu
+def test_large_file_read_in_parts(pkg, tmp_path):
+    """A regular file is read by parallel preads, one part per 4 MB (here 7
+    threads over ~27 MB: uneven parts, cells across part boundaries): the same
+    output as the same text through a pipe, and the oracle's distances."""
+    rng = np.random.default_rng(31)
+    n, L = 1800, 1500
+    A = (np.arange(L, dtype=np.uint64)[None, :] << np.uint64(20)) + rng.integers(1, 30, size=(n, L)).astype(np.uint64)
+    A[rng.random((n, L)) < 0.03] = 0
+    lines = ["FILE\t" + "\t".join(f"L{k}" for k in range(L))]
+    lines += [f"s{i}\t" + "\t".join("-" if v == 0 else str(v) for v in A[i].tolist()) for i in range(n)]
+    text = "\n".join(lines) + "\n"
+    p = tmp_path / "big.tsv"
+    p.write_text(text)
+    assert p.stat().st_size > 6 * (4 << 20)
+    r_file = run(pkg, ["-s", "-i", str(p), "-t", "7"])
+    assert r_file.returncode == 0, r_file.stderr
+    r_pipe = run(pkg, ["-s", "-i", "-", "-t", "7"], stdin=text)
+    assert r_pipe.returncode == 0, r_pipe.stderr
+    assert r_file.stdout == r_pipe.stdout
+    x, _ = oracle.dense_ranks(A)
+    np.testing.assert_array_equal(parse(r_file.stdout), oracle.hamming(x).astype(np.int64))
+
+
+@pytest.mark.gpu
 def test_filters_and_cell_options(pkg, tmp_path):
     text = ("F\ta\tb\tc\td\n"
             "A\t1\tX\t1\tINF-2\n"
