@@ -251,7 +251,6 @@ def serving_bench(tch, synth, args, device):
     rids = [None] * R
     bslot = [None] * R
     submit_delay = np.zeros(R)
-    tb = time.perf_counter() + 0.05
 
     def submitter():
         for k in range(R):
@@ -266,7 +265,8 @@ def serving_bench(tch, synth, args, device):
                                 out_qq=bufs[j][1][:m * m].reshape(m, m))
             submit_delay[k] = time.perf_counter() - t
 
-    link_before = host_link(device)
+    link_before = host_link(device)  # first use of torch here: outside the arrival clock
+    tb = time.perf_counter() + 0.05
     th = threading.Thread(target=submitter)
     th.start()
     lat = np.zeros(R)
@@ -536,37 +536,9 @@ def main():
             roofline["traffic_source"] = kv.get("source", "").strip()
 
     # e2e through the C ABI with host buffers: tch_run (the reference's entry
-    # point, host-encoded operands) and tch_run_calls (allele calls, device encoder)
-    # serving: in a process of its own, as a service would run, and before the
-    # legs that churn host memory (its large copies slow down after them)
-    serving = None
-    if rank == 0 and ws == 1 and not args.no_serving:
-        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--serving-only",
-                            "--serve-db", str(args.serve_db), "--serve-requests", str(args.serve_requests)],
-                           capture_output=True, text=True, env=dict(os.environ, CUDA_VISIBLE_DEVICES=str(device)))
-        if r.returncode:
-            raise RuntimeError("serving leg failed: " + r.stderr[-2000:])
-        serving = json.loads(r.stdout.strip().splitlines()[-1])
-        serving["process"] = "separate (bench.py --serving-only)"
-        log("serving:", serving)
-
-    # learned vs analytic tau: whole-triangle device time at each pick and at
-    # a sweep of taus around them (fresh solvers)
-    tau_cmp = None
-    if rank == 0 and ws == 1 and not args.no_tau_sweep:
-        swept = {int(tau): ms_per_step}
-        cands = {512, 1024, 2048, 4096, 8192} | set(tau_pick.values())
-        for t in sorted(cands):
-            if t not in swept:
-                ms_t, used = time_whole(tch, A, t, device, out, ldo, stream)
-                swept[int(used)] = ms_t
-        best = min(swept, key=swept.get)
-        tau_cmp = {"used": int(tau), "swept_ms": {str(k): v for k, v in sorted(swept.items())},
-                   "best_swept": {"tau": best, "ms": swept[best]}}
-        for k, v in tau_pick.items():
-            tau_cmp[k] = {"tau": v, "ms": swept.get(v)}
-        log("tau comparison:", tau_cmp)
-
+    # point, host-encoded operands) and tch_run_calls (allele calls, device
+    # encoder), first after the device-resident timing: copies from host memory
+    # run slower after the legs that pin and release gigabytes of it
     e2e = None
     e2e_calls = None
     if rank == 0 and args.e2e_steps > 0:
@@ -620,6 +592,37 @@ def main():
                      "d2h_bytes_per_step": int(d2h), "seconds_per_step": ec, "tau": int(tu.value), "host_link_gbs": link,
                      "samples_s": [round(t, 5) for t in times_calls],
                      "path": "tch_run_calls: allele calls uploaded, device encoder, same stripes and copy-back"}
+
+    # serving: in a process of its own, as a service would run, after the e2e
+    # legs and before the legs that churn host memory (large copies from host
+    # memory slow down after them)
+    serving = None
+    if rank == 0 and ws == 1 and not args.no_serving:
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--serving-only",
+                            "--serve-db", str(args.serve_db), "--serve-requests", str(args.serve_requests)],
+                           capture_output=True, text=True, env=dict(os.environ, CUDA_VISIBLE_DEVICES=str(device)))
+        if r.returncode:
+            raise RuntimeError("serving leg failed: " + r.stderr[-2000:])
+        serving = json.loads(r.stdout.strip().splitlines()[-1])
+        serving["process"] = "separate (bench.py --serving-only)"
+        log("serving:", serving)
+
+    # learned vs analytic tau: whole-triangle device time at each pick and at
+    # a sweep of taus around them (fresh solvers)
+    tau_cmp = None
+    if rank == 0 and ws == 1 and not args.no_tau_sweep:
+        swept = {int(tau): ms_per_step}
+        cands = {512, 1024, 2048, 4096, 8192} | set(tau_pick.values())
+        for t in sorted(cands):
+            if t not in swept:
+                ms_t, used = time_whole(tch, A, t, device, out, ldo, stream)
+                swept[int(used)] = ms_t
+        best = min(swept, key=swept.get)
+        tau_cmp = {"used": int(tau), "swept_ms": {str(k): v for k, v in sorted(swept.items())},
+                   "best_swept": {"tau": best, "ms": swept[best]}}
+        for k, v in tau_pick.items():
+            tau_cmp[k] = {"tau": v, "ms": swept.get(v)}
+        log("tau comparison:", tau_cmp)
 
     # the reference's TSV writer (main.rs:224-265) on the GPU: the full matrix
     # as text, delivered block by block to a callback that discards it
