@@ -395,7 +395,7 @@ def main():
             return
         threads = os.cpu_count() or 1
         vals = []
-        for _ in range(args.warmup if args.warmup < 1 else 1):
+        for _ in range(args.warmup):  # short untimed samples (~1 s each)
             cpu_sample(x, 1.0, 0)
         for _ in range(args.steps):
             rate, pairs, rows, dt = cpu_sample(x, args.cpu_seconds / max(args.steps, 1), 0)
@@ -403,7 +403,7 @@ def main():
         v = statistics.median(vals)
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": pairs_total / v * 1e3,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
+                "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "u16",
                 "data": "synthetic", "config": workload,
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                  "sample": f"brute-force count (check.py:39-44 restated in C, OpenMP) over the "
