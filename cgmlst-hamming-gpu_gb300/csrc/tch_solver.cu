@@ -654,7 +654,7 @@ struct ListUploader {
     std::thread th;
     std::mutex mu;
     std::condition_variable cv;
-    int issued = 0;  // stripes whose copy is issued and whose event is recorded
+    int issued = 0;  // chunks whose copy is issued and whose event is recorded
     cudaError_t err = cudaSuccess;
     bool stop = false;
     cudaStream_t st = nullptr;
@@ -745,7 +745,7 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
     std::vector<RowChunk> chunks;
     int ci = 0;             // next row chunk
     const bool pull = s->defer_js && host_pages_visible(s->device);
-    ListUploader up;
+    ListUploader uploader;
     cudaStream_t st[2] = {nullptr, nullptr};
     cudaEvent_t done[2] = {nullptr, nullptr}, t0 = nullptr, t1 = nullptr;
     int rc = 1, prev = -1;
@@ -767,7 +767,7 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
         TCH_CK(e, cudaMalloc(&dflags, hflags.size() * sizeof(int)));
         // on stripe stream 0 before the start event, which stream 1 also waits for
         TCH_CK(e, cudaMemsetAsync(dflags, 0, hflags.size() * sizeof(int), st[0]));
-        TCH_CK(e, up.start(s, chunks, pull));
+        TCH_CK(e, uploader.start(s, chunks, pull));
     }
     w_setup = wall() - w0;
     TCH_CK(e, cudaEventCreate(&t0));
@@ -786,7 +786,7 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
                 // stripe's cells below the diagonal are not part of the output)
                 for (; ci < (int)chunks.size() && chunks[ci].r0 < r0 + rows; ci++) {
                     cudaEvent_t uploaded = nullptr;
-                    TCH_CK(e, up.ready(ci, &uploaded));
+                    TCH_CK(e, uploader.ready(ci, &uploaded));
                     TCH_CK(e, cudaStreamWaitEvent(st[b], uploaded, 0));
                     RareCSR rc;
                     rc.start = s->dStart;
@@ -837,8 +837,8 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
     if (verbose()) {
         double up_s;
         {
-            std::lock_guard<std::mutex> lk(up.mu);
-            up_s = up.seconds;
+            std::lock_guard<std::mutex> lk(uploader.mu);
+            up_s = uploader.seconds;
         }
         fprintf(stderr,
                 "tch: stripes %d rows: setup %.1f ms, pipeline %.1f ms (device %.1f ms, callbacks %.1f ms, "
