@@ -688,37 +688,59 @@ int main(int argc, char** argv) {
     in = InputText();
     log(fmt("Loaded %zu samples x %zu loci in %.2fs", n, L, now() - t));
 
-    // ---- completeness filters (main.rs:313-348)
+    // ---- completeness filters (main.rs:313-348), counted and compacted in parallel
     if (args.has_locus) {
+        // non-missing calls per locus: blocks of rows counted apart, then summed
+        const size_t parts = std::max<size_t>(1, std::min<size_t>(threads, n / 256 + 1));
+        std::vector<std::vector<size_t>> part(parts, std::vector<size_t>(L, 0));
+        parallel_for(threads, parts, 1, [&](size_t a, size_t b) {
+            for (size_t p = a; p < b; p++) {
+                std::vector<size_t>& c = part[p];
+                for (size_t i = n * p / parts; i < n * (p + 1) / parts; i++) {
+                    const uint64_t* row = calls.data() + i * L;
+                    for (size_t k = 0; k < L; k++) c[k] += row[k] != 0;
+                }
+            }
+        });
         std::vector<size_t> keep;
         for (size_t k = 0; k < L; k++) {
             size_t c = 0;
-            for (size_t i = 0; i < n; i++) c += calls[i * L + k] != 0;
+            for (size_t p = 0; p < parts; p++) c += part[p][k];
             if (((double)c / (double)n) * 100.0 >= args.locus_pct) keep.push_back(k);
         }
         if (keep.size() != L) {
-            CallMatrix nc(n * keep.size());
-            for (size_t i = 0; i < n; i++)
-                for (size_t d = 0; d < keep.size(); d++) nc[i * keep.size() + d] = calls[i * L + keep[d]];
+            const size_t lk = keep.size();
+            CallMatrix nc(n * lk);
+            parallel_for(threads, n, 256, [&](size_t a, size_t b) {
+                for (size_t i = a; i < b; i++)
+                    for (size_t d = 0; d < lk; d++) nc[i * lk + d] = calls[i * L + keep[d]];
+            });
             calls.swap(nc);
-            L = keep.size();
+            L = lk;
         }
         log(fmt("Locus completeness >= %s%%: kept %zu loci", fmt("%g", args.locus_pct).c_str(), L));
     }
     if (args.has_sample) {
+        std::vector<char> ok(n, 0);
+        parallel_for(threads, n, 256, [&](size_t a, size_t b) {
+            for (size_t i = a; i < b; i++) {
+                size_t c = 0;
+                const uint64_t* row = calls.data() + i * L;
+                for (size_t k = 0; k < L; k++) c += row[k] != 0;
+                ok[i] = ((double)c / (double)L) * 100.0 >= args.sample_pct;
+            }
+        });
         std::vector<size_t> keep;
-        for (size_t i = 0; i < n; i++) {
-            size_t c = 0;
-            for (size_t k = 0; k < L; k++) c += calls[i * L + k] != 0;
-            if (((double)c / (double)L) * 100.0 >= args.sample_pct) keep.push_back(i);
-        }
+        for (size_t i = 0; i < n; i++)
+            if (ok[i]) keep.push_back(i);
         if (keep.size() != n) {
             CallMatrix nc(keep.size() * L);
-            std::vector<std::string> nids;
-            for (size_t d = 0; d < keep.size(); d++) {
-                std::copy(calls.begin() + keep[d] * L, calls.begin() + (keep[d] + 1) * L, nc.begin() + d * L);
-                nids.push_back(ids[keep[d]]);
-            }
+            parallel_for(threads, keep.size(), 256, [&](size_t a, size_t b) {
+                for (size_t d = a; d < b; d++)
+                    std::copy(calls.begin() + keep[d] * L, calls.begin() + (keep[d] + 1) * L, nc.begin() + d * L);
+            });
+            std::vector<std::string> nids(keep.size());
+            for (size_t d = 0; d < keep.size(); d++) nids[d] = std::move(ids[keep[d]]);
             calls.swap(nc);
             ids.swap(nids);
             n = keep.size();
