@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library or CLI links or
  * calls this file; tests, the smoke check and the CPU-baseline leg of the
- * benchmark use it as the checker.
+ * benchmark use it as the oracle.
  *
  * It restates the reference's brute-force count, which is the definition
  * every GPU result is compared with:

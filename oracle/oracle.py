@@ -1,7 +1,8 @@
 """CPU oracle for the exact cgMLST Hamming distance path.
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` import this module, and only as the checker.
+CPU-baseline leg of ``bench.py`` import this module, and only as the oracle
+(the reference result a GPU result is compared with, or the CPU time measured).
 The product library (``libtch``) and the CLI never call it.
 
 It restates, function by function, what the reference computes on the host

@@ -1,6 +1,6 @@
 """CPU oracle of the learned tau model (test infrastructure only).
 
-The reference has no learned component; this is the checker for the
+The reference has no learned component; this is the oracle for the
 library's MLP kernels (csrc/k_mlp.cu): the same network, loss and parameter
 layout in float64 numpy, forward and backward written out by hand, plus a
 central finite-difference gradient that pins the hand-written backward.
