@@ -1,0 +1,89 @@
+"""Host code under AddressSanitizer and UBSan, on the CPU: the library's host
+encoder (csrc/encode_host.cpp) and the CLI's input path (parallel preads,
+line split, cell parse), compiled here with -fsanitize and run on generated
+inputs.  A sanitizer report makes the program exit non-zero."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG_DIR = os.path.join(ROOT, "cgmlst-hamming-gpu_gb300")
+FLAGS = ["-O1", "-g", "-std=c++17", "-pthread", "-fsanitize=address,undefined", "-fno-sanitize-recover=undefined",
+         "-fno-omit-frame-pointer"]
+
+
+def build(tmp_path, name, srcs, extra=()):
+    exe = str(tmp_path / name)
+    r = subprocess.run(["g++", *FLAGS, "-I", os.path.join(ROOT, "include"), *srcs, "-o", exe, *extra],
+                       capture_output=True, text=True)
+    if r.returncode:
+        if "asan" in r.stderr.lower() or "ubsan" in r.stderr.lower():
+            pytest.skip("no sanitizer runtime for g++ here")
+        raise AssertionError(r.stderr[-3000:])
+    return exe
+
+
+def test_host_encoder_under_sanitizers(tmp_path):
+    exe = build(tmp_path, "encode_check", [os.path.join(ROOT, "tests", "sanitize", "encode_host_check.cpp"),
+                                           os.path.join(PKG_DIR, "csrc", "encode_host.cpp")])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "encode_host ok" in r.stdout, r.stdout + r.stderr[-3000:]
+
+
+def expected(text: str):
+    """bytes, lines (str::lines), fields before each line's end, and the sum
+    of the parsed ids, for inputs of digits, '-', 'INF-' ids and spaces."""
+    lines = text.split("\n")
+    if lines and lines[-1] == "":
+        lines.pop()
+    lines = [ln[:-1] if ln.endswith("\r") else ln for ln in lines]
+    cells, total = 0, 0
+    for ln in lines:
+        fields = ln.split("\t")
+        if ln.endswith("\t"):
+            fields.pop()
+        if ln == "":
+            fields = []
+        cells += len(fields)
+        for f in fields:
+            f = f.strip(" ")
+            if f.startswith("INF-"):
+                f = f[4:]
+            if f and f != "-" and f.isdigit():
+                total += int(f)
+    return len(text.encode()), len(lines), cells, total
+
+
+def test_cli_input_path_under_sanitizers(tmp_path, pkg):
+    lib_dir = os.path.join(PKG_DIR, "lib")
+    exe = build(tmp_path, "cli_read_check", [os.path.join(ROOT, "tests", "sanitize", "cli_read_check.cpp")],
+                extra=["-I", os.path.join(PKG_DIR, "host"), "-L", lib_dir, "-ltch", "-ldl",
+                       f"-Wl,-rpath,{lib_dir}"])
+    rng = np.random.default_rng(3)
+    n, L = 2500, 700
+    ids = rng.integers(1, 10**9, size=(n, L))
+    rows = []
+    for i in range(n):
+        cells = [str(v) for v in ids[i].tolist()]
+        for k in rng.integers(0, L, size=20).tolist():
+            cells[k] = "-"
+        cells[i % L] = f"INF-{ids[i, 0]}"
+        cells[(i * 7) % L] = f" {ids[i, 1]} "
+        if i % 97 == 0:
+            cells = cells[: L // 2]  # a short row
+        rows.append(f"s{i}\t" + "\t".join(cells) + ("\r\n" if i % 5 == 0 else "\n"))
+    big = "FILE\t" + "\t".join(f"L{k}" for k in range(L)) + "\n" + "".join(rows)
+    files = {"big.tsv": big, "small.tsv": "FILE\tA\nx\t1\n\n y \tINF-3", "empty.tsv": ""}
+    for name, text in files.items():
+        (tmp_path / name).write_text(text)
+    assert len(big) > 12 * (1 << 20)  # at least three read parts
+    r = subprocess.run([exe, *[str(tmp_path / f) for f in files]], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr[-3000:]
+    out = r.stdout.strip().split("\n")
+    assert len(out) == 4 * len(files)
+    for k, (name, text) in enumerate(files.items()):
+        got = out[4 * k: 4 * k + 4]
+        assert len(set(got)) == 1, (name, got)  # every thread count reads the same
+        assert tuple(int(v) for v in got[0].split()) == expected(text), name
