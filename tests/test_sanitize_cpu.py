@@ -1,7 +1,7 @@
 """Host code under AddressSanitizer and UBSan, on the CPU: the library's host
-encoder (csrc/encode_host.cpp) and the CLI's input path (parallel preads,
-line split, cell parse), compiled here with -fsanitize and run on generated
-inputs.  A sanitizer report makes the program exit non-zero."""
+encoder (csrc/encode_host.cpp), the CLI's input path (parallel preads, line
+split, cell parse) and its gzip writer, compiled here with -fsanitize and run
+on generated inputs.  A sanitizer report makes the program exit non-zero."""
 import os
 import subprocess
 
@@ -21,6 +21,8 @@ def build(tmp_path, name, srcs, extra=()):
     if r.returncode:
         if "asan" in r.stderr.lower() or "ubsan" in r.stderr.lower():
             pytest.skip("no sanitizer runtime for g++ here")
+        if "zlib.h" in r.stderr or "-lz" in r.stderr:
+            pytest.skip("no zlib for g++ here")
         raise AssertionError(r.stderr[-3000:])
     return exe
 
@@ -87,3 +89,21 @@ def test_cli_input_path_under_sanitizers(tmp_path, pkg):
         got = out[4 * k: 4 * k + 4]
         assert len(set(got)) == 1, (name, got)  # every thread count reads the same
         assert tuple(int(v) for v in got[0].split()) == expected(text), name
+
+
+@pytest.mark.parametrize("zlib", [True, False])
+def test_gzip_writer_under_sanitizers(tmp_path, zlib):
+    """Stored blocks and zlib deflate both decompress to the bytes written."""
+    import gzip
+
+    extra = ["-I", os.path.join(PKG_DIR, "host")] + (["-DTCH_HAVE_ZLIB", "-lz"] if zlib else [])
+    exe = build(tmp_path, f"gzip_check_{int(zlib)}", [os.path.join(ROOT, "tests", "sanitize", "gzip_check.cpp")],
+                extra=extra)
+    rng = np.random.default_rng(4)
+    data = b"".join([rng.integers(0, 10, 3_000_000, dtype=np.uint8).astype(np.uint8).tobytes() + b"\t",
+                     b"", bytes(range(256)) * 9000, b"x" * 2_500_000])
+    for payload in (data, b"", b"a"):
+        r = subprocess.run([exe], input=payload, capture_output=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-3000:]
+        assert gzip.decompress(r.stdout) == payload
+
