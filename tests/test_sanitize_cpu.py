@@ -1,6 +1,6 @@
 """Host code under AddressSanitizer and UBSan, on the CPU: the library's host
 encoder (csrc/encode_host.cpp), the CLI's input path (parallel preads, line
-split, cell parse) and its gzip writer, compiled here with -fsanitize and run
+split, cell parse), its CPU TSV writer and its gzip writer, compiled here with -fsanitize and run
 on generated inputs.  A sanitizer report makes the program exit non-zero."""
 import os
 import subprocess
@@ -106,4 +106,29 @@ def test_gzip_writer_under_sanitizers(tmp_path, zlib):
         r = subprocess.run([exe], input=payload, capture_output=True, timeout=600)
         assert r.returncode == 0, r.stderr[-3000:]
         assert gzip.decompress(r.stdout) == payload
+
+
+def test_cpu_writer_under_sanitizers(tmp_path, pkg):
+    """The --host-format writer's text equals the oracle's (main.rs:224-265)
+    for every layout, a cap and a multi-byte separator, over more than one
+    1 024-row chunk."""
+    import oracle
+
+    lib_dir = os.path.join(PKG_DIR, "lib")
+    exe = build(tmp_path, "writer_check", [os.path.join(ROOT, "tests", "sanitize", "writer_check.cpp")],
+                extra=["-I", os.path.join(PKG_DIR, "host"), "-L", lib_dir, "-ltch", "-ldl",
+                       f"-Wl,-rpath,{lib_dir}"])
+    rng = np.random.default_rng(6)
+    n = 1100
+    U = np.triu(rng.integers(0, 70000, size=(n, n)) % 65536, 1).astype(np.int64)
+    H = U + U.T
+    text_in = f"{n}\n" + "\n".join(" ".join(map(str, row)) for row in H.tolist()) + "\n"
+    ids = [f"s{i}" for i in range(n)]
+    for osep, index_name, mode, cap, threads in [("\t", "cgmlst-hamming-gpu", "full", 0, 7),
+                                                  (";", "ID", "lower-tri", 0, 3),
+                                                  ("::", "x", "upper-tri", 1000, 16)]:
+        r = subprocess.run([exe, osep, index_name, mode, str(cap), str(threads)], input=text_in,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-3000:]
+        assert r.stdout == oracle.write_matrix(ids, H, osep=osep, index_name=index_name, mode=mode, cap=cap), mode
 
