@@ -373,12 +373,81 @@ bool parse_allele(std::string_view s, size_t b, size_t e, bool skip_repl, const 
     return true;
 }
 
+// The cells of one data row (main.rs:295-311): the row is text[f, e), f at the
+// separator after the sample id (or e).  Cell k goes to out[k] for k < L;
+// cells past L are read and dropped, cells missing at the row's end are 0.
+// A cell of 1-19 ASCII digits running up to the separator is parsed in the
+// same pass that finds its end (such a value cannot overflow, trimming and the
+// INF- prefix do not apply, and the missing token is not all digits when the
+// fast path is on); any other cell is found with memchr and read by
+// parse_allele.  Returns false with [*bad_b, *bad_e) at the first cell whose
+// id overflows u64 (that cell reads 0).
+struct RowFormat {
+    char sep;
+    bool skip_repl;
+    const std::string* missing;
+    bool fast;  // the separator is not a digit and the missing token is not all digits
+};
+
+RowFormat row_format(char sep, bool skip_repl, const std::string& missing) {
+    bool digits = !missing.empty();
+    for (char c : missing) digits = digits && c >= '0' && c <= '9';
+    return RowFormat{sep, skip_repl, &missing, !(sep >= '0' && sep <= '9') && !digits};
+}
+
+bool parse_row(std::string_view text, size_t f, size_t e, const RowFormat& rf, size_t L, uint64_t* out,
+               size_t* bad_b, size_t* bad_e) {
+    const char* s = text.data();
+    bool ok = true;
+    size_t k = 0;
+    while (f < e) {
+        const size_t cb = f + 1;
+        size_t q = cb;
+        uint64_t v = 0;
+        if (rf.fast)
+            while (q < e && q - cb < 19) {
+                const unsigned d = (unsigned)(unsigned char)s[q] - (unsigned)'0';
+                if (d > 9) break;
+                v = v * 10 + d;
+                q++;
+            }
+        size_t ce;
+        if (rf.fast && q > cb && (q == e || s[q] == rf.sep)) {
+            ce = q;
+        } else {
+            const void* hit = cb < e ? memchr(s + cb, rf.sep, e - cb) : nullptr;
+            ce = hit ? (size_t)((const char*)hit - s) : e;
+            if (!parse_allele(text, cb, ce, rf.skip_repl, *rf.missing, &v)) {
+                if (ok) {
+                    *bad_b = cb;
+                    *bad_e = ce;
+                }
+                ok = false;
+                v = 0;
+            }
+        }
+        if (k < L) out[k] = v;
+        k++;
+        f = ce;
+    }
+    for (; k < L; k++) out[k] = 0;
+    return ok;
+}
+
 // UTF-8 check of s[b, e): every sequence that starts there is complete and
 // well formed (it may read up to 3 bytes past e to finish one).
 bool valid_utf8_range(std::string_view s, size_t b, size_t e) {
     size_t i = b;
     const size_t n = s.size();
     while (i < e) {
+        // a run of ASCII, eight bytes at a time (no byte with its high bit set)
+        while (i + 8 <= e) {
+            uint64_t w;
+            memcpy(&w, s.data() + i, 8);
+            if (w & 0x8080808080808080ull) break;
+            i += 8;
+        }
+        if (i >= e) break;
         const unsigned char c = (unsigned char)s[i];
         size_t len;
         uint32_t cp;
@@ -655,33 +724,22 @@ int main(int argc, char** argv) {
     std::atomic<long> bad_row{-1};
     std::vector<std::string> bad_cell(1);
     std::atomic<bool> bad_taken{false};
+    const RowFormat rf = row_format(sep, args.skip_repl, args.missing);
     parallel_for(threads, n, 64, [&](size_t a, size_t b) {
         for (size_t i = a; i < b; i++) {
-            size_t p = data[i].first, e = data[i].second;
+            const size_t p = data[i].first, e = data[i].second;
             size_t f = text.find(sep, p);
             if (f == std::string_view::npos || f > e) f = e;
             ids[i] = std::string(text.substr(p, f - p));
-            size_t k = 0;
-            while (f < e) {
-                const size_t cb = f + 1;
-                size_t ce = text.find(sep, cb);
-                if (ce == std::string_view::npos || ce > e) ce = e;
-                uint64_t v;
-                if (!parse_allele(text, cb, ce, args.skip_repl, args.missing, &v)) {
-                    bool expect = false;
-                    if (bad_taken.compare_exchange_strong(expect, true)) {
-                        size_t tb = cb, te = ce;
-                        trim(text, tb, te);
-                        bad_cell[0] = std::string(text.substr(tb, te - tb));
-                        bad_row = (long)i;
-                    }
-                    v = 0;
+            size_t cb = 0, ce = 0;
+            if (!parse_row(text, f, e, rf, L, calls.data() + i * L, &cb, &ce)) {
+                bool expect = false;
+                if (bad_taken.compare_exchange_strong(expect, true)) {
+                    trim(text, cb, ce);
+                    bad_cell[0] = std::string(text.substr(cb, ce - cb));
+                    bad_row = (long)i;
                 }
-                if (k < L) calls[i * L + k] = v;
-                k++;
-                f = ce;
             }
-            for (; k < L; k++) calls[i * L + k] = 0;  // a short row: missing to the end
         }
     });
     if (bad_row >= 0) die(fmt("sample %s: allele '%s' too large", ids[bad_row].c_str(), bad_cell[0].c_str()));

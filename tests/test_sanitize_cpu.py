@@ -1,6 +1,7 @@
 """Host code under AddressSanitizer and UBSan, on the CPU: the library's host
-encoder (csrc/encode_host.cpp), the CLI's input path (parallel preads, line
-split, cell parse), its CPU TSV writer and its gzip writer, compiled here with -fsanitize and run
+encoder (csrc/encode_host.cpp), the CLI's input path (parallel preads, UTF-8
+check, line split, cell parse, the fused row parser), its CPU TSV writer and its
+gzip writer, compiled here with -fsanitize and run
 on generated inputs.  A sanitizer report makes the program exit non-zero."""
 import os
 import subprocess
@@ -34,9 +35,14 @@ def test_host_encoder_under_sanitizers(tmp_path):
     assert r.returncode == 0 and "encode_host ok" in r.stdout, r.stdout + r.stderr[-3000:]
 
 
+# Unicode White_Space, the set Rust's str::trim removes
+WHITE_SPACE = ("\t\n\x0b\x0c\r \x85\xa0\u1680" + "".join(chr(c) for c in range(0x2000, 0x200B))
+               + "\u2028\u2029\u202f\u205f\u3000")
+
+
 def expected(text: str):
     """bytes, lines (str::lines), fields before each line's end, and the sum
-    of the parsed ids, for inputs of digits, '-', 'INF-' ids and spaces."""
+    of the parsed ids, for inputs of digits, '-', 'INF-' ids and white space."""
     lines = text.split("\n")
     if lines and lines[-1] == "":
         lines.pop()
@@ -50,7 +56,7 @@ def expected(text: str):
             fields = []
         cells += len(fields)
         for f in fields:
-            f = f.strip(" ")
+            f = f.strip(WHITE_SPACE)
             if f.startswith("INF-"):
                 f = f[4:]
             if f and f != "-" and f.isdigit():
@@ -77,9 +83,10 @@ def test_cli_input_path_under_sanitizers(tmp_path, pkg):
             cells = cells[: L // 2]  # a short row
         rows.append(f"s{i}\t" + "\t".join(cells) + ("\r\n" if i % 5 == 0 else "\n"))
     big = "FILE\t" + "\t".join(f"L{k}" for k in range(L)) + "\n" + "".join(rows)
-    files = {"big.tsv": big, "small.tsv": "FILE\tA\nx\t1\n\n y \tINF-3", "empty.tsv": ""}
+    files = {"big.tsv": big, "small.tsv": "FILE\tA\nx\t1\n\n y \tINF-3", "empty.tsv": "",
+             "utf8.tsv": "FILE\tA\u00e9\n\u3000s\u00e9\t\u00a012\u2003\n\U0001F600\t7\n" * 5000}
     for name, text in files.items():
-        (tmp_path / name).write_text(text)
+        (tmp_path / name).write_text(text, encoding="utf-8")
     assert len(big) > 12 * (1 << 20)  # at least three read parts
     r = subprocess.run([exe, *[str(tmp_path / f) for f in files]], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr[-3000:]
@@ -89,6 +96,26 @@ def test_cli_input_path_under_sanitizers(tmp_path, pkg):
         got = out[4 * k: 4 * k + 4]
         assert len(set(got)) == 1, (name, got)  # every thread count reads the same
         assert tuple(int(v) for v in got[0].split()) == expected(text), name
+    # invalid UTF-8 anywhere (also past the first 8-byte ASCII runs) is an error,
+    # as Rust's str::from_utf8 (and Python's decoder) has it
+    ascii_run = b"FILE\tA\n" + b"s1\t123\n" * 3
+    bad = {"lone_continuation": b"\x80", "truncated": b"\xe3\x80", "overlong": b"\xc0\xaf",
+           "surrogate": b"\xed\xa0\x80", "too_large": b"\xf4\x90\x80\x80", "bad_lead": b"\xff"}
+    good = {"two_byte": "\u00e9".encode(), "three_byte": "\u3000".encode(), "four_byte": "\U0001F600".encode()}
+    for name, seq in {**bad, **good}.items():
+        for where in (0, 5, len(ascii_run)):
+            data = ascii_run[:where] + seq + ascii_run[where:]
+            (tmp_path / "u.tsv").write_bytes(data)
+            r = subprocess.run([exe, str(tmp_path / "u.tsv")], capture_output=True, text=True, timeout=60)
+            assert r.returncode == 0, r.stderr[-3000:]
+            try:
+                data.decode("utf-8")
+                valid = True
+            except UnicodeDecodeError:
+                valid = False
+            assert valid == (name in good)
+            lines = r.stdout.strip().split("\n")
+            assert all(("error" not in ln) == valid for ln in lines), (name, where, lines)
 
 
 @pytest.mark.parametrize("zlib", [True, False])
@@ -131,4 +158,17 @@ def test_cpu_writer_under_sanitizers(tmp_path, pkg):
                            capture_output=True, text=True, timeout=600)
         assert r.returncode == 0, r.stderr[-3000:]
         assert r.stdout == oracle.write_matrix(ids, H, osep=osep, index_name=index_name, mode=mode, cap=cap), mode
+
+
+def test_row_parser_matches_the_per_cell_parse(tmp_path, pkg):
+    """The CLI's fused row parser (a fast path for plain digit cells) gives the
+    values, verdict and first bad cell of the per-cell parse on 36 000 random
+    rows of adversarial cells, for two separators, three missing tokens (one
+    all digits) and both INF- settings."""
+    lib_dir = os.path.join(PKG_DIR, "lib")
+    exe = build(tmp_path, "parse_row_check", [os.path.join(ROOT, "tests", "sanitize", "parse_row_check.cpp")],
+                extra=["-I", os.path.join(PKG_DIR, "host"), "-L", lib_dir, "-ltch", "-ldl",
+                       f"-Wl,-rpath,{lib_dir}"])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "parse_row ok" in r.stdout, r.stdout + r.stderr[-3000:]
 
