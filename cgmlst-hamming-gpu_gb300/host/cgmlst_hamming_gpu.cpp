@@ -617,27 +617,44 @@ void on_stripe(void* ctx, int r0, int rows, size_t w, const uint16_t* stripe) {
     });
 }
 
-inline uint16_t at(const std::vector<std::vector<uint16_t>>& upper, size_t i, size_t j) {
-    if (i == j) return 0;
-    if (j > i) return upper[i][j - i - 1];
-    return upper[j][i - j - 1];
-}
-
-inline void put_int(std::string& b, int v) {
-    char tmp[16];
-    int k = 0;
-    bool neg = v < 0;
-    unsigned u = neg ? 0u - (unsigned)v : (unsigned)v;
-    do {
-        tmp[k++] = (char)('0' + u % 10);
-        u /= 10;
-    } while (u);
-    if (neg) tmp[k++] = '-';
-    while (k) b.push_back(tmp[--k]);
+// A distance (0-65 535) in decimal at p, two digits per table lookup; returns
+// the end.
+inline char* put_u16(char* p, unsigned v) {
+    static const char d2[] =
+        "00010203040506070809101112131415161718192021222324252627282930313233343536373839"
+        "40414243444546474849505152535455565758596061626364656667686970717273747576777879"
+        "8081828384858687888990919293949596979899";
+    if (v < 10) {
+        *p = (char)('0' + v);
+        return p + 1;
+    }
+    if (v < 100) {
+        memcpy(p, d2 + 2 * v, 2);
+        return p + 2;
+    }
+    if (v >= 10000) {
+        *p++ = (char)('0' + v / 10000);
+        v %= 10000;
+        memcpy(p, d2 + 2 * (v / 100), 2);
+        memcpy(p + 2, d2 + 2 * (v % 100), 2);
+        return p + 4;
+    }
+    if (v >= 1000) {
+        memcpy(p, d2 + 2 * (v / 100), 2);
+        memcpy(p + 2, d2 + 2 * (v % 100), 2);
+        return p + 4;
+    }
+    *p = (char)('0' + v / 100);
+    memcpy(p + 1, d2 + 2 * (v % 100), 2);
+    return p + 3;
 }
 
 // write_matrix (main.rs:225-265): header, then rows formatted in parallel
-// chunks of 1024 and written in order.
+// chunks of 1024 and written in order.  A row is written through a pointer
+// into a buffer sized for its longest text (id, then per cell the separator
+// and at most five digits), reused for every chunk: cells left of the
+// diagonal come from the earlier rows' upper parts, cells right of it from the
+// row's own, and cells the layout blanks are 0.
 template <class W>
 void write_matrix(W& out, const std::vector<std::string>& ids, const std::vector<std::vector<uint16_t>>& upper,
                   const std::string& osep, const std::string& index_name, Layout lay, int cap, size_t threads) {
@@ -649,28 +666,50 @@ void write_matrix(W& out, const std::vector<std::string>& ids, const std::vector
     }
     head += '\n';
     out.write(head.data(), head.size());
-    const size_t CHUNK = 1024;
-    std::vector<std::string> bufs;
+    const size_t CHUNK = 1024, sl = osep.size();
+    size_t maxid = 0;
+    for (auto& id : ids) maxid = std::max(maxid, id.size());
+    const size_t cap_row = maxid + n * (sl + 5) + 1;
+    const size_t rows_buf = std::min(n, CHUNK);
+    std::unique_ptr<char[]> text(new char[std::max<size_t>(rows_buf * cap_row, 1)]);
+    std::vector<size_t> len(rows_buf);
+    const unsigned vcap = cap > 0 ? (unsigned)cap : 65535u;
     for (size_t start = 0; start < n; start += CHUNK) {
         const size_t end = std::min(n, start + CHUNK);
-        bufs.assign(end - start, std::string());
         parallel_for(threads, end - start, 8, [&](size_t a, size_t b) {
             for (size_t q = a; q < b; q++) {
                 const size_t i = start + q;
-                std::string& buf = bufs[q];
-                buf.reserve((n + 1) * 7);
-                buf += ids[i];
-                for (size_t j = 0; j < n; j++) {
-                    buf += osep;
-                    const bool keep = lay == Layout::Full ? true : lay == Layout::LowerTri ? j <= i : j >= i;
-                    int v = keep ? (int)at(upper, i, j) : 0;
-                    if (cap > 0 && v > cap) v = cap;
-                    put_int(buf, v);
+                char* const row = text.get() + q * cap_row;
+                char* p = row;
+                memcpy(p, ids[i].data(), ids[i].size());
+                p += ids[i].size();
+                auto sep = [&]() {
+                    if (sl == 1) *p++ = osep[0];
+                    else {
+                        memcpy(p, osep.data(), sl);
+                        p += sl;
+                    }
+                };
+                // columns j < i (blank in the upper-tri layout)
+                for (size_t j = 0; j < i; j++) {
+                    sep();
+                    const unsigned v = lay == Layout::UpperTri ? 0u : upper[j][i - j - 1];
+                    p = put_u16(p, std::min(v, vcap));
                 }
-                buf += '\n';
+                sep();  // the diagonal
+                *p++ = '0';
+                // columns j > i (blank in the lower-tri layout)
+                const uint16_t* u = upper[i].data();
+                for (size_t j = i + 1; j < n; j++) {
+                    sep();
+                    const unsigned v = lay == Layout::LowerTri ? 0u : u[j - i - 1];
+                    p = put_u16(p, std::min(v, vcap));
+                }
+                *p++ = '\n';
+                len[q] = (size_t)(p - row);
             }
         });
-        for (auto& b : bufs) out.write(b.data(), b.size());
+        for (size_t q = 0; q < end - start; q++) out.write(text.get() + q * cap_row, len[q]);
     }
 }
 
