@@ -92,7 +92,7 @@ extern "C" {
 int tch_dense_ranks(const uint64_t* calls, int n, int L, uint16_t* x, uint32_t* n_distinct, int threads,
                     char* err, int errlen) {
     if (n < 0 || L < 0) return set_err(err, errlen, "negative size");
-    if ((size_t)n * L && (!calls || !x || !n_distinct)) return set_err(err, errlen, "null buffer");
+    if ((size_t)n * L != 0 && (!calls || !x || !n_distinct)) return set_err(err, errlen, "null buffer");
     std::atomic<int> bad_locus{-1};
     std::atomic<size_t> bad_count{0};
     parallel_for(threads, (size_t)L, 1, [&](size_t kb, size_t ke) {
@@ -232,19 +232,28 @@ int tch_encode_host(const uint16_t* x, const uint32_t* nd, int n, int L, int tau
                 }
         });
     }
-    // partners per row (main.rs:418-433)
-    std::vector<std::atomic<uint64_t>> counts((size_t)n);
-    for (auto& v : counts) v.store(0, std::memory_order_relaxed);
-    parallel_for(threads, c.cnt.size(), 1024, [&](size_t q0, size_t q1) {
-        for (size_t q = q0; q < q1; q++) {
-            const size_t g0 = goff[q], g1 = goff[q + 1];
-            for (size_t a = g0; a < g1; a++) counts[members[a]].fetch_add(g1 - 1 - a, std::memory_order_relaxed);
+    // partners per row (main.rs:418-433): row i's partners at locus k are the
+    // members of its group after its own entry (groups list rows ascending);
+    // its place in a group is found by binary search
+    auto own_place = [&](size_t g0, size_t g1, uint32_t i) {
+        return (size_t)(std::lower_bound(members.begin() + g0, members.begin() + g1, i) - members.begin());
+    };
+    std::vector<uint64_t> rowcnt((size_t)n, 0);
+    parallel_for(threads, (size_t)n, 64, [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; i++) {
+            uint64_t sum = 0;
+            for (int k = 0; k < L; k++) {
+                const int a = x[i * L + k];
+                const size_t q = c.off[k] + a, g0 = goff[q], g1 = goff[q + 1];
+                if (a && g1 > g0) sum += g1 - 1 - own_place(g0, g1, (uint32_t)i);
+            }
+            rowcnt[i] = sum;
         }
     });
     uint64_t n_rare = 0;
     for (int i = 0; i < n; i++) {
         out->start[i] = (uint32_t)n_rare;
-        n_rare += counts[i].load(std::memory_order_relaxed);
+        n_rare += rowcnt[i];
         if (n_rare >= (1ull << 32)) {
             tch_host_encoding_free(out);
             return set_err(err, errlen, "too many rare pairs: raise --tau");
@@ -257,22 +266,61 @@ int tch_encode_host(const uint16_t* x, const uint32_t* nd, int n, int L, int tau
         tch_host_encoding_free(out);
         return set_err(err, errlen, "out of host memory");
     }
-    {
-        std::vector<std::atomic<uint32_t>> fill((size_t)n);
-        for (int i = 0; i < n; i++) fill[i].store(out->start[i], std::memory_order_relaxed);
-        parallel_for(threads, c.cnt.size(), 1024, [&](size_t q0, size_t q1) {
-            for (size_t q = q0; q < q1; q++) {
-                const size_t g0 = goff[q], g1 = goff[q + 1];
-                for (size_t a = g0; a < g1; a++)
-                    for (size_t b = a + 1; b < g1; b++)
-                        out->js[fill[members[a]].fetch_add(1, std::memory_order_relaxed)] = members[b];
+    // each row's list, ascending, a partner repeated once per shared rare
+    // allele: the row's partners are counted in a per-thread array over the
+    // columns, then emitted in column order — by sorting the distinct partners
+    // when the row has few partners against its width, by a scan of the width
+    // otherwise (the row's partner count decides, before any is counted)
+    std::atomic<bool> mismatch{false};
+    parallel_for(threads, (size_t)n, 64, [&](size_t i0, size_t i1) {
+        std::vector<uint32_t> cnt((size_t)n, 0), touched;
+        for (size_t i = i0; i < i1; i++) {
+            const bool few = rowcnt[i] * 16 < (uint64_t)n - i;
+            touched.clear();
+            for (int k = 0; k < L; k++) {
+                const int a = x[i * L + k];
+                const size_t q = c.off[k] + a, g0 = goff[q], g1 = goff[q + 1];
+                if (!a || g1 == g0) continue;
+                const size_t b0 = own_place(g0, g1, (uint32_t)i) + 1;
+                if (few) {
+                    for (size_t b = b0; b < g1; b++)
+                        if (cnt[members[b]]++ == 0) touched.push_back(members[b]);
+                } else {
+                    for (size_t b = b0; b < g1; b++) cnt[members[b]]++;
+                }
             }
-        });
-    }
-    // ascending partners per row
-    parallel_for(threads, (size_t)n, 256, [&](size_t i0, size_t i1) {
-        for (size_t i = i0; i < i1; i++) std::sort(out->js + out->start[i], out->js + out->start[i + 1]);
+            uint32_t* w = out->js + out->start[i];
+            auto emit = [&](uint32_t j) {
+                for (uint32_t r = cnt[j]; r; r--) *w++ = j;
+                cnt[j] = 0;
+            };
+            if (few) {
+                std::sort(touched.begin(), touched.end());
+                for (uint32_t j : touched) emit(j);
+            } else {
+                // branch-free for counts 0 and 1: the column is always stored
+                // and the end advances by the count (a store at the end of the
+                // row's slice lands in a scratch word instead)
+                uint32_t* const end = out->js + out->start[i + 1];
+                uint32_t scratch;
+                for (size_t j = i + 1; j < (size_t)n; j++) {
+                    const uint32_t cj = cnt[j];
+                    if (cj <= 1) {
+                        *(w < end ? w : &scratch) = (uint32_t)j;
+                        w += cj;
+                        cnt[j] = 0;
+                    } else {
+                        emit((uint32_t)j);
+                    }
+                }
+            }
+            if (w != out->js + out->start[i + 1]) mismatch = true;
+        }
     });
+    if (mismatch) {
+        tch_host_encoding_free(out);
+        return set_err(err, errlen, "internal error: rare partner lists do not match their counts");
+    }
     return 0;
 }
 
