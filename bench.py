@@ -24,9 +24,17 @@ n (n - 1) / 2 = 1 984 783 510 exact pairs.
            (the C restatement in oracle/), all host threads, bounded sample.
 
 --impl reference runs that CPU brute force alone (the reference's CPU path
-for the matrix) and prints its line.  Under torchrun each rank computes a
-balanced share of the rows (equal pair counts, no collective on the data
-path); value = all pairs / max time over ranks.
+for the matrix, restated in C in oracle/) on every host thread and prints its
+line; it loads nothing of the package: the profiles come from synth.py loaded
+by file path and are ranked by the oracle.  Each of its steps counts the rows
+k, k + s, k + 2 s, ... of the upper triangle (a sample spread over the whole
+triangle; s consecutive steps cover every row once), and value = pairs
+counted / seconds over the timed steps.
+
+Only one-GPU runs are offered: the tile pass may share operand tiles between
+the CTAs of a cluster by TMA multicast, which is valid within one GPU's
+memory only, so under torchrun with WORLD_SIZE > 1 the GPU arm refuses to run
+(the reference arm runs on rank 0 and the other ranks exit).
 """
 from __future__ import annotations
 
@@ -46,6 +54,7 @@ sys.path.insert(0, ROOT)
 PKG = "cgmlst-hamming-gpu_gb300"
 
 METRIC = "exact_pairs_per_s"
+DTYPE = "fp8(e4m3 0/1) -> fp32 exact ints -> u16"
 UNIT = "pairs/s"
 
 
@@ -60,15 +69,95 @@ def dist_env():
     return ws, rank, local
 
 
-def row_shares(n: int, ws: int):
-    """Row ranges [a, b) with about equal upper-triangle pair counts."""
-    cum = np.cumsum(np.arange(n - 1, -1, -1, dtype=np.float64))
-    total = cum[-1]
-    bounds = [0]
-    for r in range(1, ws):
-        bounds.append(int(np.searchsorted(cum, total * r / ws)))
-    bounds.append(n)
-    return [(bounds[i], bounds[i + 1]) for i in range(ws)]
+def workload_config(n: int, L: int) -> dict:
+    """The workload as both arms name it (the same dict in both lines)."""
+    return {"workload": f"long-tail outbreak profiles {n} x {L} (synthetic, seeded)", "n": n, "loci": L,
+            "pairs": n * (n - 1) // 2,
+            "l2": "inputs larger than L2 (operands ~1 GB, rare groups and per-step rare counts of several GB)"}
+
+
+def load_synth():
+    """synth.py by file path: the generator without importing the package."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("tch_synth", os.path.join(ROOT, PKG, "synth.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def load_oracle():
+    d = os.path.join(ROOT, "oracle")
+    if d not in sys.path:
+        sys.path.insert(0, d)
+    import oracle
+
+    return oracle
+
+
+def cpu_count_steps(x: np.ndarray, stride: int, k0: int, steps: int):
+    """The oracle's brute-force count (all host threads) over the rows k,
+    k + stride, ... of the upper triangle for k = k0 .. k0 + steps - 1 (mod
+    stride), one call per step.  Returns (pairs, seconds)."""
+    import ctypes
+
+    lib = load_oracle().lib()
+    n, L = x.shape
+    x = np.ascontiguousarray(x, dtype=np.uint16)
+    xp = x.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16))
+    pairs, secs = 0, 0.0
+    for k in range(k0, k0 + steps):
+        acc = ctypes.c_uint64(0)
+        t = time.perf_counter()
+        pairs += lib.orc_upper_rows_step(xp, n, L, k % stride, stride, ctypes.byref(acc), 0)
+        secs += time.perf_counter() - t
+    return pairs, secs
+
+
+def reference_arm(args) -> dict:
+    """The reference's CPU path for the matrix (the brute-force count of
+    tensorcore/rs/check.py:39-44, restated in C with OpenMP), all host
+    threads, rows k, k + s, ... per step."""
+    import ctypes
+
+    oracle = load_oracle()
+    synth = load_synth()
+    t0 = time.perf_counter()
+    A = synth.longtail(n=args.n, L=args.L)
+    x, _ = oracle.dense_ranks(A)
+    n, L = x.shape
+    log(f"reference arm: generated + ranked {n}x{L} in {time.perf_counter() - t0:.1f}s")
+    s = max(1, args.ref_stride)
+    cpu_count_steps(x, s, 0, args.warmup)
+    pairs, secs = cpu_count_steps(x, s, args.warmup, args.steps)
+    v = pairs / secs
+    threads = oracle.lib().orc_num_threads()
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / max(args.steps, 1) * 1e3,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "u16",
+            "data": "synthetic", "config": workload_config(n, L),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"brute-force count (check.py:39-44 restated in C, OpenMP, {threads} threads) "
+                                       f"over rows k, k+{s}, k+{2 * s}, ... of the upper triangle per step "
+                                       f"(~1/{s} of its pairs; {s} consecutive steps cover every row); "
+                                       f"{pairs} pairs in {secs:.1f} s over {args.steps} steps"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def parity_rows(x: np.ndarray, out, rows: int = 256) -> dict:
+    """Spread rows i of the device output (row i at out[i], column j at
+    out[i, j]) against the oracle's count for every j in (i, n)."""
+    oracle = load_oracle()
+    n = x.shape[0]
+    idx = sorted(set(np.linspace(0, n - 2, rows).astype(int).tolist()) | {0, n - 2})
+    cells = bad = 0
+    for i in idx:
+        got = out[i, i + 1:n].cpu().numpy().view(np.uint16)
+        want = oracle.hamming_block(x, i, i + 1, i + 1, n)[0]
+        cells += got.size
+        bad += int((got != want).sum())
+    return {"rows": len(idx), "cells": cells, "mismatches": bad,
+            "oracle": "orc_hamming_block (check.py:39-44 restated in C)"}
 
 
 class Clocks:
@@ -121,45 +210,18 @@ def measured_peaks():
     return None
 
 
-def tc_fp8_peak(tch):
-    """Measured tcgen05 kind::f8f6f4 MMA rate of this GPU (tch-peak probe)."""
+def tc_peaks():
+    """Measured rates of this GPU's arithmetic paths (the tch-peak probe).
+    The fp4 probe runs in a process of its own."""
     exe = os.path.join(ROOT, PKG, "bin", "tch-peak")
-    try:
-        out = subprocess.run([exe], capture_output=True, text=True, timeout=120).stdout
-        return json.loads(out.strip().splitlines()[-1])
-    except Exception as e:  # noqa: BLE001
-        log("peak probe failed:", e)
-        return {}
-
-
-def cpu_sample(x: np.ndarray, target_s: float, threads: int = 0):
-    """The oracle's brute-force count on the first rows of the upper triangle,
-    sized to about target_s seconds.  Returns (pairs/s, pairs, rows, secs)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import ctypes
-
-    import oracle
-
-    lib = oracle.lib()
-    n, L = x.shape
-    xp = x.ctypes.data_as(ctypes.POINTER(ctypes.c_uint16))
-    s = ctypes.c_uint64(0)
-    rows = 16
-    t = time.perf_counter()
-    pairs = lib.orc_upper_rows(xp, n, L, 0, rows, ctypes.byref(s), threads)
-    dt = time.perf_counter() - t
-    rate = pairs / max(dt, 1e-9)
-    want_pairs = rate * target_s
-    # rows from the top of the triangle: row i has n - 1 - i pairs
-    r1 = rows
-    acc = 0
-    while r1 < n and acc < want_pairs:
-        acc += n - 1 - r1
-        r1 += 1
-    t = time.perf_counter()
-    pairs = lib.orc_upper_rows(xp, n, L, rows, r1, ctypes.byref(s), threads)
-    dt = time.perf_counter() - t
-    return pairs / dt, int(pairs), (rows, r1), dt
+    res = {}
+    for paths in (["b1", "s8", "e4m3", "popc", "tc_f8"], ["tc_f4"]):
+        try:
+            out = subprocess.run([exe, *paths], capture_output=True, text=True, timeout=120).stdout
+            res.update(json.loads(out.strip().splitlines()[-1]))
+        except Exception as e:  # noqa: BLE001
+            log("peak probe failed:", paths, e)
+    return res
 
 
 def time_whole(tch, A, tau, device, out, ldo, stream, reps=3):
@@ -306,22 +368,8 @@ def batch_bench(tch, args, device):
     with the autotuned schedule and tau chosen per matrix."""
     import torch
 
-    rng = np.random.default_rng(21)
-    b = tch.Batch(device=device)
-    pairs = 0
-    build_s = 0.0
-    for _ in range(args.batch_count):
-        n = int(np.exp(rng.uniform(np.log(50), np.log(5000))))
-        L = int(rng.choice([1142, 1343, 2794, 3016]))
-        s = float(rng.uniform(1.0, 1.4))
-        k = np.clip(np.rint(rng.lognormal(np.log(40.0), 1.0, L)), 2, 500).astype(np.int64)
-        a = (rng.zipf(max(s, 1.01), size=(n, L)) - 1) % k[None, :]
-        A = (np.arange(L, dtype=np.uint64)[None, :] << np.uint64(20)) + a.astype(np.uint64) + np.uint64(1)
-        A[rng.random((n, L)) < rng.uniform(0.0, 0.08)] = 0
-        t0 = time.perf_counter()
-        b.add(A)  # device encoding (tau per matrix)
-        build_s += time.perf_counter() - t0
-        pairs += n * (n - 1) // 2
+    b, shapes, build_s = batch_sets(tch, args.batch_count, device)
+    pairs = sum(n * (n - 1) // 2 for n, _ in shapes)
     off, ld = b.layout()
     out = torch.empty(int(off[-1]) + 8, dtype=torch.int16, device=f"cuda:{device}")
     stream = torch.cuda.Stream(device=device)
@@ -348,6 +396,91 @@ def batch_bench(tch, args, device):
             "encode_s": build_s, "tune_s": tune_s}
 
 
+def step_timing(tch, synth, args, device):
+    """--step-timing: the two passes of one whole-triangle solve of the
+    long-tail generator at --n profiles and --tau (rare counts, then the tile
+    pass), timed apart with CUDA events, --reps times.  The small case the
+    kernel profiles are captured on: one launch of each kernel per rep."""
+    import torch
+
+    n = args.n
+    A = synth.longtail(n=n, L=args.L)
+    with tch.Solver.from_calls(A, tau=args.tau, kernel=args.kernel, device=device) as s:
+        info = s.info()
+        log(info)
+        ldr = (n + 255) // 256 * 256
+        ldo = (n + 7) // 8 * 8
+        R = torch.empty((n, ldr), dtype=torch.int16, device=f"cuda:{device}")
+        out = torch.empty((n, ldo), dtype=torch.int16, device=f"cuda:{device}")
+        st = torch.cuda.current_stream().cuda_stream
+        for _ in range(args.reps):
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record()
+            s.rare_counts(0, n, R.data_ptr(), ldr, st)
+            e1.record()
+            s.stripe_counts(0, n, out.data_ptr(), ldo, R.data_ptr(), ldr, st)
+            e2.record()
+            torch.cuda.synchronize()
+            rare_ms, tile_ms = e0.elapsed_time(e1), e1.elapsed_time(e2)
+            print(f"rare counts {rare_ms:.3f} ms  tile pass {tile_ms:.3f} ms  "
+                  f"{info['n_rare'] / rare_ms * 1e3:.3e} rare pairs/s", flush=True)
+        s.check()
+
+
+def batch_sets(tch, count, device):
+    """The batched leg's generator: count sets, n log-uniform in [50, 5 000],
+    L from {1 142, 1 343, 2 794, 3 016}, Zipf s in [1.0, 1.4] over lognormal
+    distinct counts, 0-8 % missing (seed 21), added to a new tch.Batch."""
+    rng = np.random.default_rng(21)
+    b = tch.Batch(device=device)
+    shapes = []
+    build_s = 0.0
+    for _ in range(count):
+        n = int(np.exp(rng.uniform(np.log(50), np.log(5000))))
+        L = int(rng.choice([1142, 1343, 2794, 3016]))
+        s = float(rng.uniform(1.0, 1.4))
+        k = np.clip(np.rint(rng.lognormal(np.log(40.0), 1.0, L)), 2, 500).astype(np.int64)
+        a = (rng.zipf(max(s, 1.01), size=(n, L)) - 1) % k[None, :]
+        A = (np.arange(L, dtype=np.uint64)[None, :] << np.uint64(20)) + a.astype(np.uint64) + np.uint64(1)
+        A[rng.random((n, L)) < rng.uniform(0.0, 0.08)] = 0
+        t0 = time.perf_counter()
+        b.add(A)  # device encoding (tau per matrix)
+        build_s += time.perf_counter() - t0
+        shapes.append((n, L))
+    return b, shapes, build_s
+
+
+def batch_timing(tch, args, device):
+    """--batch-timing: one batched solve with a fixed schedule (--branches,
+    --cluster): CUDA-event time of a graph replay (median of 5 after 3
+    untimed) and the largest sets with their tau."""
+    import torch
+
+    b, shapes, _ = batch_sets(tch, args.batch_count, device)
+    off, _ = b.layout()
+    out = torch.empty(int(off[-1]) + 8, dtype=torch.int16, device=f"cuda:{device}")
+    st = torch.cuda.Stream(device=device)
+    b.set_schedule(args.branches, args.cluster, args.cluster)
+    for _ in range(3):
+        b.run(out.data_ptr(), st.cuda_stream)
+    ms = []
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        b.run(out.data_ptr(), st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    b.check()
+    taus = b.info()["taus"]
+    pairs = [n * (n - 1) // 2 for n, _ in shapes]
+    print(f"ms per batch {sorted(ms)[len(ms) // 2]:.3f} ({sum(pairs)} pairs, {args.batch_count} sets, "
+          f"{args.branches} branches, cluster {args.cluster})", flush=True)
+    for i in sorted(range(len(shapes)), key=lambda i: -pairs[i])[:8]:
+        print(f"  set {i}: n {shapes[i][0]} L {shapes[i][1]} tau {taus[i]}", flush=True)
+    b.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -358,7 +491,7 @@ def main():
     ap.add_argument("--tau", type=int, default=0, help="0 = the analytic GB300 model's choice")
     ap.add_argument("--stripe", type=int, default=4096, help="rows per stripe of the e2e tch_run call")
     ap.add_argument("--e2e-steps", type=int, default=5, help="timed e2e passes; the median is reported")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-steps", type=int, default=4, help="CPU baseline: steps of the reference arm's sample")
     ap.add_argument("--n", type=int, default=63005)
     ap.add_argument("--L", type=int, default=1142)
     ap.add_argument("--no-cpu", action="store_true")
@@ -371,14 +504,40 @@ def main():
     ap.add_argument("--serve-db", type=int, default=200000)
     ap.add_argument("--serve-requests", type=int, default=100)
     ap.add_argument("--serving-only", action="store_true", help="run the serving leg alone and print its JSON")
+    ap.add_argument("--step-timing", action="store_true",
+                    help="time the rare counts and the tile pass of one solve of --n profiles at --tau, --reps times")
+    ap.add_argument("--batch-timing", action="store_true",
+                    help="time one batched replay of --batch-count sets with --branches and --cluster")
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--branches", type=int, default=32)
+    ap.add_argument("--cluster", type=int, default=1)
+    ap.add_argument("--ref-stride", type=int, default=6,
+                    help="reference arm: rows k, k + s, ... of the triangle per step")
+    ap.add_argument("--parity-rows", type=int, default=256,
+                    help="spread rows of the timed output compared with the oracle")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
     ws, rank, local = dist_env()
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(reference_arm(args)), flush=True)
+        return
+    if ws > 1:
+        log("bench.py: this build offers one-GPU runs only (the tile pass may use TMA multicast within a "
+            "thread-block cluster, valid in one GPU's memory); run it without torchrun")
+        sys.exit(2)
+
     tch = importlib.import_module(PKG)
     synth = importlib.import_module(PKG + ".synth")
     if args.serving_only:  # a service runs in its own process
         print(json.dumps(serving_bench(tch, synth, args, local)), flush=True)
+        return
+    if args.step_timing:
+        step_timing(tch, synth, args, local)
+        return
+    if args.batch_timing:
+        batch_timing(tch, args, local)
         return
 
     t0 = time.perf_counter()
@@ -386,39 +545,11 @@ def main():
     x, nd = tch.dense_ranks(A)
     n, L = x.shape
     pairs_total = n * (n - 1) // 2
-    workload = {"workload": f"long-tail outbreak profiles {n} x {L} (synthetic, seeded)", "n": n, "loci": L,
-                "pairs": pairs_total, "tau": args.tau, "l2": "inputs larger than L2 (operands ~1 GB + 8 GB rare counts per step)"}
+    workload = workload_config(n, L)
     log(f"generated + ranked {n}x{L} in {time.perf_counter() - t0:.1f}s")
-
-    if args.impl == "reference":
-        if rank != 0:
-            return
-        threads = os.cpu_count() or 1
-        vals = []
-        for _ in range(args.warmup):  # short untimed samples (~1 s each)
-            cpu_sample(x, 1.0, 0)
-        for _ in range(args.steps):
-            rate, pairs, rows, dt = cpu_sample(x, args.cpu_seconds / max(args.steps, 1), 0)
-            vals.append(rate)
-        v = statistics.median(vals)
-        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": pairs_total / v * 1e3,
-                "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "u16",
-                "data": "synthetic", "config": workload,
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                 "sample": f"brute-force count (check.py:39-44 restated in C, OpenMP) over the "
-                                           f"first upper-triangle rows, ~{args.cpu_seconds / max(args.steps, 1):.0f} s "
-                                           f"per step; ms_per_step extrapolates to all {pairs_total} pairs"},
-                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return
 
     import torch
 
-    if ws > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     device = local
     torch.cuda.set_device(device)
     assert tch.device_count() > 0
@@ -435,11 +566,9 @@ def main():
     solver = tch.Solver.from_calls(A, tau=args.tau, kernel=args.kernel, device=device)  # device encoder
     info = solver.info()
     tau = info["tau"]
-    workload["tau"] = tau
     log(f"device-encoded tau={tau}: D={info['d_onehot']} n_rare={info['n_rare']} in "
         f"{time.perf_counter() - t0:.1f}s", info)
-    shares = row_shares(n, ws)
-    a, b = shares[rank]
+    a, b = 0, n
     ldo = (n + 7) // 8 * 8
     out = torch.empty(((b - a), ldo), dtype=torch.int16, device=f"cuda:{device}")
     stream = torch.cuda.Stream(device=device)
@@ -456,8 +585,6 @@ def main():
     clocks = Clocks(device)
     clocks.start()
     time.sleep(0.3)
-    if ws > 1:
-        torch.distributed.barrier()
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -470,18 +597,15 @@ def main():
         evs[k][1].record(stream)
     ev1.record(stream)
     torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
     ck = clocks.stop()
     solver.check()
     total_ms = ev0.elapsed_time(ev1)
     launch_ms = [s.elapsed_time(e) for s, e in evs]
-    if ws > 1:
-        tt = torch.tensor([total_ms], device=f"cuda:{device}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt.item())
     ms_per_step = total_ms / args.steps
     value = pairs_total / (ms_per_step / 1e3)
+    # the last timed step's output against the oracle on spread rows
+    parity = parity_rows(load_oracle().dense_ranks(A)[0], out, args.parity_rows) if args.parity_rows else None
+    log("parity:", parity)
 
     # a dense-rare solver's step is two launches: the stripe's rare counts,
     # then the tile pass that subtracts them; time them apart for the roofline
@@ -513,7 +637,7 @@ def main():
     my_pairs = sum(n - 1 - i for i in range(a, b))
     ops_per_launch = 2.0 * my_pairs * k_alg
     achieved = ops_per_launch / (tc_ms / 1e3) / 1e12
-    peak_info = tc_fp8_peak(tch) if rank == 0 else {}
+    peak_info = tc_peaks()
     mp = measured_peaks()
     peak = peak_info.get("tc_f8_tflops")
     peak_src = "tch-peak tcgen05 kind::f8f6f4 probe on this GPU"
@@ -528,7 +652,7 @@ def main():
     # DRAM bytes of one whole-triangle tile pass, from the ncu capture of this
     # workload (valid for the tau and row share it was taken at)
     prof = os.path.join(ROOT, "profiles", "tc_stripe_longtail_traffic.txt")
-    if os.path.exists(prof) and ws == 1:
+    if os.path.exists(prof):
         with open(prof) as f:
             kv = dict(line.split(":", 1) for line in f if ":" in line)
         if int(kv.get("tau", "0")) == tau and int(kv.get("n", "0")) == n:
@@ -541,7 +665,7 @@ def main():
     # run slower after the legs that pin and release gigabytes of it
     e2e = None
     e2e_calls = None
-    if rank == 0 and args.e2e_steps > 0:
+    if args.e2e_steps > 0:
         import ctypes
 
         os.environ["TCH_VERBOSE"] = "1"  # phase breakdown on stderr
@@ -597,7 +721,7 @@ def main():
     # legs and before the legs that churn host memory (large copies from host
     # memory slow down after them)
     serving = None
-    if rank == 0 and ws == 1 and not args.no_serving:
+    if not args.no_serving:
         r = subprocess.run([sys.executable, os.path.abspath(__file__), "--serving-only",
                             "--serve-db", str(args.serve_db), "--serve-requests", str(args.serve_requests)],
                            capture_output=True, text=True, env=dict(os.environ, CUDA_VISIBLE_DEVICES=str(device)))
@@ -610,7 +734,7 @@ def main():
     # learned vs analytic tau: whole-triangle device time at each pick and at
     # a sweep of taus around them (fresh solvers)
     tau_cmp = None
-    if rank == 0 and ws == 1 and not args.no_tau_sweep:
+    if not args.no_tau_sweep:
         swept = {int(tau): ms_per_step}
         cands = {512, 1024, 2048, 4096, 8192} | set(tau_pick.values())
         for t in sorted(cands):
@@ -627,7 +751,7 @@ def main():
     # the reference's TSV writer (main.rs:224-265) on the GPU: the full matrix
     # as text, delivered block by block to a callback that discards it
     tsv = None
-    if rank == 0 and ws == 1 and not args.no_tsv:
+    if not args.no_tsv:
         import ctypes
 
         nbytes = [0]
@@ -654,7 +778,7 @@ def main():
         log("tsv writer:", tsv)
 
     batched = None
-    if rank == 0 and ws == 1 and not args.no_batch:
+    if not args.no_batch:
         solver.close()
         del out
         torch.cuda.empty_cache()
@@ -662,26 +786,25 @@ def main():
         log("batched:", batched)
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
-        rate, pairs, rows, dt = cpu_sample(x, args.cpu_seconds, 0)
-        cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": f"oracle brute force (check.py:39-44 in C, OpenMP) on rows {rows[0]}-{rows[1]} of the upper "
-                         f"triangle: {pairs} pairs in {dt:.1f} s"}
+    if not args.no_cpu:
+        st = max(1, args.ref_stride)
+        cpu_steps = max(1, min(st, args.cpu_steps))
+        pairs, dt = cpu_count_steps(x, st, 0, cpu_steps)
+        threads = load_oracle().lib().orc_num_threads()
+        cpu = {"value": pairs / dt, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"oracle brute force (check.py:39-44 in C, OpenMP, {threads} threads) over rows k, k+{st}, "
+                         f"... of the upper triangle for k = 0..{cpu_steps - 1}: {pairs} pairs in {dt:.1f} s"}
 
-    if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-                "scaling": "strong", "vs_baseline": None, "dtype": "fp8(e4m3 0/1) -> fp32 exact ints -> u16",
-                "data": "synthetic", "config": dict(workload, kernel=info["kernel"], stripe_e2e=args.stripe,
-                                                    parallelism=f"row shares x{ws}"),
-                "gpu_launches": args.steps * launches_per_step, "step_split": split,
-                "clocks": ck, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "e2e_device_encoder": e2e_calls, "tau_choice": tau_cmp, "tsv_writer": tsv, "batched": batched, "serving": serving,
-                "peak_probe": peak_info}
-        print(json.dumps(line), flush=True)
-    if ws > 1:
-        solver.close()
-        torch.distributed.destroy_process_group()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": DTYPE,
+            "data": "synthetic", "config": workload,
+            "solver": {"tau": tau, "kernel": info["kernel"], "stripe_e2e": args.stripe, "rows_per_step": n},
+            "gpu_launches": args.steps * launches_per_step, "step_split": split, "parity": parity,
+            "clocks": ck, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "e2e_device_encoder": e2e_calls, "tau_choice": tau_cmp, "tsv_writer": tsv, "batched": batched,
+            "serving": serving, "peak_probe": peak_info}
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

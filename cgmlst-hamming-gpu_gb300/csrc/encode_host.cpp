@@ -273,7 +273,11 @@ int tch_encode_host(const uint16_t* x, const uint32_t* nd, int n, int L, int tau
     // otherwise (the row's partner count decides, before any is counted)
     std::atomic<bool> mismatch{false};
     parallel_for(threads, (size_t)n, 64, [&](size_t i0, size_t i1) {
-        std::vector<uint32_t> cnt((size_t)n, 0), touched;
+        // one counter array per worker thread, sized once: emission resets
+        // every entry it touched to 0, so it is clean for the next chunk
+        thread_local std::vector<uint32_t> cnt;
+        thread_local std::vector<uint32_t> touched;
+        if (cnt.size() < (size_t)n) cnt.assign((size_t)n, 0);
         for (size_t i = i0; i < i1; i++) {
             const bool few = rowcnt[i] * 16 < (uint64_t)n - i;
             touched.clear();

@@ -36,7 +36,6 @@ namespace {
 static __device__ __align__(256) uint8_t g_noalloc_scratch[TCH_NOALLOC_SCRATCH_BYTES];
 
 constexpr size_t kErrBytes = 256;
-constexpr int kMaxDevices = 64;
 
 std::mutex g_mu;
 uint8_t* g_addr[kMaxDevices];  // device address of g_noalloc_scratch, per device
@@ -60,6 +59,26 @@ __global__ void check_offsets_kernel(const uint32_t* __restrict__ start, int n, 
         const uint32_t a = start[i], b = start[i + 1];
         if (a > b || (size_t)b > n_rare) atomicOr(err, DEVERR_RARE_PAIR);
     }
+}
+
+// Makes `device` current for the call and gives the caller's device back on
+// every return.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t set(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        return cudaSetDevice(device);
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+// An error after work was queued: wait for that work first, so that no
+// kernel of this call still uses the shared array when the caller retries.
+int fail_queued(cudaStream_t st, Err& e, const char* what, cudaError_t ce) {
+    cudaStreamSynchronize(st);
+    return e.set("%s: %s", what, cudaGetErrorString(ce));
 }
 
 int read_error(int* d_err, cudaStream_t st, Err& e) {
@@ -101,7 +120,8 @@ extern "C" int tch_stripe_noalloc(int device, int n, const uint8_t* d_O, size_t 
                      need, n, x_rows, kb, (size_t)TCH_NOALLOC_SCRATCH_BYTES);
     if (kb > (size_t)INT32_MAX) return e.set("rows too wide");
 
-    cudaError_t ce = cudaSetDevice(device);
+    DeviceScope scope;
+    cudaError_t ce = scope.set(device);
     if (ce != cudaSuccess) return e.set("cudaSetDevice(%d): %s", device, cudaGetErrorString(ce));
     uint8_t* scratch = nullptr;
     if (scratch_address(device, &scratch, e)) return 1;
@@ -113,10 +133,10 @@ extern "C" int tch_stripe_noalloc(int device, int n, const uint8_t* d_O, size_t 
 
     // 1. clear the error word, check the CSR offsets before anything walks them
     ce = cudaMemsetAsync(d_err, 0, sizeof(int), st);
-    if (ce != cudaSuccess) return e.set("cudaMemsetAsync: %s", cudaGetErrorString(ce));
+    if (ce != cudaSuccess) return fail_queued(st, e, "cudaMemsetAsync", ce);
     check_offsets_kernel<<<(n + 255) / 256, 256, 0, st>>>(d_start, n, n_rare, d_err);
     ce = cudaGetLastError();
-    if (ce != cudaSuccess) return e.set("offset check: %s", cudaGetErrorString(ce));
+    if (ce != cudaSuccess) return fail_queued(st, e, "offset check", ce);
     if (read_error(d_err, st, e)) return 1;
 
     // 2. bits -> e4m3 operand rows in the scratch array, 3. the stripe
@@ -126,7 +146,7 @@ extern "C" int tch_stripe_noalloc(int device, int n, const uint8_t* d_O, size_t 
     bits.wP = (int)(K2 / 32);
     bits.wO = (int)(K1 / 32);
     ce = launch_expand_bits(bits, n, x_rows, X, (int)kb, (int)kp, (int)K2, (int)K1, 0x38, 0x38, st);
-    if (ce != cudaSuccess) return e.set("operand expansion: %s", cudaGetErrorString(ce));
+    if (ce != cudaSuccess) return fail_queued(st, e, "operand expansion", ce);
     ByteOperands ops;
     ops.X = X;
     ops.n_rows = x_rows;
@@ -145,6 +165,6 @@ extern "C" int tch_stripe_noalloc(int device, int n, const uint8_t* d_O, size_t 
     a.ldo = ldo;
     a.err = d_err;
     ce = launch_tc_stripe(TCH_KERNEL_TC_F8, ops, nullptr, rare, a, sms, st);
-    if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
+    if (ce != cudaSuccess) return fail_queued(st, e, "stripe kernel", ce);
     return read_error(d_err, st, e);
 }

@@ -138,6 +138,52 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// Writes x into 32 consecutive TMEM columns of the warp's 32 lanes (taddr:
+// lane quarter of the warp in bits 16+, first column in the low bits).
+__device__ __forceinline__ void tmem_fill32(uint32_t taddr, uint32_t x) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+        "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(
+            taddr),
+        "r"(x)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// Block-scaled fp4 MMA: A and B are packed e2m1 (two elements per byte,
+// K-major), K = 64 elements (32 bytes) per instruction, one ue8m0 scale per
+// 32 elements of K read from TMEM at tsfa / tsfb.  D is fp32 in TMEM.
+__device__ __forceinline__ void tc_mma_mxf4(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t tsfa, uint32_t tsfb, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %6, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::mxf4.block_scale.block32 [%0], %1, %2, %3, [%4], [%5], p;\n\t}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(tsfa), "r"(tsfb), "r"(accumulate)
+        : "memory");
+}
+
+// The same product through kind::mxf4nvf4: BLOCK = 32 (ue8m0 scales) or 16
+// (ue4m3 scales, two per 32 elements of K).
+template <int BLOCK>
+__device__ __forceinline__ void tc_mma_nvf4(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t tsfa, uint32_t tsfb, uint32_t accumulate) {
+    if (BLOCK == 32)
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %6, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::mxf4nvf4.block_scale.block32 [%0], %1, %2, %3, [%4], [%5], p;\n\t}\n" ::"r"(
+                tmem_d),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(tsfa), "r"(tsfb), "r"(accumulate)
+            : "memory");
+    else
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %6, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::mxf4nvf4.block_scale.block16 [%0], %1, %2, %3, [%4], [%5], p;\n\t}\n" ::"r"(
+                tmem_d),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(tsfa), "r"(tsfb), "r"(accumulate)
+            : "memory");
+}
+
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, rows of 128 B,
 // 8-row swizzle atoms 1024 B apart (SBO); LBO unused for this layout.
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
@@ -154,6 +200,16 @@ __host__ __device__ constexpr uint32_t make_idesc(uint32_t dfmt, uint32_t abfmt,
     return (dfmt << 4) | (abfmt << 7) | (abfmt << 10) | (negb << 14) | ((uint32_t)(N >> 3) << 17) |
            ((uint32_t)(M >> 4) << 24);
 }
+
+// Instruction descriptor of the block-scaled kinds: A/B formats (e2m1 = 1 for
+// kind::mxf4), K-major A and B, N, scale type (1 = ue8m0), M; scale-factor
+// ids 0 and no negation (the fp4 kinds have none).  D is always fp32.
+__host__ __device__ constexpr uint32_t make_idesc_mx(uint32_t abfmt, uint32_t sf_ue8m0, int M, int N) {
+    return (abfmt << 7) | (abfmt << 10) | ((uint32_t)(N >> 3) << 17) | (sf_ue8m0 << 23) | ((uint32_t)(M >> 4) << 24);
+}
+constexpr uint32_t kE2M1 = 1;          // e2m1 in the fp4 kinds' format field
+constexpr uint32_t kUe8m0One = 0x7Fu;  // ue8m0 scale 2^0
+constexpr uint32_t kUe4m3One = 0x38u;  // ue4m3 scale 1.0
 
 
 }  // namespace ptx

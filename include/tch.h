@@ -346,7 +346,9 @@ void tch_solver_destroy(tch_solver* s);
  * The first call on a device takes the array's address (cudaGetSymbolAddress)
  * and must come before any stream capture.  Every call reuses the array, so
  * calls that overlap on the GPU race; the call synchronises `stream` before it
- * returns.  A device that has loaded the array keeps it until process exit. */
+ * returns, on success and on every failure after it has queued work.  The
+ * caller's current device is the same after the call as before it.  A device
+ * that has loaded the array keeps it until process exit. */
 int tch_stripe_noalloc(int device, int n, const uint8_t* d_O, size_t K1, const uint8_t* d_P, size_t K2,
                        const uint32_t* d_start, const uint32_t* d_js, size_t n_rare, int r0, int rows,
                        uint16_t* d_out, size_t ldo, void* stream, char* err, int errlen);

@@ -98,6 +98,31 @@ int64_t orc_upper_rows(const uint16_t* x, int64_t n, int64_t L, int64_t i0, int6
     return pairs;
 }
 
+/* The same count over the rows i0, i0 + step, i0 + 2 step, ... below n: a
+ * sample spread over the whole triangle (step consecutive offsets cover every
+ * row once).  Returns the pairs evaluated; *sum as above. */
+int64_t orc_upper_rows_step(const uint16_t* x, int64_t n, int64_t L, int64_t i0, int64_t step, uint64_t* sum,
+                            int threads) {
+    const int nt = pick_threads(threads);
+    uint64_t total = 0;
+    int64_t pairs = 0;
+    const int64_t TJ = 256, ntj = (n + TJ - 1) / TJ;
+    const int64_t rows = i0 < n && step > 0 ? (n - i0 + step - 1) / step : 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total, pairs) num_threads(nt)
+    for (int64_t t = 0; t < rows * ntj; t++) {
+        const int64_t i = i0 + (t / ntj) * step, bj = (t % ntj) * TJ;
+        const int64_t ej = bj + TJ < n ? bj + TJ : n;
+        const int64_t sj = bj > i + 1 ? bj : i + 1;
+        const uint16_t* a = x + i * L;
+        for (int64_t j = sj; j < ej; j++) {
+            total += pair_dist(a, x + j * L, L);
+            pairs++;
+        }
+    }
+    if (sum) *sum = total;
+    return pairs;
+}
+
 /* Rolling checksum of tc_hamming.cu:240-241 over one stripe buffer laid out
  * like the tch_run callback: rows x w, row stride ld, column c <-> j = r0 + c;
  * only c > r is part of the upper triangle. */

@@ -72,6 +72,8 @@ def lib():
         L.orc_hamming_block.restype = None
         L.orc_upper_rows.argtypes = [u16p, i64, i64, i64, i64, u64p, ctypes.c_int]
         L.orc_upper_rows.restype = i64
+        L.orc_upper_rows_step.argtypes = [u16p, i64, i64, i64, i64, u64p, ctypes.c_int]
+        L.orc_upper_rows_step.restype = i64
         L.orc_rollhash_stripe.argtypes = [ctypes.c_uint64, u16p, i64, i64, i64]
         L.orc_rollhash_stripe.restype = ctypes.c_uint64
         L.orc_rollhash_ranks.argtypes = [u16p, i64, i64, ctypes.c_int]

@@ -1,9 +1,9 @@
 #!/usr/bin/env python3
 """Writes the golden fixtures of tests/golden/ from the reference's own code.
 
-Run once, in a checkout that has the reference project next to it:
+Run once, with the path of a checkout of the reference project:
 
-    python tests/golden/make_golden.py /root/reference [--kat]
+    python tests/golden/make_golden.py <reference checkout> [--kat]
 
 It imports the reference's exactness check (tensorcore/rs/check.py) and calls
 its ``make`` and ``ref`` functions, and it runs the reference's synthetic
@@ -44,7 +44,10 @@ def mat_sha(M) -> str:
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if len(args) != 1:
+        sys.exit("usage: make_golden.py <reference checkout> [--kat]")
+    ref_root = args[0]
     kat = "--kat" in sys.argv
     spec = importlib.util.spec_from_file_location("ref_check", os.path.join(ref_root, "tensorcore/rs/check.py"))
     check = importlib.util.module_from_spec(spec)
