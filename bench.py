@@ -19,7 +19,8 @@ n (n - 1) / 2 = 1 984 783 510 exact pairs.
            algorithmic MACs (unpadded K = L + D per pair, 2 ops per MAC) per
            launch / CUDA-event duration of that launch alone (the two passes
            are timed apart through tch_solver_rare_counts and
-           tch_solver_stripe_counts), against the measured fp8 tcgen05 peak.
+           tch_solver_stripe_counts), against the measured fp4 (kind::mxf4)
+           tcgen05 peak of the same GPU.
     cpu_baseline   the brute-force count of the reference's exactness check
            (the C restatement in oracle/), all host threads, bounded sample.
 
@@ -31,10 +32,10 @@ k, k + s, k + 2 s, ... of the upper triangle (a sample spread over the whole
 triangle; s consecutive steps cover every row once), and value = pairs
 counted / seconds over the timed steps.
 
-Only one-GPU runs are offered: the tile pass may share operand tiles between
-the CTAs of a cluster by TMA multicast, which is valid within one GPU's
-memory only, so under torchrun with WORLD_SIZE > 1 the GPU arm refuses to run
-(the reference arm runs on rank 0 and the other ranks exit).
+Only one-GPU runs are offered (the library drives one device per process, and
+the workload is quoted on one GPU): under torchrun with WORLD_SIZE > 1 the GPU
+arm refuses to run (the reference arm runs on rank 0 and the other ranks
+exit).
 """
 from __future__ import annotations
 
@@ -54,7 +55,7 @@ sys.path.insert(0, ROOT)
 PKG = "cgmlst-hamming-gpu_gb300"
 
 METRIC = "exact_pairs_per_s"
-DTYPE = "fp8(e4m3 0/1) -> fp32 exact ints -> u16"
+DTYPE = "fp4(e2m1 0/+-1, block scales 1.0) -> fp32 exact ints -> u16"
 UNIT = "pairs/s"
 
 
@@ -451,8 +452,8 @@ def batch_sets(tch, count, device):
 
 
 def batch_timing(tch, args, device):
-    """--batch-timing: one batched solve with a fixed schedule (--branches,
-    --cluster): CUDA-event time of a graph replay (median of 5 after 3
+    """--batch-timing: one batched solve with a fixed schedule (--branches):
+    CUDA-event time of a graph replay (median of 5 after 3
     untimed) and the largest sets with their tau."""
     import torch
 
@@ -460,7 +461,7 @@ def batch_timing(tch, args, device):
     off, _ = b.layout()
     out = torch.empty(int(off[-1]) + 8, dtype=torch.int16, device=f"cuda:{device}")
     st = torch.cuda.Stream(device=device)
-    b.set_schedule(args.branches, args.cluster, args.cluster)
+    b.set_schedule(args.branches)
     for _ in range(3):
         b.run(out.data_ptr(), st.cuda_stream)
     ms = []
@@ -475,7 +476,7 @@ def batch_timing(tch, args, device):
     taus = b.info()["taus"]
     pairs = [n * (n - 1) // 2 for n, _ in shapes]
     print(f"ms per batch {sorted(ms)[len(ms) // 2]:.3f} ({sum(pairs)} pairs, {args.batch_count} sets, "
-          f"{args.branches} branches, cluster {args.cluster})", flush=True)
+          f"{args.branches} branches)", flush=True)
     for i in sorted(range(len(shapes)), key=lambda i: -pairs[i])[:8]:
         print(f"  set {i}: n {shapes[i][0]} L {shapes[i][1]} tau {taus[i]}", flush=True)
     b.close()
@@ -487,7 +488,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--kernel", default="tc_f8")
+    ap.add_argument("--kernel", default="tc_f4")
     ap.add_argument("--tau", type=int, default=0, help="0 = the analytic GB300 model's choice")
     ap.add_argument("--stripe", type=int, default=4096, help="rows per stripe of the e2e tch_run call")
     ap.add_argument("--e2e-steps", type=int, default=5, help="timed e2e passes; the median is reported")
@@ -507,10 +508,9 @@ def main():
     ap.add_argument("--step-timing", action="store_true",
                     help="time the rare counts and the tile pass of one solve of --n profiles at --tau, --reps times")
     ap.add_argument("--batch-timing", action="store_true",
-                    help="time one batched replay of --batch-count sets with --branches and --cluster")
+                    help="time one batched replay of --batch-count sets with --branches")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--branches", type=int, default=32)
-    ap.add_argument("--cluster", type=int, default=1)
     ap.add_argument("--ref-stride", type=int, default=6,
                     help="reference arm: rows k, k + s, ... of the triangle per step")
     ap.add_argument("--parity-rows", type=int, default=256,
@@ -524,8 +524,7 @@ def main():
             print(json.dumps(reference_arm(args)), flush=True)
         return
     if ws > 1:
-        log("bench.py: this build offers one-GPU runs only (the tile pass may use TMA multicast within a "
-            "thread-block cluster, valid in one GPU's memory); run it without torchrun")
+        log("bench.py: this build offers one-GPU runs only; run it without torchrun")
         sys.exit(2)
 
     tch = importlib.import_module(PKG)
@@ -639,15 +638,15 @@ def main():
     achieved = ops_per_launch / (tc_ms / 1e3) / 1e12
     peak_info = tc_peaks()
     mp = measured_peaks()
-    peak = peak_info.get("tc_f8_tflops")
-    peak_src = "tch-peak tcgen05 kind::f8f6f4 probe on this GPU"
+    peak = peak_info.get("tc_f4_tflops") if peak_info.get("tc_f4_tflops_check") == "exact" else None
+    peak_src = "tch-peak tcgen05 kind::mxf4 probe on this GPU (same process)"
     if not peak:
-        peak = 2 * (mp or {}).get("bf16_tflops", 1900.0)
-        peak_src = "2 x measured bf16 (fp8 dense rate ratio)"
+        peak = 4 * (mp or {}).get("bf16_tflops", 1900.0)
+        peak_src = "4 x measured bf16 (fp4 dense rate ratio)"
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "peak_source": peak_src,
                 "algorithmic_ops_per_launch": ops_per_launch, "k_per_pair": k_alg,
-                "k_padded_bytes": info["k_presence"] + info["k_onehot"],
+                "k_padded_columns": info["k_presence"] + info["k_onehot"],
                 "bf16_measured_tflops": (mp or {}).get("bf16_tflops"), "traffic": None}
     # DRAM bytes of one whole-triangle tile pass, from the ncu capture of this
     # workload (valid for the tau and row share it was taken at)

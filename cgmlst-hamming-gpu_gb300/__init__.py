@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libtch.so")
 CLI_PATH = os.path.join(HERE, "bin", "cgmlst-hamming-gpu")
 RANKS_TOOL_PATH = os.path.join(HERE, "bin", "tch-ranks")
 
-KERNELS = {"auto": 0, "popc": 1, "mma_b1": 2, "tc_f8": 3, "tc_i8": 4, "tc_f16": 5}
+KERNELS = {"auto": 0, "popc": 1, "mma_b1": 2, "tc_f8": 3, "tc_i8": 4, "tc_f16": 5, "tc_f4": 6}
 
 # The reference host's analytic-model rates, measured on an L4 (main.rs:170-171).
 REF_GEMM_RATE = 5.9e14
@@ -160,12 +160,11 @@ def lib():
         L.tch_batch_run.argtypes = [c_void, c_void, c_void, c_char_p, c_int]
         L.tch_batch_run.restype = c_int
         L.tch_batch_check.argtypes, L.tch_batch_check.restype = [c_void, c_char_p, c_int], c_int
-        L.tch_batch_tune.argtypes = [c_void, c_void, c_void, c_int, P(c_double), P(c_int), P(c_int), P(c_int),
-                                     c_char_p, c_int]
+        L.tch_batch_tune.argtypes = [c_void, c_void, c_void, c_int, P(c_double), P(c_int), c_char_p, c_int]
         L.tch_batch_tune.restype = c_int
-        L.tch_batch_set_schedule.argtypes = [c_void, c_int, c_int, c_int]
+        L.tch_batch_set_schedule.argtypes = [c_void, c_int]
         L.tch_batch_set_schedule.restype = c_int
-        L.tch_batch_info.argtypes = [c_void, P(c_int), c_void, P(c_int), P(c_int), P(c_int)]
+        L.tch_batch_info.argtypes = [c_void, P(c_int), c_void, P(c_int)]
         L.tch_batch_info.restype = c_int
         L.tch_batch_destroy.argtypes, L.tch_batch_destroy.restype = [c_void], None
         L.tch_solver_from_ranks.argtypes = [c_int, c_int, c_int, c_void, c_int, c_int, P(c_void), c_char_p, c_int]
@@ -695,25 +694,22 @@ class Batch:
 
     def tune(self, d_out: int, stream: int = 0, reps: int = 3) -> dict:
         ms = ctypes.c_double()
-        nb, cs, cl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        nb = ctypes.c_int()
         err = _errbuf()
         _check(lib().tch_batch_tune(self._h, ctypes.c_void_p(d_out), ctypes.c_void_p(stream) if stream else None,
-                                    reps, ctypes.byref(ms), ctypes.byref(nb), ctypes.byref(cs), ctypes.byref(cl),
-                                    err, len(err)), err)
-        return dict(ms=ms.value, branches=nb.value, cluster_small=cs.value, cluster_large=cl.value)
+                                    reps, ctypes.byref(ms), ctypes.byref(nb), err, len(err)), err)
+        return dict(ms=ms.value, branches=nb.value)
 
-    def set_schedule(self, branches: int, cluster_small: int = 2, cluster_large: int = 2):
-        if lib().tch_batch_set_schedule(self._h, branches, cluster_small, cluster_large):
+    def set_schedule(self, branches: int):
+        if lib().tch_batch_set_schedule(self._h, branches):
             raise TchError("invalid schedule")
 
     def info(self) -> dict:
         c = ctypes.c_int()
         taus = np.zeros(max(len(self.shapes), 1), np.int32)
-        nb, cs, cl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        lib().tch_batch_info(self._h, ctypes.byref(c), _ptr(taus), ctypes.byref(nb), ctypes.byref(cs),
-                             ctypes.byref(cl))
-        return dict(count=c.value, taus=taus[:c.value].tolist(), branches=nb.value, cluster_small=cs.value,
-                    cluster_large=cl.value)
+        nb = ctypes.c_int()
+        lib().tch_batch_info(self._h, ctypes.byref(c), _ptr(taus), ctypes.byref(nb))
+        return dict(count=c.value, taus=taus[:c.value].tolist(), branches=nb.value)
 
     def close(self):
         if self._h:

@@ -13,8 +13,7 @@
 // join is captured once as a CUDA graph and replayed on every later run.
 //
 // tch_batch_tune is the autotuner of that schedule: it times the graph for
-// every combination of branch count and tile-pass cluster size (1 or 2 CTAs,
-// chosen separately for small and large sets) and keeps the fastest.
+// every branch count and keeps the fastest.
 
 #include <math.h>
 #include <string.h>
@@ -33,8 +32,6 @@ struct tch_batch {
     std::vector<size_t> off;  // u16 elements: set s at off[s], n_s x ld_s; off.back() = total
     std::vector<size_t> ld;
     int branches = 8;
-    int cm_small = 2, cm_large = 2;
-    int small_tiles = 64;  // a set with fewer 128 x 256 tiles than this counts as small
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> events;  // branches + 1
     cudaStream_t origin = nullptr;  // the stream the fork / join is captured on
@@ -71,11 +68,6 @@ fail:
     return 1;
 }
 
-long long tiles_of(int n) {
-    const long long bi = (n + 127) / 128, bj = (n + 255) / 256;
-    return bi * bj / 2 + bi;
-}
-
 // Rare-count block of set s: n x up(n, 256) u16.
 size_t rare_ld(int n) { return up((size_t)std::max(n, 1), kRareDenseAlign); }
 
@@ -92,16 +84,14 @@ fail:
     return 1;
 }
 
-// One eager solve per cluster size before the first capture, so one-time set-up
-// (kernel attributes, occupancy queries) never runs inside it.
+// One eager solve before the first capture, so one-time set-up (kernel
+// attributes) never runs inside it.
 int warm_up(tch_batch* b, uint16_t* d_out, Err& e) {
     int best = -1;
     for (size_t s = 0; s < b->sets.size(); s++)
         if (solver_size(b->sets[s]) > 1 && (best < 0 || solver_work(b->sets[s]) < solver_work(b->sets[best])))
             best = (int)s;
-    if (best >= 0)
-        for (int cm : {1, 2}) {
-            solver_set_cluster(b->sets[best], cm);
+    if (best >= 0) {
             const int n = solver_size(b->sets[best]);
             if (ensure_rbuf(b, 0, (size_t)n * rare_ld(n) * 2, e)) return 1;
             if (solver_stripe_counts(b->sets[best], 0, n, d_out + b->off[best], b->ld[best], b->rbuf[0], rare_ld(n),
@@ -142,8 +132,6 @@ int build_graph(tch_batch* b, uint16_t* d_out, Err& e) {
     }
     for (int k = 0; k < nb; k++)
         if (ensure_rbuf(b, k, need[k], e)) return 1;
-    for (size_t s = 0; s < b->sets.size(); s++)
-        solver_set_cluster(b->sets[s], tiles_of(solver_size(b->sets[s])) < b->small_tiles ? b->cm_small : b->cm_large);
     TCH_CK(e, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     TCH_CK(e, cudaEventRecord(b->events[nb], st));
     for (int k = 0; k < nb; k++) TCH_CK(e, cudaStreamWaitEvent(b->streams[k], b->events[nb], 0));
@@ -251,41 +239,33 @@ int tch_batch_check(tch_batch* b, char* err, int errlen) {
 }
 
 int tch_batch_tune(tch_batch* b, uint16_t* d_out, void* stream, int reps, double* best_ms, int* best_branches,
-                   int* best_cm_small, int* best_cm_large, char* err, int errlen) {
+                   char* err, int errlen) {
     Err e{err, errlen};
     cudaStream_t st = (cudaStream_t)stream;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     double best = 1e300;
-    int bb = b ? b->branches : 8, bs = 2, bl = 2;
+    int bb = b ? b->branches : 8;
     if (!b || !d_out) return e.set("null argument");
     if (cudaSetDevice(b->device) != cudaSuccess) return e.set("cudaSetDevice(%d) failed", b->device);
     reps = std::max(reps, 1);
     TCH_CK(e, cudaEventCreate(&t0));
     TCH_CK(e, cudaEventCreate(&t1));
-    for (int nb : {1, 4, 8, 16, 32})
-        for (int cs : {1, 2})
-            for (int cl : {1, 2}) {
-                b->branches = nb;
-                b->cm_small = cs;
-                b->cm_large = cl;
-                if (build_graph(b, d_out, e)) goto fail;
-                TCH_CK(e, cudaGraphLaunch(b->exec, st));  // warm
-                TCH_CK(e, cudaEventRecord(t0, st));
-                for (int r = 0; r < reps; r++) TCH_CK(e, cudaGraphLaunch(b->exec, st));
-                TCH_CK(e, cudaEventRecord(t1, st));
-                TCH_CK(e, cudaEventSynchronize(t1));
-                float ms = 0;
-                TCH_CK(e, cudaEventElapsedTime(&ms, t0, t1));
-                if (ms / reps < best) best = ms / reps, bb = nb, bs = cs, bl = cl;
-            }
+    for (int nb : {1, 4, 8, 16, 32}) {
+        b->branches = nb;
+        if (build_graph(b, d_out, e)) goto fail;
+        TCH_CK(e, cudaGraphLaunch(b->exec, st));  // warm
+        TCH_CK(e, cudaEventRecord(t0, st));
+        for (int r = 0; r < reps; r++) TCH_CK(e, cudaGraphLaunch(b->exec, st));
+        TCH_CK(e, cudaEventRecord(t1, st));
+        TCH_CK(e, cudaEventSynchronize(t1));
+        float ms = 0;
+        TCH_CK(e, cudaEventElapsedTime(&ms, t0, t1));
+        if (ms / reps < best) best = ms / reps, bb = nb;
+    }
     b->branches = bb;
-    b->cm_small = bs;
-    b->cm_large = bl;
     if (build_graph(b, d_out, e)) goto fail;
     if (best_ms) *best_ms = best;
     if (best_branches) *best_branches = bb;
-    if (best_cm_small) *best_cm_small = bs;
-    if (best_cm_large) *best_cm_large = bl;
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     return 0;
@@ -295,17 +275,14 @@ fail:
     return 1;
 }
 
-int tch_batch_set_schedule(tch_batch* b, int branches, int cm_small, int cm_large) {
-    if (!b || branches < 1 || branches > 64 || (cm_small != 1 && cm_small != 2) || (cm_large != 1 && cm_large != 2))
-        return 1;
+int tch_batch_set_schedule(tch_batch* b, int branches) {
+    if (!b || branches < 1 || branches > 64) return 1;
     b->branches = branches;
-    b->cm_small = cm_small;
-    b->cm_large = cm_large;
     drop_graph(b);
     return 0;
 }
 
-int tch_batch_info(const tch_batch* b, int* count, int* taus, int* branches, int* cm_small, int* cm_large) {
+int tch_batch_info(const tch_batch* b, int* count, int* taus, int* branches) {
     if (!b) return 1;
     if (count) *count = (int)b->sets.size();
     if (taus)
@@ -315,8 +292,6 @@ int tch_batch_info(const tch_batch* b, int* count, int* taus, int* branches, int
             taus[s] = info.tau;
         }
     if (branches) *branches = b->branches;
-    if (cm_small) *cm_small = b->cm_small;
-    if (cm_large) *cm_large = b->cm_large;
     return 0;
 }
 

@@ -168,18 +168,25 @@ __global__ void cell_rank_kernel(const uint64_t* __restrict__ calls, int n, int 
     }
 }
 
+// +1.0 at column col of row `row` of a packed e2m1 operand (zeroed before):
+// the 32-bit word holding columns 8w .. 8w + 7 gets the nibble by an atomic
+// OR, as two columns of one byte belong to different cells.
+__device__ __forceinline__ void set_fp4_one(const KChunks& X, size_t row, size_t col) {
+    uint32_t* w = reinterpret_cast<uint32_t*>(X.at(row, (int)((col >> 1) & ~(size_t)3)));
+    atomicOr(w, kFp4One << (4 * (col & 7)));
+}
+
 __global__ void pack_x_kernel(const uint16_t* __restrict__ x, int n, int L, const uint64_t* __restrict__ cnt_off,
-                              const int32_t* __restrict__ col_flat, const uint32_t* __restrict__ base, KChunks X,
-                              int kp, uint8_t one) {
+                              const int32_t* __restrict__ col_flat, const uint32_t* __restrict__ base, KChunks X) {
     const size_t total = (size_t)n * L;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
         const size_t i = t / L;
         const int k = (int)(t % L);
         const int a = x[t];
         if (!a) continue;
-        *X.at(i, k) = one;
+        set_fp4_one(X, i, (size_t)k);
         const int32_t c = col_flat[cnt_off[k] + a];
-        if (c >= 0) *X.at(i, kp + (int)base[k] + c) = one;
+        if (c >= 0) set_fp4_one(X, i, (size_t)L + base[k] + (size_t)c);
     }
 }
 
@@ -363,7 +370,7 @@ std::vector<TauRow> tau_rows(const std::vector<uint32_t>& cnt_flat, const std::v
         for (uint64_t q = off[k] + 1; q < off[k + 1]; q++)
             if (cnt_flat[q]) cs.push_back((double)cnt_flat[q]);
     const double pairs = (double)n * (double)(n - 1) / 2.0;
-    const size_t rows = up((size_t)std::max(n, 1), 256), kp = up((size_t)L, 128);
+    const size_t rows = up((size_t)std::max(n, 1), 256);
     const double nl = (double)n * (double)L;
     std::vector<TauRow> out;
     for (int tau = 2; tau <= (dense ? 65536 : 4096); tau *= 2) {
@@ -379,7 +386,7 @@ std::vector<TauRow> tau_rows(const std::vector<uint32_t>& cnt_flat, const std::v
                 }
             }
         }
-        w.kb = (double)(kp + up(w.d, 128));
+        w.kb = (double)fp4_columns(L, w.d);  // K: MACs per pair; the two operand copies take K bytes per row
         if (dense) {  // ranks, own positions, group members (a stripe's counts come later)
             w.mem = (double)rows * w.kb + nl * 6.0 + 4.0 * w.cells;
             w.t = pairs * w.kb / m.gemm_rate + w.r / m.dense_rate;
@@ -658,8 +665,8 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
         }
         base[L] = (uint32_t)D;
         out->D = D;
-        out->kp = (int)up((size_t)L, 128);
-        out->kb = out->kp + (int)up(D, 128);
+        if (fp4_columns(L, D) / 2 > (size_t)INT32_MAX) { e.set("%llu one-hot columns: too many", (unsigned long long)D); goto fail; }
+        out->kb = (int)(fp4_columns(L, D) / 2);
         out->x_rows = up((size_t)std::max(n, 1), 256);
         const uint64_t n_members = goff[off_h[L]];
         if (dense_rare && n_members >= (1ull << 32)) {
@@ -674,22 +681,19 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
         TCH_CK(e, cudaMemcpy(goff_d, goff.data(), (off_h[L] + 1) * 8, cudaMemcpyHostToDevice));
 
         mark("tau and column maps");
-        // ---- 4: operand rows
+        // ---- 4: operand rows: pos by nibble, neg from pos
         {
-            const int w = chunk_width_for(out->kb, out->x_rows, max_chunk_bytes);
-            if (!w) { e.set("the operand needs more than %d K chunks of %zu bytes", kMaxKChunks, max_chunk_bytes); goto fail; }
-            out->X.kb = out->kb;
-            out->X.width = w;
-            out->X.n = (out->kb + w - 1) / w;
-            for (int c = 0; c < out->X.n; c++) {
-                const size_t bytes = out->x_rows * (size_t)out->X.width_of(c);
-                TCH_CK(e, dalloc(&out->X.p[c], bytes, &out->bytes));
-                TCH_CK(e, cudaMemset(out->X.p[c], 0, bytes));
+            if (!chunk_width_for(out->kb, out->x_rows, max_chunk_bytes)) {
+                e.set("the operand needs more than %d K chunks of %zu bytes", kMaxKChunks, max_chunk_bytes);
+                goto fail;
             }
+            TCH_CK(e, alloc_fp4(&out->X, out->x_rows, out->kb, max_chunk_bytes, true, true, &out->bytes));
+            for (int c = 0; c < out->X.pos.n; c++)
+                TCH_CK(e, cudaMemset(out->X.pos.p[c], 0, out->x_rows * (size_t)out->X.pos.width_of(c)));
         }
-        pack_x_kernel<<<grid_for((size_t)n * L, sms), 256>>>(out->x, n, L, cnt_off_d, col_d, base_d, out->X, out->kp,
-                                                             0x38);
+        pack_x_kernel<<<grid_for((size_t)n * L, sms), 256>>>(out->x, n, L, cnt_off_d, col_d, base_d, out->X.pos);
         TCH_CK(e, cudaGetLastError());
+        TCH_CK(e, launch_negate_onehot(out->X, L, 0));
 
         mark("operand rows");
         // ---- 5: rare groups, sorted
@@ -791,7 +795,7 @@ fail:
 
 void free_device_encoding(DeviceEncoding* d) {
     cudaFree(d->x);
-    for (int c = 0; c < d->X.n; c++) cudaFree(d->X.p[c]);
+    free_fp4(&d->X);
     cudaFree(d->start);
     cudaFree(d->js);
     cudaFree(d->cnt_off);
@@ -805,7 +809,7 @@ void free_device_encoding(DeviceEncoding* d) {
     d->col = nullptr;
     d->base = nullptr;
     d->x = nullptr;
-    d->X = KChunks();
+    d->X = Fp4Operands();
     d->start = d->js = nullptr;
     d->cnt_off = d->goff = nullptr;
     d->members = d->mpos = nullptr;

@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
             }
             __syncthreads();
             uint4* dst = Rrow + ((wb - cbeg) >> 3);
-            for (int w = tid; w < nq; w += T) dst[w] = smem_rd[w];
+            for (int w = tid; w < nq; w += T) __stcs(dst + w, smem_rd[w]);  // streamed: keeps the members in L2
             __syncthreads();
         }
     }
@@ -309,13 +309,68 @@ __global__ void __launch_bounds__(T, 1024 / T)
             }
             __syncthreads();
             uint4* dst = Rrow + (wb >> 3);
-            for (int w = tid; w < nq; w += T) dst[w] = smem_rd[w];
+            for (int w = tid; w < nq; w += T) __stcs(dst + w, smem_rd[w]);  // streamed: keeps the members in L2
+            __syncthreads();
+        }
+    }
+}
+
+// The same block from pair lists: one CTA per stripe row (persistent), the
+// row's partners read once per counter pass with consecutive threads on
+// consecutive entries, each partner in the pass's columns adding 1 with a
+// shared atomic.  A partner outside (i, n) is reported and skipped.
+__global__ void __launch_bounds__(1024, 1)
+    rare_lists_kernel(const uint32_t* __restrict__ start, const uint32_t* __restrict__ js, int n, int r0, int rows,
+                      uint16_t* __restrict__ R, size_t ldr, int cend, int cwords, int* err) {
+    extern __shared__ uint4 smem_rd[];
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(smem_rd);
+    const int tid = threadIdx.x;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int i = r0 + r;
+        const uint32_t pa = __ldg(start + i), pb = __ldg(start + i + 1);
+        const int cbeg = r0 + (r & ~(kRareDenseAlign - 1));  // first column of the row's diagonal tile
+        uint4* Rrow = reinterpret_cast<uint4*>(R + (size_t)r * ldr + (size_t)(cbeg - r0));
+        for (int wb = cbeg; wb < cend; wb += 2 * cwords) {
+            const int we = min(cend, wb + 2 * cwords);
+            const int nq = (we - wb) >> 3;
+            for (int w = tid; w < nq; w += blockDim.x) smem_rd[w] = make_uint4(0, 0, 0, 0);
+            __syncthreads();
+            for (uint32_t p = pa + (uint32_t)tid; p < pb; p += blockDim.x) {
+                const uint32_t j = __ldg(js + p);
+                if (j <= (uint32_t)i || j >= (uint32_t)n) {
+                    if (wb == cbeg) atomicOr(err, DEVERR_RARE_PAIR);
+                    continue;
+                }
+                if (j >= (uint32_t)wb && j < (uint32_t)we) count_col(cnt, j - (uint32_t)wb);
+            }
+            __syncthreads();
+            uint4* dst = Rrow + ((wb - cbeg) >> 3);
+            for (int w = tid; w < nq; w += blockDim.x) __stcs(dst + w, smem_rd[w]);
             __syncthreads();
         }
     }
 }
 
 }  // namespace
+
+cudaError_t launch_rare_from_lists(const uint32_t* start, const uint32_t* js, int n, int r0, int rows, uint16_t* R,
+                                   size_t ldr, int* err, int sms, cudaStream_t st) {
+    if (rows <= 0) return cudaSuccess;
+    const size_t width = up((size_t)(n - r0), kRareDenseAlign);
+    if (ldr < width || (ldr & 7) || ((uintptr_t)R & 15)) return cudaErrorInvalidValue;
+    static bool attrs[kMaxDevices] = {};
+    bool& attr = attrs[current_device()];
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(rare_lists_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   RD_WORDS * 4);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const int cwords = counter_words(width);
+    rare_lists_kernel<<<std::max(1, std::min(rows, sms)), 1024, cwords * 4, st>>>(start, js, n, r0, rows, R, ldr,
+                                                                                 r0 + (int)width, cwords, err);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R, size_t ldr, int sms,
                               cudaStream_t st) {

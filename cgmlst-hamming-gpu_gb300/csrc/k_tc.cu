@@ -1,30 +1,37 @@
-// Tensor-core contraction for sm_103a: tcgen05.mma with TMEM accumulators,
-// operands staged by TMA, one fused epilogue writing u16 distances.
+// Tensor-core tile pass for sm_103a: block-scaled fp4 tcgen05.mma
+// (kind::mxf4, every scale factor 1.0) with TMEM accumulators, operands staged
+// by TMA, one fused epilogue writing u16 distances.
 //
-// Operands: X is n_rows x kb bytes, row = [presence part (kp bytes) |
-// one-hot part (kb - kp bytes)], one byte per element, 0 or +1 in e4m3
-// (0x38).  One output tile (128 rows i x 256 columns j) is
+// Operands (Fp4Operands): packed e2m1 rows [presence | one-hot | zeros], two
+// elements per byte, 0 or +1.0 in the `pos` copy, which is read as A, and 0
+// or +1.0 / -1.0 (one-hot part) in the `neg` copy, which is read as B.  One
+// output tile (128 rows i x 224 columns j) is
 //
-//   D = X_i[:, :kp] X_j[:, :kp]^T  -  X_i[:, kp:] X_j[:, kp:]^T  =  P Pt - O Ot
+//   D = pos_i . neg_j^T  =  P Pt - O Ot
 //
-// with the minus taken by the instruction descriptor's negate-B bit on the
-// one-hot stages.  Every partial sum is an integer with |value| <= number of
-// loci < 2^24, so fp32 accumulation is exact; the epilogue re-checks the
-// integrality of every value anyway and reports a device error if it ever
-// fails.  This replaces the reference's two CUTLASS b1 GEMMs
-// (tensorcore/rs/cuda/tch.cu:22-32, 128-129): on GB300 the b1 and s8 warp
-// MMAs issue at ~150 TOPS, and tcgen05 kind::i8 does not exist on sm_103a.
+// Every product is 0 or +-1 and every partial sum an integer of magnitude at
+// most the number of loci (< 2^24), so the fp32 accumulation is exact; the
+// epilogue re-checks the integrality of every value and reports a device
+// error if it ever fails.  This replaces the reference's two CUTLASS b1 GEMMs
+// (tensorcore/rs/cuda/tch.cu:22-32, 128-129): on GB300 the b1 warp MMA issues
+// at ~150 TOPS, kind::i8 does not exist on sm_103a, and the fp4 kinds run at
+// twice the fp8 rate from half the operand bytes (tch-peak).  The fp4 kinds
+// have no negate bit, hence the second operand copy with the one-hot sign in
+// the data.
 //
-// CTA = 6 warps, persistent over the stripe's tiles (upper triangle only):
-//   warp 0   TMA producer     4-stage ring of (A 128x128 B, B 256x128 B) tiles
-//   warp 1   MMA issuer       4 x tcgen05.mma (K = 32 bytes) per stage into one
-//                             of two 256-column TMEM accumulators
-//   warps 2-5 epilogue        tcgen05.ld 32 columns at a time -> int -> u16
-//                             in shared memory -> rare pairs of the row
-//                             subtracted (ascending CSR walk) -> coalesced
-//                             stores of the valid cells
-// Tiles are visited in groups of 8 row blocks (column-major inside a group) so
-// that concurrently running CTAs share A and B tiles in L2.
+// CTA = 10 warps, one CTA per SM, persistent over the stripe's tiles (upper
+// triangle only, or every tile of a rectangle):
+//   warp 0    TMA producer   5-stage ring of (A 128 x 128 B, B 224 x 128 B)
+//   warp 1    MMA issuer     4 x tcgen05.mma (K = 64 elements) per stage into
+//                            one of two 224-column TMEM accumulators
+//   warps 2-9 epilogue       two per TMEM lane quarter, one per column half:
+//                            tcgen05.ld 16 columns -> int -> minus the dense
+//                            rare counts (16-byte loads issued before the TMEM
+//                            read) -> u16 -> 32-byte stores from registers
+// TMEM: accumulators at columns 0 and 256, the scale factors (1.0, written
+// once by the epilogue warps before the first MMA) in columns 480-511.
+// Tiles are visited in raster groups of 16 row blocks, column-major inside a
+// group, so that the CTAs running at the same time share A and B tiles in L2.
 //
 // Every mbarrier wait is bounded (about 2 s of %globaltimer); on a timeout the
 // CTA records DEVERR_TIMEOUT, stops issuing work, drains what it issued,
@@ -39,115 +46,107 @@
 namespace tch {
 namespace {
 
-constexpr int BM = 128;            // tile rows (TMEM lanes)
-constexpr int BN = 256;            // tile columns (MMA N)
-constexpr int BK = 128;            // bytes of K per stage = one 128-byte swizzle row
-constexpr int STAGES = 4;
-constexpr int A_BYTES = BM * BK;   // 16 KB
-constexpr int B_BYTES = BN * BK;   // 32 KB
+constexpr int BM = 128;             // tile rows (TMEM lanes)
+constexpr int BN = 224;             // tile columns (MMA N)
+constexpr int BK = 128;             // bytes of K per stage: one 128-byte swizzle row, 256 elements
+constexpr int STAGES = 5;
+constexpr int A_BYTES = BM * BK;    // 16 KB
+constexpr int B_BYTES = BN * BK;    // 28 KB
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int EPI_WARPS = 8;      // two per TMEM lane quarter, one per column half
+constexpr int EPI_WARPS = 8;
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
-constexpr int EPI_PITCH = 34;      // u16 per staged row: 32 + 2 keeps row writes conflict-free
-constexpr int EPI_BYTES = EPI_WARPS * 32 * EPI_PITCH * 2;
-constexpr int TMEM_COLS = 2 * BN;  // two accumulators
-constexpr int GROUP_M = 16;        // row blocks per raster group (default; TCH_TC_GROUP overrides)
-constexpr int RBUF = 16;           // rare partners fetched per batch in the epilogue
-constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + EPI_BYTES + 256;
-
-enum Kind { KIND_F8 = 0, KIND_I8 = 1 };
+constexpr int ACC_STRIDE = 256;     // TMEM columns from one accumulator to the next
+constexpr int SF_COL = 480;         // 32 TMEM columns of scale factors
+constexpr int TMEM_COLS = 512;
+constexpr int CHUNK = 16;           // accumulator columns per tcgen05.ld
+constexpr int WARP_CHUNKS = BN / CHUNK / 2;  // chunks per epilogue warp (its column half)
+constexpr int GROUP_M = 16;         // row blocks per raster group (default; TCH_TC_GROUP overrides)
+constexpr int BAR_BYTES = 256;
+constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + BAR_BYTES;
+static_assert(SMEM_BYTES <= 232448, "shared memory per CTA");
+static_assert(BN % (2 * CHUNK) == 0 && BN <= ACC_STRIDE && ACC_STRIDE + BN <= SF_COL, "TMEM layout");
+static_assert(A_BYTES % 1024 == 0 && B_BYTES % 1024 == 0, "stages stay 1024-byte aligned (128-byte swizzle)");
 
 using namespace ptx;
 
-// ---------------------------------------------------------------- tile order
-// A cluster of CM CTAs works on CM vertically adjacent 128-row blocks (a
-// "super-row" sr of CM * 128 rows) against one 256-column block bj; CTA rank r
-// owns row block bi = sr * CM + r.  With CM = 2 the two CTAs share the B tile:
-// each loads one 128-row half and multicasts it to both.
-// Row blocks per raster group: GROUP_M unless TCH_TC_GROUP gives another even
-// count in [2, 256].  Larger groups read the column side of the operand fewer
+// Row blocks per raster group: GROUP_M unless TCH_TC_GROUP gives another
+// count in [1, 256].  Larger groups read the column side of the operand fewer
 // times (once per group) at the cost of a larger row-side working set.
 int group_row_blocks() {
     static int g = 0;
     if (!g) {
         const char* v = getenv("TCH_TC_GROUP");
         const int x = v ? atoi(v) : 0;
-        g = (x >= 2 && x <= 256 && x % 2 == 0) ? x : GROUP_M;
+        g = (x >= 1 && x <= 256) ? x : GROUP_M;
     }
     return g;
 }
 
+// ---------------------------------------------------------------- tile order
+// Row block bi covers rows a_r0 + BM bi .. + BM of the A operand, column block
+// bj columns c0 + BN bj .. + BN.  In a triangle (c0 = r0) the row block's
+// first column block is the one holding its first diagonal cell.
 struct TileSpace {
-    int nsr, nbj;  // super-rows of the stripe, column blocks of [c0, n)
-    int cm;        // row blocks per super-row (cluster size)
-    int gs;        // super-rows per raster group
-    int rect;      // 1: every tile of the rectangle (rows of one set against columns of another)
+    int nbi, nbj;  // row blocks of the stripe, column blocks of [c0, n)
+    int gs;        // row blocks per raster group
+    int rect;      // 1: every tile (rows of one set against columns of another)
 };
 
-// Columns of super-row sr: bj >= sr * cm / 2 (128-row blocks against 256-wide
-// column blocks that both start at r0; earlier columns lie below the diagonal);
-// all of them for a rectangle.
-__host__ __device__ __forceinline__ int first_col(const TileSpace& ts, int sr) {
-    return ts.rect ? 0 : sr * ts.cm / 2;
+__host__ __device__ __forceinline__ int first_col(const TileSpace& ts, int bi) {
+    return ts.rect ? 0 : (BM * bi) / BN;
+}
+// The last row block present in column block bj.
+__host__ __device__ __forceinline__ int last_row(const TileSpace& ts, int bj) {
+    const int r = ((bj + 1) * BN - 1) / BM;
+    return ts.rect || r > ts.nbi - 1 ? ts.nbi - 1 : r;
 }
 
-__host__ __device__ __forceinline__ long long count_tiles(const TileSpace& ts) {
+__host__ __device__ __forceinline__ long long tiles_in(const TileSpace& ts, int b0, int b1) {
     long long c = 0;
-    for (int sr = 0; sr < ts.nsr; sr++) c += ts.nbj > first_col(ts, sr) ? ts.nbj - first_col(ts, sr) : 0;
+    for (int bi = b0; bi < b1; bi++) c += ts.nbj > first_col(ts, bi) ? ts.nbj - first_col(ts, bi) : 0;
     return c;
 }
 
-constexpr int MAX_GROUPS = 1024;   // raster groups with a precomputed first tile
+constexpr int MAX_GROUPS = 1024;  // raster groups with a precomputed first tile
 
-// First tile index of every raster group (groups of gs super-rows,
-// column-major inside a group), so a tile's coordinates cost a binary search
-// over groups plus a few steps instead of a walk over the whole stripe.
+// First tile index of every raster group, so a tile's coordinates cost a
+// binary search over groups plus a few steps.
 struct GroupTable {
     int ngroups;
     int first[MAX_GROUPS + 1];
 };
 
-__host__ __device__ __forceinline__ int group_tiles(const TileSpace& ts, int g0, int g1) {
-    int cnt = 0;
-    for (int sr = g0; sr < g1; sr++) cnt += ts.nbj > first_col(ts, sr) ? ts.nbj - first_col(ts, sr) : 0;
-    return cnt;
-}
-
-// t -> (sr, bj).
-__device__ bool tile_coords(const TileSpace& ts, const GroupTable& gt, int t, int* sr_out, int* bj_out) {
-    const int gs = ts.gs;
-    int lo = 0, hi = gt.ngroups;     // last group whose first tile is <= t
+// t -> (bi, bj).
+__device__ bool tile_coords(const TileSpace& ts, const GroupTable& gt, int t, int* bi_out, int* bj_out) {
+    int lo = 0, hi = gt.ngroups;  // last group whose first tile is <= t
     while (hi - lo > 1) {
         const int mid = (lo + hi) / 2;
         if (gt.first[mid] <= t) lo = mid; else hi = mid;
     }
     t -= gt.first[lo];
-    const int g0 = lo * gs, g1 = min(ts.nsr, g0 + gs);
-    // columns where only part of the group lies on or above the diagonal
-    // (super-row sr is present in column bj iff sr * cm <= 2 bj + 1)
+    const int g0 = lo * ts.gs, g1 = min(ts.nbi, g0 + ts.gs);
+    // columns that hold only part of the group (those that cross the diagonal)
     int bj = first_col(ts, g0);
-    for (; !ts.rect && bj < ts.nbj; bj++) {
-        const int rows = min(g1 - 1, (2 * bj + 1) / ts.cm) - g0 + 1;
+    for (; bj < ts.nbj; bj++) {
+        const int rows = min(g1 - 1, last_row(ts, bj)) - g0 + 1;  // rows g0 .. of the group in column bj
         if (rows == g1 - g0) break;  // from here on every column holds the whole group
-        if (rows > 0) {
-            if (t < rows) {
-                *sr_out = g0 + t;
-                *bj_out = bj;
-                return true;
-            }
-            t -= rows;
+        if (t < rows) {
+            *bi_out = g0 + t;
+            *bj_out = bj;
+            return true;
         }
+        t -= rows;
     }
     const int full = g1 - g0;
     bj += t / full;
     if (bj >= ts.nbj) return false;
-    *sr_out = g0 + t % full;
+    *bi_out = g0 + t % full;
     *bj_out = bj;
     return true;
 }
 
-// Tensor maps of every K chunk of the operand: A boxes (128 rows) and B boxes
-// (256 / CM rows), and the 128-byte K blocks of each chunk.
+// Tensor maps of every K chunk: A boxes (128 rows of the pos copy) and B
+// boxes (224 rows of the neg copy), and the 128-byte K blocks of each chunk.
 struct TcMaps {
     CUtensorMap a[kMaxKChunks];
     CUtensorMap b[kMaxKChunks];
@@ -157,50 +156,28 @@ struct TcMaps {
 
 struct TcParams {
     int n, r0, rows;  // columns end at n; rows [r0, r0 + rows) of the A operand
-    int c0;           // first column: r0 (upper triangle) or 0 (rectangle against the B operand)
-    int kblocks, kblocks_p;  // K stages in total and in the presence part
+    int c0;           // first column: r0 (upper triangle) or 0 (rectangle)
+    int kblocks;      // K stages per tile
     TileSpace ts;
     GroupTable gt;
     int num_tiles;
-    const uint32_t* start;
-    const uint32_t* js;
-    int fuse_rare;
-    const int* unsorted;  // optional device flag: non-zero turns the fused subtraction off
-    const uint16_t* rdense;  // dense rare counts of the stripe (row stride ldr, column j at j - r0), or null
+    const uint16_t* rdense;  // dense rare counts (row stride ldr, column j at j - c0), or null
     size_t ldr;
     uint16_t* out;
     size_t ldo;
+    int vec_store;  // 1: 16-byte stores (ldo a multiple of 8, out 16-byte aligned)
     int* err;
 };
 
-__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* __restrict__ js, uint32_t lo, uint32_t hi,
-                                                    uint32_t key) {
-    while (lo < hi) {
-        const uint32_t mid = lo + (hi - lo) / 2;
-        if (__ldg(js + mid) < key) lo = mid + 1; else hi = mid;
-    }
-    return lo;
-}
-
-template <int KIND, int CM>
-__global__ void __launch_bounds__(THREADS, 1)
-tc_stripe_kernel(const __grid_constant__ TcMaps maps,
-                 const TcParams p) {
-    static_assert(CM == 1 || CM == 2, "cluster of 1 or 2 CTAs");
-    constexpr int B_PART = B_BYTES / CM;  // bytes of the B tile this CTA loads per stage
-    const uint32_t rank = CM == 1 ? 0u : cluster_ctarank();
-    const int cid = CM == 1 ? (int)blockIdx.x : (int)cluster_id_x();
-    const int ncl = CM == 1 ? (int)gridDim.x : (int)num_clusters_x();
+__global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_constant__ TcMaps maps, const TcParams p) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
-    // 1024-byte alignment of the swizzled stage buffers
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* stage_a = smem;
     uint8_t* stage_b = smem + STAGES * A_BYTES;
-    uint16_t* epi = (uint16_t*)(smem + STAGES * STAGE_BYTES);
-    uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES + EPI_BYTES);
-    uint64_t* full = bars;                  // STAGES
-    uint64_t* empty = bars + STAGES;        // STAGES
-    uint64_t* tfull = bars + 2 * STAGES;    // 2
+    uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+    uint64_t* full = bars;                     // STAGES
+    uint64_t* empty = bars + STAGES;           // STAGES
+    uint64_t* tfull = bars + 2 * STAGES;       // 2
     uint64_t* tempty = bars + 2 * STAGES + 2;  // 2
     uint64_t* drain = bars + 2 * STAGES + 4;   // 1
     uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 5);
@@ -211,7 +188,7 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], CM);  // released by the MMA warp of every CTA that reads the stage
+            mbar_init(&empty[s], 1);
         }
         for (int a = 0; a < 2; a++) {
             mbar_init(&tfull[a], 1);
@@ -233,9 +210,17 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
     }
     tc_fence_before();
     __syncthreads();
-    if (CM > 1) cluster_sync();  // the peer's barriers exist before any multicast reaches them
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
+    // scale factors 1.0 in every lane of the 32 scale-factor columns, one
+    // epilogue warp per lane quarter, before any MMA reads them
+    if (warp >= 2 && warp < 6) {
+        tmem_fill32(tmem_base + ((uint32_t)((warp & 3) * 32) << 16) + SF_COL, 0x01010101u * kUe8m0One);
+        tmem_wait_st();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
 
     if (warp == 0) {
         // ------------------------------------------------------------ producer
@@ -246,21 +231,16 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
             int issued[STAGES];
             uint32_t issued_ph[STAGES];
             for (int q = 0; q < STAGES; q++) issued[q] = 0, issued_ph[q] = 0;
-            for (int t = cid; ok && t < p.num_tiles; t += ncl) {
-                int sr, bj;
-                if (!tile_coords(p.ts, p.gt, t, &sr, &bj)) break;
-                const int bi = sr * CM + (int)rank;
-                const int y_a = p.r0 + bi * BM, y_b = p.c0 + bj * BN + (int)rank * (BN / CM);
+            for (int t = blockIdx.x; ok && t < p.num_tiles; t += gridDim.x) {
+                int bi, bj;
+                if (!tile_coords(p.ts, p.gt, t, &bi, &bj)) break;
+                const int y_a = p.r0 + bi * BM, y_b = p.c0 + bj * BN;
                 int ch = 0, kbl = 0;  // K chunk and block inside it
                 for (int kb = 0; kb < p.kblocks; kb++) {
                     if (!mbar_wait(&empty[s], ph ^ 1, abort_flag, p.err)) { ok = false; break; }
-                    mbar_expect_tx(&full[s], STAGE_BYTES);  // A + both halves of B land here
+                    mbar_expect_tx(&full[s], STAGE_BYTES);
                     tma_load_2d(&maps.a[ch], &full[s], stage_a + s * A_BYTES, kbl * BK, y_a);
-                    if (CM == 1)
-                        tma_load_2d(&maps.b[ch], &full[s], stage_b + s * B_BYTES, kbl * BK, y_b);
-                    else
-                        tma_load_2d_multicast(&maps.b[ch], &full[s], stage_b + s * B_BYTES + rank * B_PART, kbl * BK,
-                                              y_b, (uint16_t)((1u << CM) - 1));
+                    tma_load_2d(&maps.b[ch], &full[s], stage_b + s * B_BYTES, kbl * BK, y_b);
                     if (++kbl == maps.kblocks[ch]) kbl = 0, ch++;
                     issued[s] = 1;
                     issued_ph[s] = ph;
@@ -286,27 +266,24 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
     } else if (warp == 1) {
         // ------------------------------------------------------------ MMA issuer
         if (lane == 0) {
-            const uint32_t id_pos = KIND == KIND_F8 ? make_idesc(1, 0, 0, BM, BN) : make_idesc(2, 1, 0, BM, BN);
-            const uint32_t id_neg = KIND == KIND_F8 ? make_idesc(1, 0, 1, BM, BN) : make_idesc(2, 1, 0, BM, BN);
+            const uint32_t idesc = make_idesc_mx(kE2M1, 1, BM, BN);
+            const uint32_t sf = tmem_base + SF_COL;
             int s = 0, acc = 0;
             uint32_t ph = 0, aph = 0;
             bool ok = true;
-            for (int t = cid; ok && t < p.num_tiles; t += ncl) {
+            for (int t = blockIdx.x; ok && t < p.num_tiles; t += gridDim.x) {
                 if (!mbar_wait(&tempty[acc], aph ^ 1, abort_flag, p.err)) { ok = false; break; }
                 tc_fence_after();
-                const uint32_t d_tmem = tmem_base + (uint32_t)(acc * BN);
+                const uint32_t d_tmem = tmem_base + (uint32_t)(acc * ACC_STRIDE);
                 for (int kb = 0; kb < p.kblocks; kb++) {
                     if (!mbar_wait(&full[s], ph, abort_flag, p.err)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t a0 = smem_u32(stage_a + s * A_BYTES), b0 = smem_u32(stage_b + s * B_BYTES);
-                    const uint32_t idesc = kb < p.kblocks_p ? id_pos : id_neg;
 #pragma unroll
                     for (int k = 0; k < BK / 32; k++)
-                        tc_mma_f8(d_tmem, sw128_desc(a0 + 32 * k), sw128_desc(b0 + 32 * k), idesc,
-                                     (kb | k) ? 1u : 0u);
-                    // stage free once these MMAs have read it (in every CTA whose B half it holds)
-                    if (CM == 1) tc_commit(&empty[s]);
-                    else tc_commit_multicast(&empty[s], (uint16_t)((1u << CM) - 1));
+                        tc_mma_mxf4(d_tmem, sw128_desc(a0 + 32 * k), sw128_desc(b0 + 32 * k), idesc, sf, sf,
+                                    (kb | k) ? 1u : 0u);
+                    tc_commit(&empty[s]);  // stage free once these MMAs have read it
                     if (++s == STAGES) s = 0, ph ^= 1;
                 }
                 if (!ok) break;
@@ -321,114 +298,76 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
         __syncwarp();
     } else {
         // ------------------------------------------------------------ epilogue
-        const int q = warp & 3;  // TMEM lanes [32 q, 32 q + 32) belong to this warp
-        const int half = (warp - 2) / 4;  // columns [128 half, 128 half + 128) of the tile
-        constexpr int CHUNKS = BN / 32 / 2;
-        uint16_t* stg = epi + (warp - 2) * 32 * EPI_PITCH;
+        const int q = warp & 3;           // TMEM lanes [32 q, 32 q + 32) belong to this warp
+        const int half = (warp - 2) / 4;  // column half of the tile
         const int iend = p.r0 + p.rows;
-        const bool fuse = p.fuse_rare && !(p.unsorted && *p.unsorted);
         const bool dense = p.rdense != nullptr;
         int acc = 0;
         uint32_t aph = 0;
         int bad = 0;
-        for (int t = cid; t < p.num_tiles; t += ncl) {
-            int sr, bj;
-            if (!tile_coords(p.ts, p.gt, t, &sr, &bj)) break;
-            const int bi = sr * CM + (int)rank;
-            const int i0 = p.r0 + bi * BM, j0 = p.c0 + bj * BN;
-            const int my_i = i0 + q * 32 + lane;
-            // this row's rare partners inside the tile: an ascending run of js
-            uint32_t rp = 0, rhi = 0;
-            if (fuse && my_i < iend) {
-                rhi = __ldg(p.start + my_i + 1);
-                rp = lower_bound_u32(p.js, __ldg(p.start + my_i), rhi, (uint32_t)(j0 + half * (BN / 2)));
-            }
-            // the next RBUF partners, fetched together (independent loads);
-            // entries [bpos, nbuf) are still to be applied
-            uint32_t rbuf[RBUF];
-            int bpos = 0, nbuf = 0;
+        for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x) {
+            int bi, bj;
+            if (!tile_coords(p.ts, p.gt, t, &bi, &bj)) break;
+            const int i = p.r0 + bi * BM + q * 32 + lane;  // this lane's row
+            const int j0 = p.c0 + bj * BN;
+            const bool row_ok = i < iend;
+            const size_t orow = (size_t)(i - p.r0) * p.ldo;
+            const size_t rrow = (size_t)(i - p.r0) * p.ldr;
             if (!mbar_wait(&tfull[acc], aph, abort_flag, p.err)) break;
             tc_fence_after();
-            const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN);
+            const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * ACC_STRIDE);
 #pragma unroll 1
-            for (int cc = 0; cc < CHUNKS; cc++) {
-                const int c = half * CHUNKS + cc;
-                const uint32_t cb = (uint32_t)(j0 + c * 32);
-                // this row's dense rare counts for the chunk's 32 columns (64 bytes),
-                // fetched before the accumulator read so the two overlap
-                uint4 rq[4] = {};
-                if (dense && my_i < iend) {
-                    const uint4* src = reinterpret_cast<const uint4*>(p.rdense + (size_t)(my_i - p.r0) * p.ldr +
-                                                                      (size_t)(cb - (uint32_t)p.c0));
-#pragma unroll
-                    for (int u = 0; u < 4; u++) rq[u] = __ldg(src + u);
+            for (int cc = 0; cc < WARP_CHUNKS; cc++) {
+                const int c = half * WARP_CHUNKS + cc;
+                const int cb = j0 + c * CHUNK;  // first column of the chunk
+                const bool live = row_ok && cb < p.n;
+                // this row's rare counts for the chunk (32 bytes), fetched before
+                // the accumulator read so the two overlap; a row of the block is
+                // at least up(n - c0, 16) wide, so a live chunk is in bounds
+                uint4 r4[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+                if (dense && live) {
+                    const uint4* src = reinterpret_cast<const uint4*>(p.rdense + rrow + (size_t)(cb - p.c0));
+                    r4[0] = __ldcs(src);  // read once: streamed past L2
+                    r4[1] = __ldcs(src + 1);
                 }
-                uint32_t v[32];
-                tmem_ld32(tbase + (uint32_t)(c * 32), v);
+                uint32_t v[16];
+                tmem_ld16(tbase + (uint32_t)(c * CHUNK), v);
                 tmem_wait_ld();
-                if (cc == CHUNKS - 1) {  // this warp's part of the accumulator is read: hand it back
+                if (cc == WARP_CHUNKS - 1) {  // this warp's part of the accumulator is read: hand it back
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&tempty[acc]);
                 }
-                // own row -> staging buffer (u16)
-                uint32_t* row32 = reinterpret_cast<uint32_t*>(stg + lane * EPI_PITCH);
+                uint32_t w[8];
 #pragma unroll
-                for (int w = 0; w < 16; w++) {
-                    int x0, x1;
-                    if (KIND == KIND_F8) {
-                        const float f0 = __uint_as_float(v[2 * w]), f1 = __uint_as_float(v[2 * w + 1]);
-                        x0 = __float2int_rn(f0);
-                        x1 = __float2int_rn(f1);
-                        bad |= (__int2float_rn(x0) != f0) | (__int2float_rn(x1) != f1);
-                    } else {
-                        x0 = (int)v[2 * w];
-                        x1 = (int)v[2 * w + 1];
-                    }
-                    if (dense) {
-                        const uint4& r4 = rq[w / 4];
-                        const uint32_t rw = (w % 4 == 0) ? r4.x : (w % 4 == 1) ? r4.y : (w % 4 == 2) ? r4.z : r4.w;
-                        x0 -= (int)(rw & 0xFFFF);
-                        x1 -= (int)(rw >> 16);
-                    }
-                    row32[w] = (uint32_t)(x0 & 0xFFFF) | ((uint32_t)(x1 & 0xFFFF) << 16);
+                for (int e = 0; e < 8; e++) {
+                    const float f0 = __uint_as_float(v[2 * e]), f1 = __uint_as_float(v[2 * e + 1]);
+                    int x0 = __float2int_rn(f0), x1 = __float2int_rn(f1);
+                    bad |= (__int2float_rn(x0) != f0) | (__int2float_rn(x1) != f1);
+                    const uint4& r = r4[e / 4];
+                    const uint32_t rw = (e % 4 == 0) ? r.x : (e % 4 == 1) ? r.y : (e % 4 == 2) ? r.z : r.w;
+                    x0 -= (int)(rw & 0xFFFF);
+                    x1 -= (int)(rw >> 16);
+                    w[e] = (uint32_t)(x0 & 0xFFFF) | ((uint32_t)(x1 & 0xFFFF) << 16);
                 }
-                // rare pairs of this row in columns [cb, cb + 32)
-                for (;;) {
-                    if (bpos == nbuf) {
-                        if (rp >= rhi) break;
-                        nbuf = rhi - rp < (uint32_t)RBUF ? (int)(rhi - rp) : RBUF;
+                if (live) {
+                    uint16_t* dst = p.out + orow + (size_t)(cb - p.c0);
+                    if (cb + CHUNK <= p.n) {
+                        if (p.vec_store) {
+                            uint4* d4 = reinterpret_cast<uint4*>(dst);
+                            __stcs(d4, make_uint4(w[0], w[1], w[2], w[3]));  // written once: streamed
+                            __stcs(d4 + 1, make_uint4(w[4], w[5], w[6], w[7]));
+                        } else {
+                            uint32_t* d1 = reinterpret_cast<uint32_t*>(dst);
 #pragma unroll
-                        for (int q = 0; q < RBUF; q++) rbuf[q] = q < nbuf ? __ldg(p.js + rp + q) : 0xFFFFFFFFu;
-                        rp += (uint32_t)nbuf;
-                        bpos = 0;
-                    }
-                    // ascending: the entries below cb + 32 form a prefix of what is left
-#pragma unroll
-                    for (int q = 0; q < RBUF; q++)
-                        if (q >= bpos && q < nbuf && rbuf[q] < cb + 32) {
-                            // (a shared atomicSub on the 32-bit word measured slower than this
-                            // plain read-modify-write of the lane's own row)
-                            stg[lane * EPI_PITCH + (int)(rbuf[q] - cb)] -= 1;
-                            bpos = q + 1;
+                            for (int e = 0; e < 8; e++) d1[e] = w[e];
                         }
-                    if (bpos < nbuf) break;  // the next partner lies beyond this chunk
-                }
-                __syncwarp();
-                // coalesced store: 16 lanes x 4 bytes per row, 2 rows per step
-#pragma unroll 4
-                for (int st = 0; st < 16; st++) {
-                    const int rr = st * 2 + lane / 16, w = lane % 16;
-                    const int i = i0 + q * 32 + rr;
-                    const int j = (int)cb + 2 * w;
-                    if (i < iend && j < p.n) {
-                        const uint32_t val = reinterpret_cast<const uint32_t*>(stg + rr * EPI_PITCH)[w];
-                        uint16_t* dst = p.out + (size_t)(i - p.r0) * p.ldo + (size_t)(j - p.c0);
-                        if (j + 1 < p.n) *reinterpret_cast<uint32_t*>(dst) = val;
-                        else *dst = (uint16_t)(val & 0xFFFF);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < CHUNK; e++)
+                            if (cb + e < p.n) dst[e] = (uint16_t)(w[e / 2] >> (16 * (e & 1)));
                     }
                 }
-                __syncwarp();
             }
             if (++acc == 2) acc = 0, aph ^= 1;
         }
@@ -437,8 +376,6 @@ tc_stripe_kernel(const __grid_constant__ TcMaps maps,
 
     tc_fence_before();
     __syncthreads();
-    // no CTA leaves while its peer may still multicast into it or arrive on its barriers
-    if (CM > 1) cluster_sync();
     if (warp == 1) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
@@ -460,6 +397,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
+// rows x kb bytes, boxes of 128 bytes of K x box_rows rows, 128-byte swizzle.
 bool make_map(CUtensorMap* m, const uint8_t* X, size_t rows, int kb, int box_rows) {
     auto fn = encode_fn();
     if (!fn) return false;
@@ -472,67 +410,30 @@ bool make_map(CUtensorMap* m, const uint8_t* X, size_t rows, int kb, int box_row
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// The K chunks of an operand (one chunk when it is a single allocation).
-KChunks chunks_of(const ByteOperands& ops) {
-    KChunks ch = ops.chunks;
-    if (ch.n == 0) {
-        ch.p[0] = const_cast<uint8_t*>(ops.X);
-        ch.n = 1;
-        ch.width = ops.kb;
-        ch.kb = ops.kb;
-    }
-    return ch;
-}
+bool same_chunking(const KChunks& x, const KChunks& y) { return x.n == y.n && x.width == y.width && x.kb == y.kb; }
 
-// ops: the A operand (the stripe's rows); bops: the B operand (the columns),
-// the same rows for the upper triangle, another set for a rectangle.
-template <int KIND, int CM>
-cudaError_t launch_kind(const ByteOperands& ops, const ByteOperands& bops, const RareCSR& rare, const StripeArgs& a,
-                        int num_sms, cudaStream_t st) {
+cudaError_t launch_one(const Fp4Operands& A, const Fp4Operands& B, const uint16_t* R, size_t ldr,
+                       const StripeArgs& a, int num_sms, cudaStream_t st) {
     static bool attrs[kMaxDevices] = {};
-    static int max_clusters_of[kMaxDevices] = {};
     const int dev = current_device();
-    bool& attr = attrs[dev];
-    int& max_clusters = max_clusters_of[dev];
-    auto kern = tc_stripe_kernel<KIND, CM>;
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute lattr[1];
-    cfg.blockDim = dim3(THREADS);
-    cfg.dynamicSmemBytes = SMEM_BYTES;
-    cfg.stream = st;
-    if (CM > 1) {
-        lattr[0].id = cudaLaunchAttributeClusterDimension;
-        lattr[0].val.clusterDim.x = CM;
-        lattr[0].val.clusterDim.y = 1;
-        lattr[0].val.clusterDim.z = 1;
-        cfg.attrs = lattr;
-        cfg.numAttrs = 1;
-    }
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (!attrs[dev]) {
+        const cudaError_t e = cudaFuncSetAttribute(tc_stripe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   SMEM_BYTES);
         if (e != cudaSuccess) return e;
-        if (CM > 1) {
-            cfg.gridDim = dim3(CM * std::max(num_sms / CM, 1));
-            e = cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg);
-            if (e != cudaSuccess) return e;
-            if (max_clusters < 1) return cudaErrorInvalidConfiguration;
-        }
-        attr = true;
+        attrs[dev] = true;
     }
-    if ((ops.kb % BK) || (ops.kp % BK) || ops.kb <= 0) return cudaErrorInvalidValue;
-    if (bops.kb != ops.kb || bops.kp != ops.kp) return cudaErrorInvalidValue;
+    const KChunks& ka = A.pos;
+    const KChunks& kb = B.neg;
+    if (A.kb <= 0 || (A.kb % BK) || B.kb != A.kb) return cudaErrorInvalidValue;
+    if (ka.n < 1 || ka.kb != A.kb || !same_chunking(ka, kb) || (ka.width % BK)) return cudaErrorInvalidValue;
     if ((a.ldo & 1) || ((uintptr_t)a.out & 3)) return cudaErrorInvalidValue;
-    if (a.rect && !rare.dense && rare.n_rare > 0) return cudaErrorInvalidValue;  // rectangles take dense counts
-    const KChunks ch = chunks_of(ops), chb = chunks_of(bops);
-    if (ch.kb != ops.kb || (ch.width % BK)) return cudaErrorInvalidValue;
-    if (chb.n != ch.n || chb.width != ch.width || chb.kb != ch.kb) return cudaErrorInvalidValue;
+    if (R && ((ldr & 7) || ((uintptr_t)R & 15))) return cudaErrorInvalidValue;
     TcMaps maps;
-    maps.n = ch.n;
-    for (int c = 0; c < ch.n; c++) {
-        const int wc = ch.width_of(c);
+    maps.n = ka.n;
+    for (int c = 0; c < ka.n; c++) {
+        const int wc = ka.width_of(c);
         if (wc <= 0 || (wc % BK)) return cudaErrorInvalidValue;
-        if (!make_map(&maps.a[c], ch.p[c], ops.n_rows, wc, BM) ||
-            !make_map(&maps.b[c], chb.p[c], bops.n_rows, wc, BN / CM))
+        if (!make_map(&maps.a[c], ka.p[c], A.n_rows, wc, BM) || !make_map(&maps.b[c], kb.p[c], B.n_rows, wc, BN))
             return cudaErrorInvalidValue;
         maps.kblocks[c] = wc / BK;
     }
@@ -541,67 +442,44 @@ cudaError_t launch_kind(const ByteOperands& ops, const ByteOperands& bops, const
     p.r0 = a.r0;
     p.c0 = a.rect ? 0 : a.r0;
     p.rows = a.rows;
-    p.kblocks = ops.kb / BK;
-    p.kblocks_p = ops.kp / BK;
-    p.ts.cm = CM;
-    p.ts.gs = group_row_blocks() / CM;
-    p.ts.nsr = ((a.rows + BM - 1) / BM + CM - 1) / CM;
+    p.kblocks = A.kb / BK;
+    p.ts.gs = group_row_blocks();
+    p.ts.nbi = (a.rows + BM - 1) / BM;
     p.ts.rect = a.rect ? 1 : 0;
     p.ts.nbj = (a.n - p.c0 + BN - 1) / BN;
-    p.num_tiles = (int)count_tiles(p.ts);
+    const long long tiles = tiles_in(p.ts, 0, p.ts.nbi);
+    if (tiles > INT32_MAX) return cudaErrorInvalidValue;
+    p.num_tiles = (int)tiles;
     {
         const int gs = p.ts.gs;
-        p.gt.ngroups = (p.ts.nsr + gs - 1) / gs;
+        p.gt.ngroups = (p.ts.nbi + gs - 1) / gs;
         if (p.gt.ngroups > MAX_GROUPS) return cudaErrorInvalidValue;  // callers split taller stripes
-        int acc = 0;
+        long long acc = 0;
         for (int g = 0; g < p.gt.ngroups; g++) {
-            p.gt.first[g] = acc;
-            acc += group_tiles(p.ts, g * gs, std::min(p.ts.nsr, g * gs + gs));
+            p.gt.first[g] = (int)acc;
+            acc += tiles_in(p.ts, g * gs, std::min(p.ts.nbi, g * gs + gs));
         }
-        p.gt.first[p.gt.ngroups] = acc;
+        p.gt.first[p.gt.ngroups] = (int)acc;
     }
-    p.start = rare.start;
-    p.js = rare.js;
-    p.fuse_rare = (!rare.dense && rare.n_rare > 0 && (rare.sorted || rare.unsorted_flag)) ? 1 : 0;
-    p.unsorted = rare.unsorted_flag;
-    p.rdense = rare.dense;
-    p.ldr = rare.ldr;
-    if (rare.dense && ((rare.ldr & 7) || ((uintptr_t)rare.dense & 15))) return cudaErrorInvalidValue;
+    p.rdense = R;
+    p.ldr = ldr;
     p.out = a.out;
     p.ldo = a.ldo;
+    p.vec_store = ((a.ldo & 7) == 0 && ((uintptr_t)a.out & 15) == 0) ? 1 : 0;
     p.err = a.err;
     if (p.num_tiles == 0) return cudaSuccess;
-    const int clusters = std::min(p.num_tiles, CM > 1 ? max_clusters : std::max(num_sms, 1));
-    cfg.gridDim = dim3(CM * clusters);
-    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, maps, p);
-    if (e != cudaSuccess) return e;
-    if (!rare.dense && rare.n_rare > 0 && !rare.sorted) return launch_rare_atomic(rare, a, st);
-    return cudaSuccess;
-}
-
-// Cluster size of the stripe kernel: 2 (B tile shared by multicast) unless
-// TCH_TC_CLUSTER=1 asks for single CTAs.
-int cluster_size() {
-    static int cm = 0;
-    if (!cm) {
-        const char* v = getenv("TCH_TC_CLUSTER");
-        cm = (v && v[0] == '1') ? 1 : 2;
-    }
-    return cm;
+    const int grid = std::min(p.num_tiles, std::max(num_sms, 1));
+    tc_stripe_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(maps, p);
+    return cudaGetLastError();
 }
 
 }  // namespace
 
-// kind::i8 does not exist on sm_103a (ptxas: "Feature '.kind::i8' not
-// supported on .target 'sm_103a'"), so TCH_KERNEL_TC_I8 is never compiled in.
-bool tc_kernel_compiled(int kernel) { return kernel == TCH_KERNEL_TC_F8; }
-
-cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const ByteOperands* bops, const RareCSR& rare,
+cudaError_t launch_tc_stripe(const Fp4Operands& ops, const Fp4Operands* bops, const uint16_t* R, size_t ldr,
                              const StripeArgs& a, int num_sms, cudaStream_t st) {
     if (a.rows <= 0 || (!a.rect && a.r0 >= a.n) || (a.rect && a.n <= 0)) return cudaSuccess;
     if (a.rect && !bops) return cudaErrorInvalidValue;
-    const ByteOperands& b = bops ? *bops : ops;
-    if (kernel != TCH_KERNEL_TC_F8) return cudaErrorNotSupported;
+    const Fp4Operands& b = bops ? *bops : ops;
     // one launch covers at most MAX_GROUPS raster groups of rows; a taller
     // stripe runs as consecutive sub-stripes writing into the same output
     const int max_rows = MAX_GROUPS * group_row_blocks() * BM;
@@ -611,11 +489,8 @@ cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const ByteOper
         s.rows = std::min(max_rows, a.rows - done);
         const size_t col = a.rect ? 0 : (size_t)done;  // a triangle's columns start at its first row
         s.out = a.out + (size_t)done * a.ldo + col;
-        RareCSR rs = rare;
-        if (rare.dense) rs.dense = rare.dense + (size_t)done * rare.ldr + col;
-        const int cm = (a.cluster == 1 || a.cluster == 2) ? a.cluster : cluster_size();
-        const cudaError_t e = cm == 2 ? launch_kind<KIND_F8, 2>(ops, b, rs, s, num_sms, st)
-                                      : launch_kind<KIND_F8, 1>(ops, b, rs, s, num_sms, st);
+        const uint16_t* Rs = R ? R + (size_t)done * ldr + col : nullptr;
+        const cudaError_t e = launch_one(ops, b, Rs, ldr, s, num_sms, st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;

@@ -11,7 +11,9 @@
 //
 // The scratch (g_noalloc_scratch, TCH_NOALLOC_SCRATCH_BYTES) holds
 //   [0, 256)       the device error word of the call
-//   [256, ...)     the e4m3 operand rows [presence | one-hot] of all n profiles
+//   [256, ...)     the two packed fp4 copies of the operand rows [presence |
+//                  one-hot] of all n profiles (K2 + K1 columns, half a byte
+//                  each, so both copies take one byte per bit column)
 // It is a static device array: the module that holds it is loaded on the
 // first call of this entry point (or at library load when CUDA loads modules
 // eagerly), and a device that has loaded it keeps the memory until the
@@ -110,13 +112,13 @@ extern "C" int tch_stripe_noalloc(int device, int n, const uint8_t* d_O, size_t 
     if (!d_O || !d_P || !d_out || (n_rare && (!d_start || !d_js)) || !d_start)
         return e.set("null device buffer");
     if (((uintptr_t)d_out & 15) != 0) return e.set("output pointer must be 16-byte aligned");
-    if (!tc_kernel_compiled(TCH_KERNEL_TC_F8)) return e.set("the tensor-core kernel is not compiled in");
-
-    const size_t kp = up(K2, 128), kb = kp + up(K1, 128);  // bytes per operand row
+    // rows of K2 presence then K1 one-hot columns (multiples of 1024): kb
+    // bytes per copy, two copies
+    const size_t kb = (K2 + K1) / 2;
     const size_t x_rows = up((size_t)n, 256);
-    const size_t need = kErrBytes + x_rows * kb;
+    const size_t need = kErrBytes + 2 * x_rows * kb;
     if (need > (size_t)TCH_NOALLOC_SCRATCH_BYTES)
-        return e.set("needs %zu bytes of scratch (n=%d padded to %zu rows x %zu bytes); the limit is %zu bytes",
+        return e.set("needs %zu bytes of scratch (n=%d padded to %zu rows x 2 x %zu bytes); the limit is %zu bytes",
                      need, n, x_rows, kb, (size_t)TCH_NOALLOC_SCRATCH_BYTES);
     if (kb > (size_t)INT32_MAX) return e.set("rows too wide");
 
@@ -139,24 +141,29 @@ extern "C" int tch_stripe_noalloc(int device, int n, const uint8_t* d_O, size_t 
     if (ce != cudaSuccess) return fail_queued(st, e, "offset check", ce);
     if (read_error(d_err, st, e)) return 1;
 
-    // 2. bits -> e4m3 operand rows in the scratch array, 3. the stripe
+    // 2. bits -> packed fp4 operand rows in the scratch array, 3. the tile
+    // pass, 4. the partner lists (any order) subtracted with atomics
     BitOperands bits;
     bits.P = reinterpret_cast<const uint32_t*>(d_P);
     bits.O = reinterpret_cast<const uint32_t*>(d_O);
     bits.wP = (int)(K2 / 32);
     bits.wO = (int)(K1 / 32);
-    ce = launch_expand_bits(bits, n, x_rows, X, (int)kb, (int)kp, (int)K2, (int)K1, 0x38, 0x38, st);
-    if (ce != cudaSuccess) return fail_queued(st, e, "operand expansion", ce);
-    ByteOperands ops;
-    ops.X = X;
+    Fp4Operands ops;
     ops.n_rows = x_rows;
     ops.kb = (int)kb;
-    ops.kp = (int)kp;
-    RareCSR rare;  // partner lists in any order: subtracted after the tile pass
+    for (int side = 0; side < 2; side++) {
+        KChunks& k = side ? ops.neg : ops.pos;
+        k.p[0] = X + side * x_rows * kb;
+        k.n = 1;
+        k.width = (int)kb;
+        k.kb = (int)kb;
+    }
+    ce = launch_expand_bits(bits, n, bits.wP, bits.wO, ops, st);
+    if (ce != cudaSuccess) return fail_queued(st, e, "operand expansion", ce);
+    RareCSR rare;
     rare.start = d_start;
     rare.js = d_js;
     rare.n_rare = n_rare;
-    rare.sorted = false;
     StripeArgs a;
     a.n = n;
     a.r0 = r0;
@@ -164,7 +171,8 @@ extern "C" int tch_stripe_noalloc(int device, int n, const uint8_t* d_O, size_t 
     a.out = d_out;
     a.ldo = ldo;
     a.err = d_err;
-    ce = launch_tc_stripe(TCH_KERNEL_TC_F8, ops, nullptr, rare, a, sms, st);
+    ce = launch_tc_stripe(ops, nullptr, nullptr, 0, a, sms, st);
+    if (ce == cudaSuccess && n_rare) ce = launch_rare_atomic(rare, a, st);
     if (ce != cudaSuccess) return fail_queued(st, e, "stripe kernel", ce);
     return read_error(d_err, st, e);
 }

@@ -118,16 +118,17 @@ __global__ void popc_rate(uint32_t seed, int rounds, uint32_t* sink) {
 
 // ------------------------------------------------------------ tcgen05
 enum TcPath { TC_F8 = 0, TC_F4 = 1, TC_NVF4_32 = 2, TC_NVF4_16 = 3 };
-constexpr int TC_M = 128, TC_N = 256;
+constexpr int TC_M = 128, TC_N_MAX = 256;
 constexpr int TC_SF_COL = 256;          // scale factors (fp4) after the accumulator
 constexpr int TC_SMEM = 120 * 1024;     // keeps one CTA per SM
-constexpr int TC_A_BYTES = TC_M * 128, TC_B_BYTES = TC_N * 128;
+constexpr int TC_A_BYTES = TC_M * 128, TC_B_BYTES = TC_N_MAX * 128;
 
-// One stage of operands (A 128 rows, B 256 rows of 128 bytes of K, every
-// byte the same value) issued `iters` x 4 times into one accumulator; then
-// every warp reads back 2 x 32 columns of its lanes and compares them with
-// `expect`.  err bit 1: a mismatch; bit 4: the completion wait timed out.
-template <int P>
+// One stage of operands (A 128 rows, B TC_N rows of 128 bytes of K, every
+// byte the same value) issued `iters` x 4 times into one accumulator of TC_N
+// columns; then every warp reads back its lanes of the first and the last 32
+// columns and compares them with `expect`.  err bit 1: a mismatch; bit 4: the
+// completion wait timed out.
+template <int P, int TC_N>
 __global__ void __launch_bounds__(128, 1) tc_rate(int iters, uint32_t a_word, uint32_t b_word, float expect,
                                                   int* err) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -194,7 +195,7 @@ __global__ void __launch_bounds__(128, 1) tc_rate(int iters, uint32_t a_word, ui
     tc_fence_after();
     if (!*abort_flag) {
         int bad = 0;
-        for (int c0 = 0; c0 < TC_N; c0 += TC_N - 32) {
+        for (int c0 = 0; c0 < TC_N; c0 += TC_N - 32) {  // columns 0-31 and TC_N-32 .. TC_N-1
             uint32_t v[32];
             tmem_ld32(tmem + lanes + (uint32_t)c0, v);
             tmem_wait_ld();
@@ -265,9 +266,9 @@ static int run_popc(Probe& pr) {
     return 0;
 }
 
-template <int P>
+template <int P, int TC_N = 256>
 static int run_tc(Probe& pr, const char* name, uint32_t a_word, uint32_t b_word, double per_mma_product) {
-    CK(cudaFuncSetAttribute(tc_rate<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    CK(cudaFuncSetAttribute(tc_rate<P, TC_N>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
     const int iters = 60000;  // 60000 x 4 x 64 < 2^24: exact in fp32
     const int kmma = P == TC_F8 ? 32 : 64;
     const int sms = pr.prop.multiProcessorCount;
@@ -275,7 +276,7 @@ static int run_tc(Probe& pr, const char* name, uint32_t a_word, uint32_t b_word,
     float ms = 0;
     auto launch = [&](bool warm) {
         const int it = warm ? 100 : iters;
-        tc_rate<P><<<sms, 128, TC_SMEM>>>(it, a_word, b_word, (float)(per_mma_product * it * 4 * kmma), pr.err);
+        tc_rate<P, TC_N><<<sms, 128, TC_SMEM>>>(it, a_word, b_word, (float)(per_mma_product * it * 4 * kmma), pr.err);
     };
     if (time_ms(launch, &ms)) return 1;
     int herr = 0;
@@ -320,6 +321,9 @@ int main(int argc, char** argv) {
     // against pairs of -1.0 (0xAA)
     if (!rc && want(argc, argv, "tc_f8")) rc = run_tc<TC_F8>(pr, "tc_f8_tflops", 0x38383838u, 0xB8B8B8B8u, -1.0);
     if (!rc && want(argc, argv, "tc_f4")) rc = run_tc<TC_F4>(pr, "tc_f4_tflops", 0x22222222u, 0xAAAAAAAAu, -1.0);
+    // the tile shape of the contraction kernel (M128 N224); run alone: tch-peak tc_f4_n224
+    if (!rc && argc > 1 && want(argc, argv, "tc_f4_n224"))
+        rc = run_tc<TC_F4, 224>(pr, "tc_f4_n224_tflops", 0x22222222u, 0xAAAAAAAAu, -1.0);
     // kind::mxf4nvf4 (not in the default set: tch-peak tc_nvf4_32 / tc_nvf4_16)
     if (!rc && argc > 1 && want(argc, argv, "tc_nvf4_32"))
         rc = run_tc<TC_NVF4_32>(pr, "tc_nvf4_32_tflops", 0x22222222u, 0xAAAAAAAAu, -1.0);

@@ -8,8 +8,10 @@
 // A query batch of m new profiles runs on the caller's stream, allocating only
 // from a stream-ordered pool:
 //   ranks      each id looked up in its locus's sorted ids (new ids -> novel)
-//   operand    e4m3 rows in the database's column layout (presence + frequent
-//              one-hot; a novel id is present but matches nothing)
+//   operand    packed fp4 rows in the database's column layout (presence +
+//              frequent one-hot, the A side of the tile pass; a novel id is
+//              present but matches nothing); the database keeps only its
+//              B-side copy (one-hot columns negated)
 //   rare       u16 counts of rare equal alleles against every database row
 //   tile pass  the tcgen05 kernel over the m x n rectangle, subtracting them
 //   q x q      the batch's own upper triangle by a direct count on the calls
@@ -59,19 +61,25 @@ __global__ void query_rank_kernel(const uint64_t* __restrict__ q, int m, int L, 
     }
 }
 
+// +1.0 at column col of row `row` (zeroed before); two columns of one byte
+// belong to different cells, hence the atomic OR on the word.
+__device__ __forceinline__ void set_fp4_one(const KChunks& X, size_t row, size_t col) {
+    uint32_t* w = reinterpret_cast<uint32_t*>(X.at(row, (int)((col >> 1) & ~(size_t)3)));
+    atomicOr(w, kFp4One << (4 * (col & 7)));
+}
+
 __global__ void query_pack_kernel(const uint32_t* __restrict__ xq, int m, int L, const uint64_t* __restrict__ cnt_off,
-                                  const int32_t* __restrict__ col, const uint32_t* __restrict__ base, KChunks X,
-                                  int kp, uint8_t one) {
+                                  const int32_t* __restrict__ col, const uint32_t* __restrict__ base, KChunks X) {
     const size_t total = (size_t)m * L;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
         const uint32_t a = xq[t];
         if (!a) continue;
         const size_t i = t / L;
         const int k = (int)(t % L);
-        *X.at(i, k) = one;
+        set_fp4_one(X, i, (size_t)k);
         if (a == kNovelRank) continue;
         const int32_t c = col[cnt_off[k] + a];
-        if (c >= 0) *X.at(i, kp + (int)base[k] + c) = one;
+        if (c >= 0) set_fp4_one(X, i, (size_t)L + base[k] + (size_t)c);
     }
 }
 
@@ -135,8 +143,12 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
     uint32_t* xq = nullptr;
     uint16_t *R = nullptr, *out = nullptr, *qq = nullptr;
     int* derr = nullptr;
-    KChunks X = enc.X;  // same K layout as the database's rows, m rows
-    for (int c = 0; c < kMaxKChunks; c++) X.p[c] = nullptr;
+    Fp4Operands QX;  // the batch's A-side rows: the database's K layout, m rows
+    QX.pos = enc.X.neg;
+    for (int c = 0; c < kMaxKChunks; c++) QX.pos.p[c] = nullptr;
+    QX.n_rows = mr;
+    QX.kb = enc.kb;
+    KChunks& X = QX.pos;
     cudaError_t ce = cudaSuccess;
     // TCH_VERBOSE=1: device time of each phase on stderr
     const char* vb = getenv("TCH_VERBOSE");
@@ -174,7 +186,7 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
             if (ce != cudaSuccess) goto done;
             mark();
             query_rank_kernel<<<grid, 256, 0, st>>>(dq, m, L, enc.cnt_off, enc.slot_ids, xq);
-            query_pack_kernel<<<grid, 256, 0, st>>>(xq, m, L, enc.cnt_off, enc.col, enc.base, X, enc.kp, 0x38);
+            query_pack_kernel<<<grid, 256, 0, st>>>(xq, m, L, enc.cnt_off, enc.col, enc.base, X);
             ce = cudaGetLastError();
             if (ce != cudaSuccess) goto done;
             RareGroups g;
@@ -189,21 +201,6 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
             ce = launch_rare_query(g, xq, m, R, ldr, db->sms, st);
             mark();
             if (ce != cudaSuccess) goto done;
-            ByteOperands qa, dbb;
-            qa.X = X.p[0];
-            qa.chunks = X;
-            qa.n_rows = mr;
-            qa.kb = enc.kb;
-            qa.kp = enc.kp;
-            dbb.X = enc.X.p[0];
-            dbb.chunks = enc.X;
-            dbb.n_rows = enc.x_rows;
-            dbb.kb = enc.kb;
-            dbb.kp = enc.kp;
-            RareCSR dr;
-            dr.dense = R;
-            dr.ldr = ldr;
-            dr.n_rare = 1;
             StripeArgs a;
             a.n = n;
             a.r0 = 0;
@@ -212,7 +209,7 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
             a.ldo = ldo;
             a.err = derr;
             a.rect = true;
-            ce = launch_tc_stripe(TCH_KERNEL_TC_F8, qa, &dbb, dr, a, db->sms, st);
+            ce = launch_tc_stripe(QX, &enc.X, R, ldr, a, db->sms, st);
             if (ce != cudaSuccess) goto done;
             mark();
             ce = cudaMemcpy2DAsync(h_qdb, (size_t)n * 2, out, ldo * 2, (size_t)n * 2, m, cudaMemcpyDeviceToHost, st);
@@ -339,7 +336,6 @@ int tch_db_create(int device, int n, int L, const uint64_t* calls, int tau, tch_
     if (n < 1 || L < 1) return e.set("the database needs n >= 1 profiles and L >= 1 loci (got n=%d, L=%d)", n, L);
     if (L > 65535) return e.set("more than 65535 loci (u16 distances)");
     if (!calls) return e.set("null input buffer");
-    if (!tc_kernel_compiled(TCH_KERNEL_TC_F8)) return e.set("the tensor-core kernel is not compiled in");
     db = new tch_db();
     db->device = device;
     db->n = n;
@@ -363,12 +359,19 @@ int tch_db_create(int device, int n, int L, const uint64_t* calls, int tau, tch_
             goto fail;
     }
     cudaFree(d_calls);
-    // the database's own triangle is not served: drop its ranks and positions
+    // the database's own triangle is not served: drop its ranks and positions,
+    // and its A-side operand copy (queries are the A side)
     cudaFree(db->enc.x);
     cudaFree(db->enc.mpos);
     db->enc.bytes -= (size_t)n * L * 6;
     db->enc.x = nullptr;
     db->enc.mpos = nullptr;
+    for (int c = 0; c < kMaxKChunks; c++)
+        if (db->enc.X.pos.p[c]) {
+            cudaFree(db->enc.X.pos.p[c]);
+            db->enc.X.pos.p[c] = nullptr;
+            db->enc.bytes -= db->enc.x_rows * (size_t)db->enc.X.pos.width_of(c);
+        }
     *out = db;
     return 0;
 fail:
@@ -400,7 +403,7 @@ void tch_db_destroy(tch_db* db) {
 
 int tch_db_info(const tch_db* db, int* n, int* L, int* tau, size_t* d_onehot, size_t* device_bytes, int* k_chunks) {
     if (!db) return 1;
-    if (k_chunks) *k_chunks = db->enc.X.n;
+    if (k_chunks) *k_chunks = db->enc.X.neg.n;
     if (n) *n = db->n;
     if (L) *L = db->L;
     if (tau) *tau = db->enc.tau;

@@ -90,16 +90,34 @@ struct KChunks {
     }
 };
 
-// Byte operands of the tensor-core kernels: one row = [presence | one-hot],
-// each part padded to a multiple of 128 bytes, row length kb bytes.
-struct ByteOperands {
-    const uint8_t* X = nullptr;  // single-chunk operand (used when chunks.n == 0)
-    size_t n_rows = 0;           // multiple of 256
-    int kb = 0;                  // bytes per row
-    int kp = 0;                  // presence bytes (prefix of the row)
-    int elem_shift = 0;          // log2(elements per byte) for the kernel's type (0 here)
-    KChunks chunks;              // K-split operand (chunks.n > 0)
+// Packed e2m1 operand rows of the tensor-core tile pass.  A row is
+// [presence (kp columns) | frequent one-hot (ko columns) | zeros], K columns
+// in all, a multiple of 256 (one 128-byte swizzle row of K per pipeline
+// stage), two 4-bit elements per byte: column c is the low nibble of byte c/2
+// when c is even, the high nibble when odd; kb = K / 2 bytes per row.  In
+// `pos` every element is 0 or +1.0 (0x2); in `neg` the one-hot columns hold
+// -1.0 (0xA) instead, so that pos_i . neg_j = P_i . P_j - O_i . O_j.  The
+// tile pass reads A rows from pos and B rows from neg.  Both copies are split
+// along K alike (KChunks); either may be absent (p[] null) where a role is
+// never used (a query batch needs only pos, a database only neg).
+constexpr uint32_t kFp4One = 0x2, kFp4MinusOne = 0xA;
+struct Fp4Operands {
+    KChunks pos, neg;
+    size_t n_rows = 0;  // multiple of 256
+    int kb = 0;         // bytes per row (K / 2)
 };
+
+// 8 bits -> 8 nibbles: bit k of x becomes bit 4k of the result.
+__host__ __device__ __forceinline__ uint32_t spread_nibbles(uint32_t x) {
+    x &= 0xFFu;
+    x = (x | (x << 12)) & 0x000F000Fu;
+    x = (x | (x << 6)) & 0x03030303u;
+    x = (x | (x << 3)) & 0x11111111u;
+    return x;
+}
+
+// Columns K of the packed rows for kp presence and ko one-hot columns.
+inline size_t fp4_columns(size_t kp, size_t ko) { return std::max<size_t>(up(kp + ko, 256), 256); }
 
 // Splits kb bytes of K into chunks of at most max_bytes per chunk for `rows`
 // rows (0 = one chunk); returns the chunk width, or 0 if more than
@@ -121,7 +139,6 @@ struct StripeArgs {
     size_t ldo = 0;
     int* err = nullptr;
     bool rect = false;
-    int cluster = 0;  // CTAs per cluster of the tile pass, 1 or 2 (0 = library default)
 };
 
 // ---- k_popc.cu --------------------------------------------------------------------
@@ -135,28 +152,35 @@ cudaError_t launch_rare_check_sorted(const RareCSR& rare, int n, int* d_flag, cu
                                      int r_end = -1);
 
 // ---- k_expand.cu ------------------------------------------------------------------
-// Bit rows -> byte operand rows for the tensor-core kernels.
-//   one = encoding of +1, neg_onehot: encode the one-hot part as -1 (kernels
-//   without a negate bit subtract through the operand itself).
-cudaError_t launch_expand_bits(const BitOperands& bits, int n, size_t n_rows, uint8_t* X, int kb, int kp,
-                               int k_presence_bits, int k_onehot_bits, uint8_t one, uint8_t one_neg,
+// Bit rows (tch_run's layout) -> packed e2m1 operand rows: the first wp words
+// of each P row (presence, kp = 32 wp columns) then the first wo words of each
+// O row (one-hot, 32 wo columns), zeros after; rows n .. n_rows - 1 all zero.
+// X.pos / X.neg as allocated by the caller (n_rows x kb bytes each, chunked).
+cudaError_t launch_expand_bits(const BitOperands& bits, int n, int wp, int wo, const Fp4Operands& X,
                                cudaStream_t st);
-// The same into a K-chunked operand.
-cudaError_t launch_expand_bits_chunked(const BitOperands& bits, int n, size_t n_rows, const KChunks& X, int kp,
-                                       int k_presence_bits, int k_onehot_bits, uint8_t one, uint8_t one_neg,
-                                       cudaStream_t st);
+// Words of the P and O rows that hold a set bit in any row (the rest are
+// zero padding): *wp, *wo.
+cudaError_t used_bit_words(const BitOperands& bits, size_t n_pad, int* wp, int* wo, cudaStream_t st);
+// neg from pos: every non-zero element at column >= kp made -1.0.
+cudaError_t launch_negate_onehot(const Fp4Operands& X, int kp, cudaStream_t st);
+// Allocates the pos and/or neg copies (n_rows x kb bytes each, split along K
+// into chunks of at most max_chunk bytes, 0 = one allocation; their chunk
+// layout is set either way); adds the bytes to *bytes.
+cudaError_t alloc_fp4(Fp4Operands* X, size_t n_rows, int kb, size_t max_chunk, bool pos, bool neg, size_t* bytes);
+void free_fp4(Fp4Operands* X);
 
 // ---- k_tc.cu ----------------------------------------------------------------------
-bool tc_kernel_compiled(int kernel);
-// ops: the rows' operand; bops: the columns' operand (nullptr = ops; required
-// for a rectangle, with the same K layout and chunking as ops).
-cudaError_t launch_tc_stripe(int kernel, const ByteOperands& ops, const ByteOperands* bops, const RareCSR& rare,
+// The tile pass: rows [r0, r0 + rows) of ops (its pos copy) against the
+// columns of bops (its neg copy; nullptr = ops, the upper triangle; required
+// for a rectangle, with the same K layout and chunking), minus the dense rare
+// counts R (row stride ldr, column j at j - c0; nullptr = no rare term).
+cudaError_t launch_tc_stripe(const Fp4Operands& ops, const Fp4Operands* bops, const uint16_t* R, size_t ldr,
                              const StripeArgs& a, int num_sms, cudaStream_t st);
 
 // ---- k_encode.cu ------------------------------------------------------------------
 // Rates of the analytic tau model on this GPU.
 struct TauModel {
-    double gemm_rate = 1.6e15;  // pair x one-byte-column MACs per second of the stripe kernel
+    double gemm_rate = 3.2e15;  // pair x column MACs per second of the fp4 tile pass
     double rare_rate = 6.0e11;  // rare pairs per second of the fused subtraction (pair lists)
     // rare pairs per second of the dense rare-count build, at the margin (its
     // fixed part, the u16 block written per stripe, does not depend on tau)
@@ -189,15 +213,20 @@ cudaError_t launch_rare_query(const RareGroups& g, const uint32_t* xq, int m, ui
                               cudaStream_t st);
 cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R, size_t ldr, int sms,
                               cudaStream_t st);
+// The same block from pair lists (partners of row i: js[start[i] .. start[i +
+// 1]), in any order, repeated once per shared rare allele); a partner outside
+// (i, n) sets DEVERR_RARE_PAIR in *err and is skipped.
+cudaError_t launch_rare_from_lists(const uint32_t* start, const uint32_t* js, int n, int r0, int rows, uint16_t* R,
+                                   size_t ldr, int* err, int sms, cudaStream_t st);
 
 // Operands built on the device from allele calls; device memory owned here.
 struct DeviceEncoding {
     int n = 0, L = 0, tau = 0;
     size_t D = 0;             // frequent one-hot columns
     uint16_t* x = nullptr;    // n x L ranks
-    KChunks X;                // x_rows x kb e4m3 operand rows, split along K
+    Fp4Operands X;            // x_rows packed e2m1 rows [presence (L) | one-hot (D)], split along K
     size_t x_rows = 0;
-    int kb = 0, kp = 0;
+    int kb = 0;               // bytes per row
     uint32_t* start = nullptr;  // n + 1 (CSR mode)
     uint32_t* js = nullptr;     // n_rare, ascending per row (CSR mode)
     size_t n_rare = 0;
@@ -238,11 +267,12 @@ void free_device_encoding(DeviceEncoding* d);
 size_t max_chunk_bytes();
 int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, bool verbose,
                       tch_solver** out, Err& e);
+// lists_uploaded: called by the stripe pipeline after the stripe's partner
+// lists reached the device (solvers that upload them stripe by stripe).
 int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e,
-                  const int* unsorted_flag = nullptr);
+                  bool lists_uploaded = false);
 int solver_check(tch_solver* s, Err& e);
 void solver_free(tch_solver* s);
-void solver_set_cluster(tch_solver* s, int cm);
 int solver_stripe_counts(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, uint16_t* R, size_t ldr,
                          cudaStream_t st, Err& e);
 double solver_work(const tch_solver* s);

@@ -5,11 +5,12 @@
 // convention, the same host fallback for rare pairs that do not fit in device
 // memory (tch.cu:105, 140-144).  Inside it, the work is organised GB300-first:
 //
-//   * operands are uploaded once and, for the tensor-core kernels, expanded
-//     from bits to bytes on the device (k_expand.cu);
-//   * each stripe is ONE fused kernel that writes u16 distances directly:
+//   * operands are uploaded once and, for the tensor-core kernel, expanded
+//     from bits to packed fp4 rows on the device (k_expand.cu);
+//   * each stripe is a rare-count pass (the stripe's pair lists counted into a
+//     u16 block) and ONE fused tile pass that writes u16 distances directly:
 //     P Pt - O Ot accumulates on the tensor pipe (or CUDA cores), the rare
-//     pairs are subtracted inside the tile, and the int32 matrix the
+//     counts are subtracted inside the tile, and the int32 matrix the
 //     reference materialises between its GEMMs, sub_rare and pack_u16 never
 //     exists (3 passes over an int32 stripe -> 0);
 //   * the u16 stripe is copied to pinned host memory on the stripe's own
@@ -92,17 +93,13 @@ static cudaError_t stripe_pool(int device, cudaMemPool_t* out) {
     return cudaSuccess;
 }
 
-static const char* kKernelNames[TCH_KERNEL_COUNT] = {"auto", "popc", "mma_b1", "tc_f8", "tc_i8", "tc_f16"};
+static const char* kKernelNames[TCH_KERNEL_COUNT] = {"auto",  "popc",   "mma_b1", "tc_f8",
+                                                      "tc_i8", "tc_f16", "tc_f4"};
 
-static bool kernel_compiled(int k) {
-    switch (k) {
-        case TCH_KERNEL_POPC: return true;
-        case TCH_KERNEL_TC_F8:
-        case TCH_KERNEL_TC_I8:
-        case TCH_KERNEL_TC_F16: return tc_kernel_compiled(k);
-        default: return false;
-    }
-}
+// Compiled in: the CUDA-core baseline and the fp4 tensor-core kernel.  The b1
+// and s8 warp MMAs issue at ~150 TOPS on GB300, kind::i8 does not exist on
+// sm_103a, and the fp8 kind runs at half the fp4 rate from twice the bytes.
+static bool kernel_compiled(int k) { return k == TCH_KERNEL_POPC || k == TCH_KERNEL_TC_F4; }
 
 static int default_kernel() {
     if (g_kernel < 0) {
@@ -119,16 +116,9 @@ static int default_kernel() {
 // for this problem (fp32 accumulation of 0/+-1 products is exact while every
 // partial sum stays below 2^24; a distance never exceeds the loci count, and
 // the presence part alone bounds every partial sum by L <= 65535).
-static int resolve_kernel(int k) {
-    if (k == TCH_KERNEL_AUTO) {
-        for (int cand : {TCH_KERNEL_TC_F8, TCH_KERNEL_TC_F16, TCH_KERNEL_TC_I8, TCH_KERNEL_POPC})
-            if (kernel_compiled(cand)) return cand;
-        return TCH_KERNEL_POPC;
-    }
-    return k;
-}
+static int resolve_kernel(int k) { return k == TCH_KERNEL_AUTO ? TCH_KERNEL_TC_F4 : k; }
 
-static bool is_tc(int k) { return k == TCH_KERNEL_TC_F8 || k == TCH_KERNEL_TC_I8 || k == TCH_KERNEL_TC_F16; }
+static bool is_tc(int k) { return k == TCH_KERNEL_TC_F4; }
 
 }  // namespace tch
 
@@ -139,9 +129,8 @@ struct tch_solver {
     size_t n_pad = 0, K1 = 0, K2 = 0, D = 0;
     uint32_t* dP = nullptr;  // bit operands (popc kernel)
     uint32_t* dO = nullptr;
-    KChunks xc;              // byte operands of the tensor-core kernels, split along K
-    size_t x_rows = 0;
-    int kb = 0, kp = 0;
+    Fp4Operands X;           // packed fp4 rows of the tensor-core kernel, split along K
+    int kb = 0, kp = 0;      // bytes per row, presence columns
     uint32_t* dStart = nullptr;
     uint32_t* dJs = nullptr;
     size_t n_rare = 0;
@@ -162,7 +151,6 @@ struct tch_solver {
     uint32_t* gmembers = nullptr;
     uint32_t* gmpos = nullptr;
     int gL = 0;                      // loci of the rank rows (>= 1)
-    int cluster = 0;                 // CTAs per cluster of the tile pass (0 = library default)
     int* dErr = nullptr;
     int num_sms = 0;
     size_t bytes = 0;
@@ -183,7 +171,7 @@ void solver_free(tch_solver* s) {
     cudaSetDevice(s->device);
     cudaFree(s->dP);
     cudaFree(s->dO);
-    for (int c = 0; c < s->xc.n; c++) cudaFree(s->xc.p[c]);
+    free_fp4(&s->X);
     cudaFree(s->dStart);
     cudaFree(s->dJs);
     cudaFree(s->dErr);
@@ -201,15 +189,6 @@ void solver_free(tch_solver* s) {
     }
     if (cur >= 0) cudaSetDevice(cur);
     delete s;
-}
-
-// The element encodings of +1 and -1 for each tensor-core kernel's operand type.
-static void tc_encoding(int kernel, uint8_t* one, uint8_t* neg) {
-    switch (kernel) {
-        case TCH_KERNEL_TC_F8: *one = 0x38; *neg = 0xB8; break;  // e4m3 +1 / -1
-        case TCH_KERNEL_TC_I8: *one = 0x01; *neg = 0xFF; break;  // s8 +1 / -1
-        default: *one = 0x01; *neg = 0xFF; break;
-    }
 }
 
 // Operands on the device from the reference's bit layout (host buffers).
@@ -255,29 +234,21 @@ static int solver_from_bits(int device, int n, size_t n_pad, const uint8_t* O, s
         TCH_CK(e, cudaMemcpy(s->dO, O, n_pad * K1 / 8, cudaMemcpyHostToDevice));
     }
     if (is_tc(kernel)) {
-        // [presence | one-hot] bytes per row; each part padded to 128 bytes
-        // (one 128-byte swizzle atom of K per pipeline stage)
+        // packed fp4 rows [presence | one-hot]: only the bit words that hold a
+        // set bit in some row (K2 and K1 carry the reference's padding to 1024)
         BitOperands bits;
         bits.P = s->dP;
         bits.O = s->dO;
         bits.wP = (int)(K2 / 32);
         bits.wO = (int)(K1 / 32);
-        uint8_t one, neg;
-        tc_encoding(kernel, &one, &neg);
-        (void)neg;  // the one-hot part is subtracted by the MMA's negate-B bit
-        s->kp = (int)up(K2, 128);
-        s->kb = s->kp + (int)up(K1, 128);
-        s->x_rows = up((size_t)std::max(n, 1), 256);
-        {
-            const int w = chunk_width_for(s->kb, s->x_rows, max_chunk_bytes());
-            if (!w) { e.set("the operand needs more than %d K chunks", kMaxKChunks); goto fail; }
-            s->xc.kb = s->kb;
-            s->xc.width = w;
-            s->xc.n = (s->kb + w - 1) / w;
-            for (int c = 0; c < s->xc.n; c++)
-                TCH_CK(e, dmalloc(s, (void**)&s->xc.p[c], s->x_rows * (size_t)s->xc.width_of(c)));
-        }
-        TCH_CK(e, launch_expand_bits_chunked(bits, n, s->x_rows, s->xc, s->kp, (int)K2, (int)K1, one, one, 0));
+        int wp = 0, wo = 0;
+        TCH_CK(e, used_bit_words(bits, n_pad, &wp, &wo, 0));
+        s->kp = 32 * wp;
+        s->kb = (int)(fp4_columns((size_t)32 * wp, (size_t)32 * wo) / 2);
+        if (!chunk_width_for(s->kb, up((size_t)std::max(n, 1), 256), max_chunk_bytes()))
+            { e.set("the operand needs more than %d K chunks", kMaxKChunks); goto fail; }
+        TCH_CK(e, alloc_fp4(&s->X, up((size_t)std::max(n, 1), 256), s->kb, max_chunk_bytes(), true, true, &s->bytes));
+        TCH_CK(e, launch_expand_bits(bits, n, wp, wo, s->X, 0));
         TCH_CK(e, cudaDeviceSynchronize());
         cudaFree(s->dP);
         cudaFree(s->dO);
@@ -364,8 +335,8 @@ static int solver_from_input(int device, int n, int L, const uint64_t* calls, co
     if (L > 65535) return e.set("more than 65535 loci (u16 distances)");
     if ((size_t)n * L && !calls && !ranks) return e.set("null input buffer");
     kernel = resolve_kernel(kernel);
-    if (kernel != TCH_KERNEL_TC_F8 || !kernel_compiled(kernel))
-        return e.set("the device encoder feeds the tensor-core kernel (tc_f8); kernel %s is not supported here",
+    if (kernel != TCH_KERNEL_TC_F4)
+        return e.set("the device encoder feeds the tensor-core kernel (tc_f4); kernel %s is not supported here",
                      tch_kernel_name(kernel));
     const int Le = std::max(L, 1);  // no loci: one all-zero column keeps every shape valid
     s = new tch_solver();
@@ -412,13 +383,13 @@ static int solver_from_input(int device, int n, int L, const uint64_t* calls, co
         enc.bytes -= (size_t)n * Le * 2;
     }
     enc.x = nullptr;
-    s->xc = enc.X;
-    s->x_rows = enc.x_rows;
+    s->X = enc.X;
+    enc.X = Fp4Operands();
     s->kb = enc.kb;
-    s->kp = enc.kp;
+    s->kp = Le;
     s->n_pad = enc.x_rows;
-    s->K2 = (size_t)enc.kp;
-    s->K1 = (size_t)(enc.kb - enc.kp);
+    s->K2 = (size_t)Le;
+    s->K1 = (size_t)enc.kb * 2 - (size_t)Le;
     s->D = enc.D;
     s->tau = enc.tau;
     s->dStart = enc.start;
@@ -452,30 +423,16 @@ static RareGroups rare_groups(const tch_solver* s) {
     return g;
 }
 
-static ByteOperands byte_operands(const tch_solver* s) {
-    ByteOperands ops;
-    ops.X = s->xc.p[0];
-    ops.chunks = s->xc;
-    ops.n_rows = s->x_rows;
-    ops.kb = s->kb;
-    ops.kp = s->kp;
-    return ops;
-}
-
-// The tile pass of a dense-rare solver with the stripe's counts in R.
+// The tile pass with the stripe's rare counts in R (nullptr: no rare term).
 static cudaError_t launch_dense_stripe(tch_solver* s, const StripeArgs& a, const uint16_t* R, size_t ldr,
                                        cudaStream_t st) {
-    RareCSR dr;
-    dr.dense = R;
-    dr.ldr = ldr;
-    dr.n_rare = s->n_rare;
-    return launch_tc_stripe(s->kernel, byte_operands(s), nullptr, dr, a, s->num_sms, st);
+    return launch_tc_stripe(s->X, nullptr, R, ldr, a, s->num_sms, st);
 }
 
 int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e,
-                         const int* unsorted_flag) {
+                  bool lists_uploaded) {
     if (r0 < 0 || rows < 0 || r0 > s->n) return e.set("stripe out of range (r0=%d rows=%d n=%d)", r0, rows, s->n);
-    if (s->defer_js && !unsorted_flag) return e.set("partner lists not uploaded (run the whole pipeline)");
+    if (s->defer_js && !lists_uploaded) return e.set("partner lists not uploaded (run the whole pipeline)");
     if (r0 + rows > s->n) rows = s->n - r0;
     if (rows == 0) return 0;
     if (ldo < (size_t)(s->n - r0)) return e.set("ldo %zu < stripe width %d", ldo, s->n - r0);
@@ -488,42 +445,44 @@ int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, 
     a.out = d_out;
     a.ldo = ldo;
     a.err = s->dErr;
-    a.cluster = s->cluster;
-    RareCSR rare;
-    if (!s->rare_on_host) {
-        rare.start = s->dStart;
-        rare.js = s->dJs;
-        rare.n_rare = s->n_rare;
-        rare.sorted = s->sorted;
-        rare.unsorted_flag = unsorted_flag;
-    }
     cudaError_t ce;
-    if (s->dense) {
-        // the stripe's rare counts, from the rare groups, into a block of the pool
-        const size_t ldr = up((size_t)(s->n - r0), kRareDenseAlign);
-        const size_t rbytes = (size_t)rows * ldr * 2;
-        cudaMemPool_t pool;
-        uint16_t* R = nullptr;
-        ce = stripe_pool(s->device, &pool);
-        if (ce == cudaSuccess) ce = cudaMallocFromPoolAsync((void**)&R, rbytes, pool, st);
-        if (ce != cudaSuccess) return e.set("rare counts of the stripe (%zu bytes): %s", rbytes, cudaGetErrorString(ce));
-        ce = launch_rare_dense(rare_groups(s), r0, rows, R, ldr, s->num_sms, st);
-        if (ce == cudaSuccess) ce = launch_dense_stripe(s, a, R, ldr, st);
-        const cudaError_t fe = cudaFreeAsync(R, st);
-        if (ce == cudaSuccess) ce = fe;
-        if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
-        return 0;
-    }
+    const bool lists = !s->dense && !s->rare_on_host && s->n_rare > 0;
     if (s->kernel == TCH_KERNEL_POPC) {
+        RareCSR rare;
+        if (lists) {
+            rare.start = s->dStart;
+            rare.js = s->dJs;
+            rare.n_rare = s->n_rare;
+            rare.sorted = s->sorted;
+        }
         BitOperands ops;
         ops.P = s->dP;
         ops.O = s->dO;
         ops.wP = (int)(s->K2 / 32);
         ops.wO = (int)(s->K1 / 32);
         ce = launch_popc_stripe(ops, rare, a, st);
-    } else {
-        ce = launch_tc_stripe(s->kernel, byte_operands(s), nullptr, rare, a, s->num_sms, st);
+        if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
+        return 0;
     }
+    if (!s->dense && !lists) {  // no rare term on the device
+        ce = launch_dense_stripe(s, a, nullptr, 0, st);
+        if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
+        return 0;
+    }
+    // the stripe's rare counts (from the rare groups or the pair lists) into a
+    // block of the pool, then the tile pass that subtracts them
+    const size_t ldr = up((size_t)(s->n - r0), kRareDenseAlign);
+    const size_t rbytes = (size_t)rows * ldr * 2;
+    cudaMemPool_t pool;
+    uint16_t* R = nullptr;
+    ce = stripe_pool(s->device, &pool);
+    if (ce == cudaSuccess) ce = cudaMallocFromPoolAsync((void**)&R, rbytes, pool, st);
+    if (ce != cudaSuccess) return e.set("rare counts of the stripe (%zu bytes): %s", rbytes, cudaGetErrorString(ce));
+    ce = s->dense ? launch_rare_dense(rare_groups(s), r0, rows, R, ldr, s->num_sms, st)
+                  : launch_rare_from_lists(s->dStart, s->dJs, s->n, r0, rows, R, ldr, s->dErr, s->num_sms, st);
+    if (ce == cudaSuccess) ce = launch_dense_stripe(s, a, R, ldr, st);
+    const cudaError_t fe = cudaFreeAsync(R, st);
+    if (ce == cudaSuccess) ce = fe;
     if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
     return 0;
 }
@@ -740,8 +699,6 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
     uint16_t* dU[2] = {nullptr, nullptr};
     uint16_t* hU[2] = {nullptr, nullptr};
     bool pooled = false;
-    int* dflags = nullptr;  // per row chunk: its partner lists are not ascending (1) / invalid (2)
-    std::vector<int> hflags;
     std::vector<RowChunk> chunks;
     int ci = 0;             // next row chunk
     const bool pull = s->defer_js && host_pages_visible(s->device);
@@ -763,10 +720,6 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
     }
     if (s->defer_js) {
         chunks = row_chunks(n, S);
-        hflags.assign(chunks.size(), 0);
-        TCH_CK(e, cudaMalloc(&dflags, hflags.size() * sizeof(int)));
-        // on stripe stream 0 before the start event, which stream 1 also waits for
-        TCH_CK(e, cudaMemsetAsync(dflags, 0, hflags.size() * sizeof(int), st[0]));
         TCH_CK(e, uploader.start(s, chunks, pull));
     }
     w_setup = wall() - w0;
@@ -779,25 +732,20 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
             const int rows = std::min(S, n - r0), b = (r0 / S) & 1;
             const size_t w = (size_t)(n - r0);
             if (s->defer_js) {
-                // each row chunk of this stripe: its partner lists, uploaded
-                // ahead by the uploader, are checked on the device; its tile pass
-                // and atomic pass read the verdict from the chunk's flag and
-                // write rows and columns from the chunk's first row on (the
-                // stripe's cells below the diagonal are not part of the output)
+                // each row chunk of this stripe, once the uploader has issued the
+                // copy of its partner lists: rare counts (which check every
+                // partner) and the tile pass, writing rows and columns from the
+                // chunk's first row on (the stripe's cells below the diagonal are
+                // not part of the output)
                 for (; ci < (int)chunks.size() && chunks[ci].r0 < r0 + rows; ci++) {
                     cudaEvent_t uploaded = nullptr;
                     TCH_CK(e, uploader.ready(ci, &uploaded));
                     TCH_CK(e, cudaStreamWaitEvent(st[b], uploaded, 0));
-                    RareCSR rc;
-                    rc.start = s->dStart;
-                    rc.js = s->dJs;
-                    rc.n_rare = s->n_rare;
                     const int ca = chunks[ci].r0, cr = chunks[ci].rows;
-                    TCH_CK(e, launch_rare_check_sorted(rc, n, dflags + ci, st[b], ca, ca + cr));
                     const size_t off = (size_t)(ca - r0);
-                    if (solver_stripe(s, ca, cr, dU[b] + off * ldo + off, ldo, st[b], e, dflags + ci)) goto fail;
+                    if (solver_stripe(s, ca, cr, dU[b] + off * ldo + off, ldo, st[b], e, true)) goto fail;
                 }
-            } else if (solver_stripe(s, r0, rows, dU[b], ldo, st[b], e, nullptr)) {
+            } else if (solver_stripe(s, r0, rows, dU[b], ldo, st[b], e, false)) {
                 goto fail;
             }
             TCH_CK(e, cudaMemcpy2DAsync(hU[b], w * 2, dU[b], ldo * 2, w * 2, rows, cudaMemcpyDeviceToHost, st[b]));
@@ -826,14 +774,6 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
     TCH_CK(e, cudaEventElapsedTime(&ms, t0, t1));
     if (gpu_secs) *gpu_secs = ms / 1e3;
     if (solver_check(s, e)) goto fail;
-    if (dflags) {
-        TCH_CK(e, cudaMemcpy(hflags.data(), dflags, hflags.size() * sizeof(int), cudaMemcpyDeviceToHost));
-        for (int f : hflags)
-            if (f & 2) {
-                e.set("rare CSR: a partner j is not in (i, n)");
-                goto fail;
-            }
-    }
     if (verbose()) {
         double up_s;
         {
@@ -854,13 +794,10 @@ fail:
         if (done[b]) cudaEventDestroy(done[b]);
     }
     pinned_release(hU, pooled);
-    if (dflags) cudaFree(dflags);
     if (t0) cudaEventDestroy(t0);
     if (t1) cudaEventDestroy(t1);
     return rc;
 }
-
-void solver_set_cluster(tch_solver* s, int cm) { s->cluster = cm; }
 
 // A stripe with the rare-count block in caller memory R (dense-rare solvers;
 // others take the ordinary path): no allocation, so it can be captured.
@@ -881,7 +818,6 @@ int solver_stripe_counts(tch_solver* s, int r0, int rows, uint16_t* d_out, size_
     a.out = d_out;
     a.ldo = ldo;
     a.err = s->dErr;
-    a.cluster = s->cluster;
     cudaError_t ce = launch_rare_dense(rare_groups(s), r0, rows, R, ldr, s->num_sms, st);
     if (ce == cudaSuccess) ce = launch_dense_stripe(s, a, R, ldr, st);
     if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
@@ -1053,7 +989,7 @@ int tch_solver_info(const tch_solver* s, tch_info* info) {
     info->n_rare = s->n_rare;
     info->rare_sorted = s->sorted ? 1 : 0;
     info->device_bytes = s->bytes;
-    info->k_chunks = s->xc.n;
+    info->k_chunks = is_tc(s->kernel) ? s->X.pos.n : 0;
     info->rare_dense = s->dense ? 1 : 0;
     return 0;
 }

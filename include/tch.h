@@ -74,7 +74,10 @@ int tch_run(int device, int n, size_t n_pad, const uint8_t* O, size_t K1, const 
 #define TCH_VERSION 1
 
 /* Contraction kernels.  AUTO picks the fastest one measured on GB300 that is
- * exact for the problem's size. */
+ * exact for the problem's size.  Compiled into this library: POPC and TC_F4;
+ * the others name paths measured by the peak probe and not built (the b1 and
+ * s8 warp MMAs issue at ~150 TOPS on GB300, kind::i8 does not exist on
+ * sm_103a, the fp8 kind runs at half the fp4 rate). */
 enum tch_kernel {
     TCH_KERNEL_AUTO = 0,
     TCH_KERNEL_POPC = 1, /* CUDA cores: LOP3 AND + popcount on the bit-packed rows */
@@ -82,11 +85,12 @@ enum tch_kernel {
     TCH_KERNEL_TC_F8 = 3, /* tcgen05.mma kind::f8f6f4, e4m3 0/+-1, TMEM fp32     */
     TCH_KERNEL_TC_I8 = 4, /* tcgen05.mma kind::i8, s8 0/+-1, TMEM s32           */
     TCH_KERNEL_TC_F16 = 5, /* tcgen05.mma kind::f16, bf16 0/+-1, TMEM fp32       */
-    TCH_KERNEL_COUNT = 6
+    TCH_KERNEL_TC_F4 = 6, /* tcgen05.mma kind::mxf4 (scales 1.0), e2m1 0/+-1, TMEM fp32 */
+    TCH_KERNEL_COUNT = 7
 };
 
 int tch_version(void);
-/* Name of a kernel id ("popc", "tc_f8", ...), or "?" */
+/* Name of a kernel id ("popc", "tc_f4", ...), or "?" */
 const char* tch_kernel_name(int kernel);
 /* 1 if `kernel` was compiled into this library. */
 int tch_kernel_available(int kernel);
@@ -102,8 +106,8 @@ typedef struct tch_info {
     int tau;           /* frequency threshold (0 when unknown) */
     int kernel;        /* enum tch_kernel actually used */
     size_t n_pad;      /* padded row count of the device operands */
-    size_t k_presence; /* presence columns on the device (padded) */
-    size_t k_onehot;   /* one-hot columns on the device (padded) */
+    size_t k_presence; /* presence columns of the device operand rows */
+    size_t k_onehot;   /* the rest of a row's columns: one-hot and padding */
     size_t d_onehot;   /* frequent one-hot columns before padding (0 if unknown) */
     size_t n_rare;     /* rare equal pairs */
     int rare_sorted;   /* 1 if every row's partner list is ascending */
@@ -253,8 +257,8 @@ void tch_server_destroy(tch_server* sv);
  * (tch_batch_layout; offsets[count] = total u16 elements), cell (i, j), i < j,
  * at (i * ld[s] + j).  The launches of all sets are spread over parallel
  * streams and captured once as a CUDA graph (per output buffer), replayed on
- * every later run; tch_batch_tune times every schedule (branch streams x
- * tile-pass cluster size for small and large sets) and keeps the fastest.
+ * every later run; tch_batch_tune times every schedule (the number of branch
+ * streams) and keeps the fastest.
  * Errors found on the device are reported by tch_batch_check. */
 typedef struct tch_batch tch_batch;
 int tch_batch_create(int device, int count, const int* n, const int* L, const uint64_t* const* calls, const int* tau,
@@ -265,9 +269,9 @@ int tch_batch_layout(const tch_batch* b, size_t* offsets, size_t* ld);
 int tch_batch_run(tch_batch* b, uint16_t* d_out, void* stream, char* err, int errlen);
 int tch_batch_check(tch_batch* b, char* err, int errlen);
 int tch_batch_tune(tch_batch* b, uint16_t* d_out, void* stream, int reps, double* best_ms, int* best_branches,
-                   int* best_cm_small, int* best_cm_large, char* err, int errlen);
-int tch_batch_set_schedule(tch_batch* b, int branches, int cm_small, int cm_large);
-int tch_batch_info(const tch_batch* b, int* count, int* taus, int* branches, int* cm_small, int* cm_large);
+                   char* err, int errlen);
+int tch_batch_set_schedule(tch_batch* b, int branches);
+int tch_batch_info(const tch_batch* b, int* count, int* taus, int* branches);
 void tch_batch_destroy(tch_batch* b);
 
 /* Fill *info. */
@@ -339,10 +343,11 @@ void tch_solver_destroy(tch_solver* s);
  *           rows i and columns max(i, r0) <= j < n; ldo even, d_out 16-byte
  *           aligned
  *
- * The e4m3 operand rows of all n profiles and the device error word live in
- * one static device array of TCH_NOALLOC_SCRATCH_BYTES bytes, so the call
- * fails with a clear message when 256 + up(n, 256) * (K2 + K1) bytes exceed
- * it (one byte per bit column; e.g. n = 2 048 with K2 + K1 up to 32 768).
+ * The two packed fp4 copies of the operand rows of all n profiles and the
+ * device error word live in one static device array of
+ * TCH_NOALLOC_SCRATCH_BYTES bytes, so the call fails with a clear message when
+ * 256 + up(n, 256) * (K2 + K1) bytes exceed it (one byte per bit column; e.g.
+ * n = 2 048 with K2 + K1 up to 32 768).
  * The first call on a device takes the array's address (cudaGetSymbolAddress)
  * and must come before any stream capture.  Every call reuses the array, so
  * calls that overlap on the GPU race; the call synchronises `stream` before it

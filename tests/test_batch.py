@@ -71,7 +71,7 @@ def test_batch_autotune_keeps_results(tch):
         b.run(out.data_ptr(), stream)
         b.check()
         check_all(sets, out.cpu().numpy().view(np.uint16), off, ld)
-        b.set_schedule(3, 1, 2)
+        b.set_schedule(3)
         out.zero_()
         b.run(out.data_ptr(), stream)
         b.check()

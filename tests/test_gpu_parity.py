@@ -19,7 +19,7 @@ def tch(pkg):
 
 
 def kernels(tch):
-    return [k for k in ("popc", "tc_f8", "tc_i8", "tc_f16", "mma_b1") if tch.kernel_available(k)]
+    return [k for k in ("popc", "tc_f4", "tc_f8", "tc_i8", "tc_f16", "mma_b1") if tch.kernel_available(k)]
 
 
 def upper_equal(H, ref):
@@ -252,7 +252,7 @@ def test_k_chunked_operand(tch):
         # rows are ~18.4 KB long and padded to 1024 rows: chunks of 2.5 KB / 8 KB of K
         for limit in (1024 * 2560, 1024 * 8192):
             tch.set_max_chunk_bytes(limit)
-            with tch.Solver.from_encoding(enc, kernel="tc_f8") as s:
+            with tch.Solver.from_encoding(enc, kernel="tc_f4") as s:
                 info = s.info()
                 H, _ = s.run(256)
             assert 1 < info["k_chunks"] <= 8
@@ -264,6 +264,6 @@ def test_k_chunked_operand(tch):
             upper_equal(H, ref)
         tch.set_max_chunk_bytes(1024)  # would need far more than 8 chunks
         with pytest.raises(tch.TchError, match="chunks"):
-            tch.Solver.from_encoding(enc, kernel="tc_f8")
+            tch.Solver.from_encoding(enc, kernel="tc_f4")
     finally:
         tch.set_max_chunk_bytes(0)
