@@ -397,6 +397,114 @@ def batch_bench(tch, args, device):
             "encode_s": build_s, "tune_s": tune_s}
 
 
+def picks(tch, A, device):
+    """The analytic and the learned model's tau for a profile set, from the
+    library's candidate rows; None without a shipped model."""
+    if not os.path.exists(tch.TAU_MLP_PATH):
+        return None
+    w = tch.load_tau_mlp()
+    taus, feats, est = tch.tau_features(A, device)
+    return {"analytic": int(taus[int(np.argmin(est))]),
+            "learned": int(taus[int(np.argmin(tch.mlp_predict(w, feats, device)))])}
+
+
+def big_config_bench(tch, synth, args, device):
+    """The all-frequent and the large-Zipf shapes (the reference's L4 could not
+    hold the first on its tensor cores: ~250 k one-hot columns).
+
+    founders   50 000 x 5 000 loci, 50 founder alleles per locus, 1 %
+               mutations to fresh ids, 2 % missing: device encoder with the
+               operand split along K into allocations of at most
+               --founders-chunk-mb, the whole upper triangle in one stripe.
+    zipf_big   200 000 x 3 000 loci, Zipf(1.1): the upper triangle (2.0e10
+               pairs, 40 GB of u16) in stripes of --big-stripe rows written
+               into one reused device buffer.
+    Each: pairs/s of the device-resident solve (CUDA events; the step is the
+    whole triangle) at the learned model's tau and at the analytic model's
+    tau, and spread rows of the last stripe against the oracle's count on the
+    raw ids."""
+    import torch
+
+    oracle = load_oracle()
+    out_legs = {}
+    stream = torch.cuda.Stream(device=device)
+    sp = stream.cuda_stream
+    for name in ("founders", "zipf_big"):
+        t0 = time.perf_counter()
+        A = synth.make(name)
+        gen_s = time.perf_counter() - t0
+        n, L = A.shape
+        pairs = n * (n - 1) // 2
+        chunk = (args.founders_chunk_mb << 20) if name == "founders" else 0
+        S = n if name == "founders" else min(n, args.big_stripe)
+        ldo = (n + 7) // 8 * 8
+        stripes = [(r0, min(S, n - r0)) for r0 in range(0, n, S)]
+        pk = picks(tch, A, device) or {}
+        variants = [("learned", 0)] if pk else []
+        variants.append(("analytic", pk.get("analytic", 0)))
+        leg = {"shape": f"{n} x {L}", "pairs": pairs, "stripe_rows": S, "stripes": len(stripes),
+               "chunk_limit_bytes": chunk, "generate_s": gen_s, "picks": pk}
+        for vname, vtau in variants:
+            if vname == "analytic" and pk:
+                tch.set_tau_mlp(None)  # vtau is the analytic pick: nothing learned is consulted
+            tch.set_max_chunk_bytes(chunk)
+            try:
+                t0 = time.perf_counter()
+                s = tch.Solver.from_calls(A, tau=vtau, device=device)
+                enc_s = time.perf_counter() - t0
+            finally:
+                tch.set_max_chunk_bytes(0)
+                if pk:
+                    tch.load_tau_mlp()
+            with s:
+                info = s.info()
+                buf = torch.empty((S, ldo), dtype=torch.int16, device=f"cuda:{device}")
+
+                def solve():
+                    for r0, rows in stripes:
+                        s.stripe(r0, rows, buf.data_ptr(), ldo, sp)
+
+                with torch.cuda.stream(stream):
+                    solve()  # warm-up
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                reps = 2
+                e0.record(stream)
+                for _ in range(reps):
+                    solve()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                s.check()
+                ms = e0.elapsed_time(e1) / reps
+                k_alg = L + int(info["d_onehot"])
+                v = {"tau": info["tau"], "ms": ms, "pairs_per_s": pairs / (ms / 1e3),
+                     "onehot_columns": int(info["d_onehot"]), "k_chunks": int(info["k_chunks"]),
+                     "device_gb": info["device_bytes"] / 1e9, "rare_pairs": int(info["n_rare"]),
+                     "ops_per_step": 2.0 * pairs * k_alg,
+                     "whole_step_tflops": 2.0 * pairs * k_alg / (ms / 1e3) / 1e12, "encode_s": enc_s}
+                if vname == variants[0][0]:
+                    # the last stripe's rows against the oracle (raw ids, no ranking)
+                    r0, rows = stripes[-1]
+                    idx = sorted(set(np.linspace(r0, r0 + rows - 2, 24).astype(int).tolist()))
+                    bad = cells = 0
+                    for i in idx:
+                        got = buf[i - r0, i + 1 - r0:n - r0].cpu().numpy().view(np.uint16)
+                        want = oracle.hamming_block_calls(A, i, i + 1, i + 1, n)[0]
+                        cells += got.size
+                        bad += int((got != want).sum())
+                    v["parity"] = {"rows": len(idx), "cells": cells, "mismatches": bad,
+                                   "oracle": "orc_hamming_block_u64 (check.py:39-44 restated in C, on the raw ids)"}
+                leg[vname] = v
+                del buf
+            torch.cuda.empty_cache()
+        first = leg[variants[0][0]]
+        leg.update(ms=first["ms"], pairs_per_s=first["pairs_per_s"], parity=first.get("parity"))
+        log(name, leg)
+        out_legs[name] = leg
+        del A
+    return out_legs
+
+
 def step_timing(tch, synth, args, device):
     """--step-timing: the two passes of one whole-triangle solve of the
     long-tail generator at --n profiles and --tau (rare counts, then the tile
@@ -501,6 +609,10 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-tsv", action="store_true")
+    ap.add_argument("--no-big", action="store_true", help="skip the founders and zipf_big legs")
+    ap.add_argument("--founders-chunk-mb", type=int, default=2048,
+                    help="largest single allocation of the founders operand (K chunks)")
+    ap.add_argument("--big-stripe", type=int, default=16384, help="rows per stripe of the zipf_big leg")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--serve-db", type=int, default=200000)
     ap.add_argument("--serve-requests", type=int, default=100)
@@ -670,7 +782,9 @@ def main():
         os.environ["TCH_VERBOSE"] = "1"  # phase breakdown on stderr
         tch.set_kernel(args.kernel)
         # the host path uploads every rare pair: its tau model charges the upload
-        tau_host = args.tau or tch.choose_tau(x, nd, args.stripe, tch.free_vram(device), 1.6e15, 1.0e11)
+        # (the tile pass's column MACs per second; pairs per second of the
+        # upload at the host link's ~190 GB/s, 4 bytes each)
+        tau_host = args.tau or tch.choose_tau(x, nd, args.stripe, tch.free_vram(device), 2.9e15, 4.5e10)
         enc = tch.encode_host(x, nd, tau_host)  # the reference host's encoding, outside the timed region
         h2d = enc.O.nbytes + enc.P.nbytes + enc.start.nbytes + enc.js.nbytes
         d2h = sum(min(args.stripe, n - r0) * (n - r0) * 2 for r0 in range(0, n, args.stripe))
@@ -784,6 +898,10 @@ def main():
         batched = batch_bench(tch, args, device)
         log("batched:", batched)
 
+    big = None
+    if not args.no_big:
+        big = big_config_bench(tch, synth, args, device)
+
     cpu = None
     if not args.no_cpu:
         st = max(1, args.ref_stride)
@@ -802,7 +920,7 @@ def main():
             "gpu_launches": args.steps * launches_per_step, "step_split": split, "parity": parity,
             "clocks": ck, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "e2e_device_encoder": e2e_calls, "tau_choice": tau_cmp, "tsv_writer": tsv, "batched": batched,
-            "serving": serving, "peak_probe": peak_info}
+            "big_configs": big, "serving": serving, "peak_probe": peak_info}
     print(json.dumps(line), flush=True)
 
 

@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
             }
             __syncthreads();
             uint4* dst = Rrow + ((wb - cbeg) >> 3);
-            for (int w = tid; w < nq; w += T) __stcs(dst + w, smem_rd[w]);  // streamed: keeps the members in L2
+            for (int w = tid; w < nq; w += T) dst[w] = smem_rd[w];
             __syncthreads();
         }
     }
@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
             }
             __syncthreads();
             uint4* dst = Rrow + (wb >> 3);
-            for (int w = tid; w < nq; w += T) __stcs(dst + w, smem_rd[w]);  // streamed: keeps the members in L2
+            for (int w = tid; w < nq; w += T) dst[w] = smem_rd[w];
             __syncthreads();
         }
     }
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(1024, 1)
             }
             __syncthreads();
             uint4* dst = Rrow + ((wb - cbeg) >> 3);
-            for (int w = tid; w < nq; w += blockDim.x) __stcs(dst + w, smem_rd[w]);
+            for (int w = tid; w < nq; w += blockDim.x) dst[w] = smem_rd[w];
             __syncthreads();
         }
     }

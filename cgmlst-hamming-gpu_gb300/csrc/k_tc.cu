@@ -30,7 +30,7 @@
 //                            read) -> u16 -> 32-byte stores from registers
 // TMEM: accumulators at columns 0 and 256, the scale factors (1.0, written
 // once by the epilogue warps before the first MMA) in columns 480-511.
-// Tiles are visited in raster groups of 16 row blocks, column-major inside a
+// Tiles are visited in raster groups of 8 row blocks, column-major inside a
 // group, so that the CTAs running at the same time share A and B tiles in L2.
 //
 // Every mbarrier wait is bounded (about 2 s of %globaltimer); on a timeout the
@@ -60,7 +60,7 @@ constexpr int SF_COL = 480;         // 32 TMEM columns of scale factors
 constexpr int TMEM_COLS = 512;
 constexpr int CHUNK = 16;           // accumulator columns per tcgen05.ld
 constexpr int WARP_CHUNKS = BN / CHUNK / 2;  // chunks per epilogue warp (its column half)
-constexpr int GROUP_M = 16;         // row blocks per raster group (default; TCH_TC_GROUP overrides)
+constexpr int GROUP_M = 8;          // row blocks per raster group (default; TCH_TC_GROUP overrides)
 constexpr int BAR_BYTES = 256;
 constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + BAR_BYTES;
 static_assert(SMEM_BYTES <= 232448, "shared memory per CTA");
@@ -327,8 +327,8 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
                 uint4 r4[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
                 if (dense && live) {
                     const uint4* src = reinterpret_cast<const uint4*>(p.rdense + rrow + (size_t)(cb - p.c0));
-                    r4[0] = __ldcs(src);  // read once: streamed past L2
-                    r4[1] = __ldcs(src + 1);
+                    r4[0] = __ldg(src);
+                    r4[1] = __ldg(src + 1);
                 }
                 uint32_t v[16];
                 tmem_ld16(tbase + (uint32_t)(c * CHUNK), v);
@@ -355,8 +355,8 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
                     if (cb + CHUNK <= p.n) {
                         if (p.vec_store) {
                             uint4* d4 = reinterpret_cast<uint4*>(dst);
-                            __stcs(d4, make_uint4(w[0], w[1], w[2], w[3]));  // written once: streamed
-                            __stcs(d4 + 1, make_uint4(w[4], w[5], w[6], w[7]));
+                            d4[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                            d4[1] = make_uint4(w[4], w[5], w[6], w[7]);
                         } else {
                             uint32_t* d1 = reinterpret_cast<uint32_t*>(dst);
 #pragma unroll

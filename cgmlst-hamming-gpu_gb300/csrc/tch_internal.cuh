@@ -180,11 +180,13 @@ cudaError_t launch_tc_stripe(const Fp4Operands& ops, const Fp4Operands* bops, co
 // ---- k_encode.cu ------------------------------------------------------------------
 // Rates of the analytic tau model on this GPU.
 struct TauModel {
-    double gemm_rate = 3.2e15;  // pair x column MACs per second of the fp4 tile pass
-    double rare_rate = 6.0e11;  // rare pairs per second of the fused subtraction (pair lists)
+    // pair x column MACs per second of the fp4 tile pass (63 005 x 1 142
+    // long-tail profiles: 3.0e15 at tau 1 024, 2.85e15 at 2 048)
+    double gemm_rate = 2.9e15;
+    double rare_rate = 1.0e12;  // rare pairs per second of the pair-list counts (pair lists)
     // rare pairs per second of the dense rare-count build, at the margin (its
     // fixed part, the u16 block written per stripe, does not depend on tau)
-    double dense_rate = 1.8e12;
+    double dense_rate = 1.5e12;
 };
 
 // The rare alleles as groups of rows, kept on the device: the dense rare

@@ -73,6 +73,32 @@ void orc_hamming_block(const uint16_t* x, int64_t n, int64_t L, int64_t i0, int6
     }
 }
 
+/* The same count on raw allele ids (u64, 0 = missing): equality of ids is
+ * what the ranks encode, so this equals orc_hamming_block on the ranks of x,
+ * without ranking a large matrix first. */
+static inline uint16_t pair_dist_u64(const uint64_t* restrict a, const uint64_t* restrict b, int64_t L) {
+    uint16_t d = 0;
+    for (int64_t k = 0; k < L; k++) d += (uint16_t)((a[k] != b[k]) & (a[k] != 0) & (b[k] != 0));
+    return d;
+}
+
+void orc_hamming_block_u64(const uint64_t* x, int64_t n, int64_t L, int64_t i0, int64_t i1, int64_t j0,
+                           int64_t j1, uint16_t* out, int64_t ldo, int threads) {
+    (void)n;
+    const int64_t TI = 8, TJ = 64;
+    const int64_t nti = (i1 - i0 + TI - 1) / TI, ntj = (j1 - j0 + TJ - 1) / TJ;
+    const int nt = pick_threads(threads);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int64_t t = 0; t < nti * ntj; t++) {
+        const int64_t bi = i0 + (t / ntj) * TI, bj = j0 + (t % ntj) * TJ;
+        const int64_t ei = bi + TI < i1 ? bi + TI : i1, ej = bj + TJ < j1 ? bj + TJ : j1;
+        for (int64_t i = bi; i < ei; i++) {
+            const uint64_t* a = x + i * L;
+            for (int64_t j = bj; j < ej; j++) out[(i - i0) * ldo + (j - j0)] = pair_dist_u64(a, x + j * L, L);
+        }
+    }
+}
+
 /* Upper-triangle pairs only: rows [i0, i1), columns j in (i, n). Returns the
  * number of pairs evaluated; the distances are folded into *sum so the work
  * cannot be optimised away. This is the CPU baseline's unit of work. */

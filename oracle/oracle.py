@@ -72,6 +72,8 @@ def lib():
         L.orc_hamming_block.restype = None
         L.orc_upper_rows.argtypes = [u16p, i64, i64, i64, i64, u64p, ctypes.c_int]
         L.orc_upper_rows.restype = i64
+        L.orc_hamming_block_u64.argtypes = [u64p, i64, i64, i64, i64, i64, i64, u16p, i64, ctypes.c_int]
+        L.orc_hamming_block_u64.restype = None
         L.orc_upper_rows_step.argtypes = [u16p, i64, i64, i64, i64, u64p, ctypes.c_int]
         L.orc_upper_rows_step.restype = i64
         L.orc_rollhash_stripe.argtypes = [ctypes.c_uint64, u16p, i64, i64, i64]
@@ -366,6 +368,18 @@ def hamming_block(x: np.ndarray, i0: int, i1: int, j0: int, j1: int, threads: in
     out = np.zeros((i1 - i0, j1 - j0), dtype=np.uint16)
     if out.size and L:
         lib().orc_hamming_block(_u16p(x), n, L, i0, i1, j0, j1, _u16p(out), j1 - j0, threads)
+    return out
+
+
+def hamming_block_calls(calls: np.ndarray, i0: int, i1: int, j0: int, j1: int, threads: int = 0) -> np.ndarray:
+    """hamming_block on raw u64 allele ids (0 = missing): the same count
+    (check.py:39-44 compares ids for equality) without ranking them first."""
+    c = np.ascontiguousarray(calls, dtype=np.uint64)
+    n, L = c.shape
+    out = np.zeros((i1 - i0, j1 - j0), dtype=np.uint16)
+    if out.size and L:
+        lib().orc_hamming_block_u64(c.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), n, L, i0, i1, j0, j1,
+                                    _u16p(out), j1 - j0, threads)
     return out
 
 

@@ -158,3 +158,15 @@ def test_write_matrix_text():
     assert oracle.write_matrix(["a", "b"], H) == "cgmlst-hamming-gpu\ta\tb\na\t0\t3\nb\t3\t0\n"
     assert oracle.write_matrix(["a", "b"], H, mode="lower-tri", osep=",") == "cgmlst-hamming-gpu,a,b\na,0,0\nb,3,0\n"
     assert oracle.write_matrix(["a", "b"], H, mode="upper-tri", cap=2, index_name="x") == "x\ta\tb\na\t0\t2\nb\t0\t0\n"
+
+
+def test_block_on_raw_ids_equals_block_on_ranks():
+    """The oracle's count on raw 64-bit ids (used where ranking a large matrix
+    first would cost more than the check) equals its count on the ranks."""
+    rng = np.random.default_rng(12)
+    A = rng.integers(0, 7, size=(260, 33)).astype(np.uint64) * np.uint64(2**40 + 3)
+    A[:, 5] = rng.integers(2**62, 2**63, size=260, dtype=np.uint64)
+    x = oracle.dense_ranks(A)[0]
+    for i0, i1, j0, j1 in [(0, 260, 0, 260), (7, 19, 100, 259), (259, 260, 0, 1)]:
+        np.testing.assert_array_equal(oracle.hamming_block_calls(A, i0, i1, j0, j1),
+                                      oracle.hamming_block(x, i0, i1, j0, j1))
