@@ -225,12 +225,14 @@ def tc_peaks():
     return res
 
 
-def time_whole(tch, A, tau, device, out, ldo, stream, reps=3):
-    """(median device ms, tau used) of one whole-triangle solve of a fresh solver."""
+def time_whole(tch, A, tau, device, out, ldo, stream, reps=3, sched=(0, 0)):
+    """(median device ms, tau used) of one whole-triangle solve of a fresh
+    solver at this tau and schedule (sub-stripe rows, raster group)."""
     import torch
 
     n = A.shape[0]
     with tch.Solver.from_calls(A, tau=tau, device=device) as s:
+        s.set_schedule(*sched)
         used = s.info()["tau"]
         s.stripe(0, n, out.data_ptr(), ldo, stream.cuda_stream)
         ms = []
@@ -397,15 +399,23 @@ def batch_bench(tch, args, device):
             "encode_s": build_s, "tune_s": tune_s}
 
 
+DEFAULT_GROUP = 8  # the library's raster group of the tile pass when none is set
+
+
 def picks(tch, A, device):
-    """The analytic and the learned model's tau for a profile set, from the
-    library's candidate rows; None without a shipped model."""
+    """The analytic model's pick (its tau, the default schedule) and the
+    learned model's pick (tau, sub-stripe rows, raster group) of a profile
+    set, from the library's candidate rows; None without a shipped model."""
     if not os.path.exists(tch.TAU_MLP_PATH):
         return None
     w = tch.load_tau_mlp()
-    taus, feats, est = tch.tau_features(A, device)
-    return {"analytic": int(taus[int(np.argmin(est))]),
-            "learned": int(taus[int(np.argmin(tch.mlp_predict(w, feats, device)))])}
+    c = tch.tau_features(A, device)
+    pred = tch.mlp_predict(w, c["feats"], device)
+    il = int(np.argmin(pred))
+    dflt = (c["subs"] == 0) & (c["groups"] == DEFAULT_GROUP)
+    ia = int(np.argmin(np.where(dflt, c["est"], np.inf)))
+    return {"analytic": (int(c["taus"][ia]), 0, 0),
+            "learned": (int(c["taus"][il]), int(c["subs"][il]), int(c["groups"][il]))}
 
 
 def big_config_bench(tch, synth, args, device):
@@ -441,7 +451,7 @@ def big_config_bench(tch, synth, args, device):
         stripes = [(r0, min(S, n - r0)) for r0 in range(0, n, S)]
         pk = picks(tch, A, device) or {}
         variants = [("learned", 0)] if pk else []
-        variants.append(("analytic", pk.get("analytic", 0)))
+        variants.append(("analytic", pk["analytic"][0] if pk else 0))
         leg = {"shape": f"{n} x {L}", "pairs": pairs, "stripe_rows": S, "stripes": len(stripes),
                "chunk_limit_bytes": chunk, "generate_s": gen_s, "picks": pk}
         for vname, vtau in variants:
@@ -477,7 +487,8 @@ def big_config_bench(tch, synth, args, device):
                 s.check()
                 ms = e0.elapsed_time(e1) / reps
                 k_alg = L + int(info["d_onehot"])
-                v = {"tau": info["tau"], "ms": ms, "pairs_per_s": pairs / (ms / 1e3),
+                v = {"tau": info["tau"], "sub_rows": info["sub_rows"], "tile_group": info["tile_group"],
+                     "ms": ms, "pairs_per_s": pairs / (ms / 1e3),
                      "onehot_columns": int(info["d_onehot"]), "k_chunks": int(info["k_chunks"]),
                      "device_gb": info["device_bytes"] / 1e9, "rare_pairs": int(info["n_rare"]),
                      "ops_per_step": 2.0 * pairs * k_alg,
@@ -668,11 +679,8 @@ def main():
     # tau: the learned model shipped with the package picks it (the analytic
     # model's pick is timed beside it below)
     tau_pick = {}
-    if not args.tau and os.path.exists(tch.TAU_MLP_PATH) and not args.analytic_tau:
-        w_mlp = tch.load_tau_mlp()
-        taus_c, feats_c, est_c = tch.tau_features(A, device)
-        tau_pick = {"analytic": int(taus_c[int(np.argmin(est_c))]),
-                    "learned": int(taus_c[int(np.argmin(tch.mlp_predict(w_mlp, feats_c, device)))])}
+    if not args.tau and not args.analytic_tau:
+        tau_pick = picks(tch, A, device) or {}
     t0 = time.perf_counter()
     solver = tch.Solver.from_calls(A, tau=args.tau, kernel=args.kernel, device=device)  # device encoder
     info = solver.info()
@@ -848,17 +856,21 @@ def main():
     # a sweep of taus around them (fresh solvers)
     tau_cmp = None
     if not args.no_tau_sweep:
-        swept = {int(tau): ms_per_step}
-        cands = {512, 1024, 2048, 4096, 8192} | set(tau_pick.values())
-        for t in sorted(cands):
-            if t not in swept:
-                ms_t, used = time_whole(tch, A, t, device, out, ldo, stream)
-                swept[int(used)] = ms_t
+        used = (int(tau), int(info.get("sub_rows", 0)), int(info.get("tile_group", 0)))
+        swept = {used: ms_per_step}
+        cands = {(t, 0, 0) for t in (512, 1024, 2048, 4096, 8192)} | set(tau_pick.values())
+        for c in sorted(cands):
+            if c not in swept:
+                ms_t, _ = time_whole(tch, A, c[0], device, out, ldo, stream, sched=c[1:])
+                swept[c] = ms_t
         best = min(swept, key=swept.get)
-        tau_cmp = {"used": int(tau), "swept_ms": {str(k): v for k, v in sorted(swept.items())},
-                   "best_swept": {"tau": best, "ms": swept[best]}}
+        key = lambda c: f"tau={c[0]} sub_rows={c[1]} group={c[2] or DEFAULT_GROUP}"  # noqa: E731
+        tau_cmp = {"used": key(used), "swept_ms": {key(k): v for k, v in sorted(swept.items())},
+                   "best_swept": {"candidate": key(best), "ms": swept[best]},
+                   "note": "analytic: its tau with the default schedule; learned: the model's tau and schedule "
+                           "(sub-stripe rows, raster group); whole-triangle device ms of fresh solvers"}
         for k, v in tau_pick.items():
-            tau_cmp[k] = {"tau": v, "ms": swept.get(v)}
+            tau_cmp[k] = {"candidate": key(v), "ms": swept.get(v)}
         log("tau comparison:", tau_cmp)
 
     # the reference's TSV writer (main.rs:224-265) on the GPU: the full matrix

@@ -46,7 +46,7 @@ class Info(ctypes.Structure):
                 ("n_pad", ctypes.c_size_t), ("k_presence", ctypes.c_size_t), ("k_onehot", ctypes.c_size_t),
                 ("d_onehot", ctypes.c_size_t), ("n_rare", ctypes.c_size_t), ("rare_sorted", ctypes.c_int),
                 ("device_bytes", ctypes.c_size_t), ("k_chunks", ctypes.c_int),
-                ("rare_dense", ctypes.c_int)]
+                ("rare_dense", ctypes.c_int), ("sub_rows", ctypes.c_int), ("tile_group", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -94,6 +94,7 @@ def lib():
                                            c_size, c_int, P(c_void), c_char_p, c_int]
         L.tch_solver_from_bits.restype = c_int
         L.tch_solver_info.argtypes, L.tch_solver_info.restype = [c_void, P(Info)], c_int
+        L.tch_solver_set_schedule.argtypes, L.tch_solver_set_schedule.restype = [c_void, c_int, c_int], c_int
         L.tch_solver_stripe.argtypes = [c_void, c_int, c_int, c_void, c_size, c_void, c_char_p, c_int]
         L.tch_solver_stripe.restype = c_int
         L.tch_solver_check.argtypes, L.tch_solver_check.restype = [c_void, c_char_p, c_int], c_int
@@ -122,7 +123,8 @@ def lib():
         L.tch_set_max_chunk_bytes.argtypes, L.tch_set_max_chunk_bytes.restype = [c_size], c_int
         L.tch_set_dense_rare_rate.argtypes, L.tch_set_dense_rare_rate.restype = [c_double], c_int
         L.tch_set_rare_term.argtypes, L.tch_set_rare_term.restype = [c_int], c_int
-        L.tch_tau_features.argtypes = [c_int, c_int, c_int, c_void, c_int, c_void, c_void, c_void, P(c_int),
+        L.tch_tau_features.argtypes = [c_int, c_int, c_int, c_void, c_int, c_void, c_void, c_void, c_void, c_void,
+                                       P(c_int),
                                        c_char_p, c_int]
         L.tch_tau_features.restype = c_int
         L.tch_mlp_init.argtypes, L.tch_mlp_init.restype = [c_void, ctypes.c_uint64], c_int
@@ -338,26 +340,32 @@ def set_tau_model(gemm_rate: float, rare_rate: float, dense_rare_rate: float | N
 # learned tau (no reference counterpart)
 # ---------------------------------------------------------------------------------------
 
-TAU_FEATURES = 12
+TAU_FEATURES = 14
 MLP_HIDDEN = 32
 MLP_PARAMS = TAU_FEATURES * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN + 1
 TAU_MLP_PATH = os.path.join(HERE, "tau_mlp_gb300.f32")
 
 
+MAX_CANDIDATES = 512
+
+
 def tau_features(calls: np.ndarray, device: int = 0):
-    """(taus, features [rows x TAU_FEATURES] f32, analytic estimates in s) of
-    the candidate taus whose encoding fits on the device."""
+    """Candidates (tau x schedule) whose encoding fits on the device:
+    dict(taus, subs, groups, feats [rows x TAU_FEATURES] f32, est: the
+    analytic estimate of the candidate's tau in s)."""
     calls = np.ascontiguousarray(calls, dtype=np.uint64)
     n, L = calls.shape
-    taus = np.zeros(32, np.int32)
-    feats = np.zeros((32, TAU_FEATURES), np.float32)
-    est = np.zeros(32, np.float64)
+    M = MAX_CANDIDATES
+    taus, subs, groups = np.zeros(M, np.int32), np.zeros(M, np.int32), np.zeros(M, np.int32)
+    feats = np.zeros((M, TAU_FEATURES), np.float32)
+    est = np.zeros(M, np.float64)
     rows = ctypes.c_int(0)
     err = _errbuf()
-    _check(lib().tch_tau_features(device, n, L, _ptr(calls), 32, _ptr(taus), _ptr(feats), _ptr(est),
-                                  ctypes.byref(rows), err, len(err)), err)
+    _check(lib().tch_tau_features(device, n, L, _ptr(calls), M, _ptr(taus), _ptr(subs), _ptr(groups), _ptr(feats),
+                                  _ptr(est), ctypes.byref(rows), err, len(err)), err)
     r = rows.value
-    return taus[:r].copy(), feats[:r].copy(), est[:r].copy()
+    return dict(taus=taus[:r].copy(), subs=subs[:r].copy(), groups=groups[:r].copy(), feats=feats[:r].copy(),
+                est=est[:r].copy())
 
 
 def mlp_init(seed: int) -> np.ndarray:
@@ -466,6 +474,13 @@ class Solver:
         i = Info()
         lib().tch_solver_info(self._h, ctypes.byref(i))
         return i.as_dict()
+
+    def set_schedule(self, sub_rows: int = 0, tile_group: int = 0):
+        """Rows per rare-count + tile-pass pair inside a stripe (0 = the whole
+        stripe) and 128-row blocks per raster group of the tile pass (0 = the
+        library default)."""
+        if lib().tch_solver_set_schedule(self._h, sub_rows, tile_group):
+            raise TchError("invalid schedule")
 
     def stripe(self, r0: int, rows: int, d_out: int, ldo: int, stream: int = 0):
         """One stripe into device memory at address d_out (row stride ldo u16)."""

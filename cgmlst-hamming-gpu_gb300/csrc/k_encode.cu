@@ -428,19 +428,30 @@ void tau_features(const std::vector<TauRow>& rows, const std::vector<uint32_t>& 
     const float base[6] = {(float)log((double)std::max(n, 1)), (float)log((double)std::max(L, 1)), (float)quant(0.25),
                            (float)quant(0.5), (float)quant(0.9), (float)(1.0 - present / nl)};
     t->taus.clear();
+    t->subs.clear();
+    t->groups.clear();
     t->feats.clear();
     t->est_s.clear();
     for (const TauRow& w : rows) {
         if (!w.fits) continue;
-        t->taus.push_back(w.tau);
-        t->est_s.push_back(w.t);
-        for (float b : base) t->feats.push_back(b);
-        t->feats.push_back((float)log((double)w.tau));
-        t->feats.push_back((float)log1p((double)w.d));
-        t->feats.push_back((float)log1p(w.r));
-        t->feats.push_back((float)log1p(w.cells));
-        t->feats.push_back((float)log(pairs * w.kb));
-        t->feats.push_back((float)log(std::max(w.t, 1e-9)));
+        for (int sub : kSchedSubs) {
+            if (sub && sub >= n) continue;  // the same as the whole stripe
+            for (int grp : kSchedGroups) {
+                t->taus.push_back(w.tau);
+                t->subs.push_back(sub);
+                t->groups.push_back(grp);
+                t->est_s.push_back(w.t);
+                for (float b : base) t->feats.push_back(b);
+                t->feats.push_back((float)log((double)w.tau));
+                t->feats.push_back((float)log1p((double)w.d));
+                t->feats.push_back((float)log1p(w.r));
+                t->feats.push_back((float)log1p(w.cells));
+                t->feats.push_back((float)log(pairs * w.kb));
+                t->feats.push_back((float)log(std::max(w.t, 1e-9)));
+                t->feats.push_back((float)(sub ? log((double)sub / std::max(n, 1)) : 0.0));
+                t->feats.push_back((float)log((double)grp));
+            }
+        }
     }
 }
 
@@ -464,12 +475,14 @@ int choose_tau_query(const std::vector<TauRow>& rows, int n, const TauModel& m, 
     return best;
 }
 
-// tau <= 0: the learned model's pick when one is set, else the analytic one.
+// tau <= 0: the learned model's pick (tau and schedule) when one is set, else
+// the analytic tau with the default schedule.  *sub / *group receive the
+// schedule (0 = defaults).
 int choose_tau_gb300(int device, const std::vector<uint32_t>& cnt_flat, const std::vector<uint64_t>& off, int n,
-                     int L, size_t free_bytes, const TauModel& m, bool dense, bool verbose) {
+                     int L, size_t free_bytes, const TauModel& m, bool dense, bool verbose, int* sub, int* group) {
     const std::vector<TauRow> rows = tau_rows(cnt_flat, off, n, L, free_bytes, m, dense);
     const int analytic = choose_tau_analytic(rows);
-    int learned = 0;
+    int learned = 0, lsub = 0, lgroup = 0;
     std::vector<float> pred;
     TauTable t;
     float w[kMlpParams];
@@ -481,32 +494,20 @@ int choose_tau_gb300(int device, const std::vector<uint32_t>& cnt_flat, const st
                                         nullptr, quiet)) {
             float best = INFINITY;
             for (size_t q = 0; q < t.taus.size(); q++)
-                if (pred[q] < best) best = pred[q], learned = t.taus[q];
+                if (pred[q] < best) best = pred[q], learned = t.taus[q], lsub = t.subs[q], lgroup = t.groups[q];
         }
     }
     if (verbose) {
-        size_t c = 0;
-        for (const TauRow& r : rows) {
-            fprintf(stderr, "  tau=%5d  one-hot=%8zu  rare=%14.0f  est %.4fs  vram %.2f GB%s", r.tau, r.d, r.r, r.t,
+        for (const TauRow& r : rows)
+            fprintf(stderr, "  tau=%5d  one-hot=%8zu  rare=%14.0f  est %.4fs  vram %.2f GB%s\n", r.tau, r.d, r.r, r.t,
                     r.mem / 1e9, r.fits ? "" : "  (does not fit)");
-            if (r.fits && c < pred.size() && t.taus[c] == r.tau) fprintf(stderr, "  learned %.2f ms", exp(pred[c++]));
-            fprintf(stderr, "\n");
-        }
-        fprintf(stderr, "  tau: analytic %d, learned %d\n", analytic, learned);
+        fprintf(stderr, "  tau: analytic %d, learned %d (sub-stripes %d rows, raster group %d)\n", analytic, learned,
+                lsub, lgroup);
     }
-    // the analytic model is the fallback: a learned pick it rates more than 1.5x
-    // slower than its own is outside what the network was trained on
-    if (learned && analytic) {
-        double t_l = 0, t_a = 0;
-        for (const TauRow& r : rows) {
-            if (r.tau == learned) t_l = r.t;
-            if (r.tau == analytic) t_a = r.t;
-        }
-        if (t_l > 1.5 * t_a) {
-            if (verbose) fprintf(stderr, "  learned pick %d rated %.1fx the analytic one: analytic\n", learned, t_l / t_a);
-            learned = 0;
-        }
-    }
+    // the learned pick is taken as it is: the held-out evaluation of the model
+    // (tau_learn.py) measures it against the analytic pick on real timings
+    *sub = learned ? lsub : 0;
+    *group = learned ? lgroup : 0;
     return learned ? learned : analytic;
 }
 
@@ -632,7 +633,8 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
         }
         if (tau <= 0) {
             tau = query_maps ? choose_tau_query(tau_rows(cnt_h, off_h, n, L, freeb, model, true), n, model, verbose)
-                             : choose_tau_gb300(device, cnt_h, off_h, n, L, freeb, model, dense_rare, verbose);
+                             : choose_tau_gb300(device, cnt_h, off_h, n, L, freeb, model, dense_rare, verbose,
+                                                &out->sub_rows, &out->tile_group);
             if (!tau) { e.set("no tau fits in %.2f GB of free device memory", freeb / 1e9); goto fail; }
         }
         out->tau = tau;

@@ -443,7 +443,7 @@ cudaError_t launch_one(const Fp4Operands& A, const Fp4Operands& B, const uint16_
     p.c0 = a.rect ? 0 : a.r0;
     p.rows = a.rows;
     p.kblocks = A.kb / BK;
-    p.ts.gs = group_row_blocks();
+    p.ts.gs = a.group > 0 ? std::min(a.group, 256) : group_row_blocks();
     p.ts.nbi = (a.rows + BM - 1) / BM;
     p.ts.rect = a.rect ? 1 : 0;
     p.ts.nbj = (a.n - p.c0 + BN - 1) / BN;
@@ -482,7 +482,8 @@ cudaError_t launch_tc_stripe(const Fp4Operands& ops, const Fp4Operands* bops, co
     const Fp4Operands& b = bops ? *bops : ops;
     // one launch covers at most MAX_GROUPS raster groups of rows; a taller
     // stripe runs as consecutive sub-stripes writing into the same output
-    const int max_rows = MAX_GROUPS * group_row_blocks() * BM;
+    const int group = a.group > 0 ? std::min(a.group, 256) : group_row_blocks();
+    const int max_rows = MAX_GROUPS * group * BM;
     for (int done = 0; done < a.rows; done += max_rows) {
         StripeArgs s = a;
         s.r0 = a.r0 + done;

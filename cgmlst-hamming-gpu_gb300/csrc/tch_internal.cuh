@@ -139,6 +139,7 @@ struct StripeArgs {
     size_t ldo = 0;
     int* err = nullptr;
     bool rect = false;
+    int group = 0;  // row blocks per raster group of the tile pass (0 = the library default)
 };
 
 // ---- k_popc.cu --------------------------------------------------------------------
@@ -229,6 +230,7 @@ struct DeviceEncoding {
     Fp4Operands X;            // x_rows packed e2m1 rows [presence (L) | one-hot (D)], split along K
     size_t x_rows = 0;
     int kb = 0;               // bytes per row
+    int sub_rows = 0, tile_group = 0;  // schedule of the learned model's pick (0 = defaults)
     uint32_t* start = nullptr;  // n + 1 (CSR mode)
     uint32_t* js = nullptr;     // n_rare, ascending per row (CSR mode)
     size_t n_rare = 0;
@@ -251,12 +253,17 @@ struct DeviceEncoding {
 // single-row groups and the maps that encode new profiles like these.
 enum EncodeFlags : int { ENC_DENSE = 1, ENC_QUERY = 2 };
 
-// Candidate taus of an encoding and their learned-model feature rows.
+// Candidates (tau x schedule) of an encoding and their learned-model feature rows.
 struct TauTable {
     std::vector<int> taus;
+    std::vector<int> subs;      // sub-stripe rows (0 = the whole stripe)
+    std::vector<int> groups;    // raster group (row blocks)
     std::vector<float> feats;   // taus.size() x TCH_TAU_FEATURES
     std::vector<double> est_s;  // analytic estimate per candidate
 };
+// Schedule values the candidates take.
+constexpr int kSchedSubs[3] = {0, 8192, 2048};
+constexpr int kSchedGroups[3] = {4, 8, 16};
 
 // With table != nullptr the encoder stops after the counts and fills it.
 int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_req, const TauModel& model,

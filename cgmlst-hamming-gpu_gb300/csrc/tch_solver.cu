@@ -151,6 +151,8 @@ struct tch_solver {
     uint32_t* gmembers = nullptr;
     uint32_t* gmpos = nullptr;
     int gL = 0;                      // loci of the rank rows (>= 1)
+    int sub_rows = 0;                // rows per rare-count + tile-pass pair inside a stripe (0 = whole)
+    int tile_group = 0;              // row blocks per raster group of the tile pass (0 = default)
     int* dErr = nullptr;
     int num_sms = 0;
     size_t bytes = 0;
@@ -392,6 +394,8 @@ static int solver_from_input(int device, int n, int L, const uint64_t* calls, co
     s->K1 = (size_t)enc.kb * 2 - (size_t)Le;
     s->D = enc.D;
     s->tau = enc.tau;
+    s->sub_rows = enc.sub_rows;
+    s->tile_group = enc.tile_group;
     s->dStart = enc.start;
     s->dJs = enc.js;
     s->n_rare = enc.n_rare;
@@ -445,6 +449,7 @@ int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, 
     a.out = d_out;
     a.ldo = ldo;
     a.err = s->dErr;
+    a.group = s->tile_group;
     cudaError_t ce;
     const bool lists = !s->dense && !s->rare_on_host && s->n_rare > 0;
     if (s->kernel == TCH_KERNEL_POPC) {
@@ -469,21 +474,32 @@ int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, 
         if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
         return 0;
     }
-    // the stripe's rare counts (from the rare groups or the pair lists) into a
-    // block of the pool, then the tile pass that subtracts them
-    const size_t ldr = up((size_t)(s->n - r0), kRareDenseAlign);
-    const size_t rbytes = (size_t)rows * ldr * 2;
+    // in sub-stripes of sub_rows rows (the solver's schedule): each one's rare
+    // counts (from the rare groups or the pair lists) into a block of the pool,
+    // then the tile pass that subtracts them
+    const int sub = (s->sub_rows > 0 && rows > s->sub_rows) ? s->sub_rows : rows;
     cudaMemPool_t pool;
-    uint16_t* R = nullptr;
     ce = stripe_pool(s->device, &pool);
-    if (ce == cudaSuccess) ce = cudaMallocFromPoolAsync((void**)&R, rbytes, pool, st);
-    if (ce != cudaSuccess) return e.set("rare counts of the stripe (%zu bytes): %s", rbytes, cudaGetErrorString(ce));
-    ce = s->dense ? launch_rare_dense(rare_groups(s), r0, rows, R, ldr, s->num_sms, st)
-                  : launch_rare_from_lists(s->dStart, s->dJs, s->n, r0, rows, R, ldr, s->dErr, s->num_sms, st);
-    if (ce == cudaSuccess) ce = launch_dense_stripe(s, a, R, ldr, st);
-    const cudaError_t fe = cudaFreeAsync(R, st);
-    if (ce == cudaSuccess) ce = fe;
-    if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
+    if (ce != cudaSuccess) return e.set("stripe pool: %s", cudaGetErrorString(ce));
+    for (int q0 = r0; q0 < r0 + rows; q0 += sub) {
+        const int qrows = std::min(sub, r0 + rows - q0);
+        const size_t ldr = up((size_t)(s->n - q0), kRareDenseAlign);
+        const size_t rbytes = (size_t)qrows * ldr * 2;
+        uint16_t* R = nullptr;
+        ce = cudaMallocFromPoolAsync((void**)&R, rbytes, pool, st);
+        if (ce != cudaSuccess)
+            return e.set("rare counts of the stripe (%zu bytes): %s", rbytes, cudaGetErrorString(ce));
+        StripeArgs qa = a;
+        qa.r0 = q0;
+        qa.rows = qrows;
+        qa.out = d_out + (size_t)(q0 - r0) * ldo + (size_t)(q0 - r0);  // a triangle's columns start at its first row
+        ce = s->dense ? launch_rare_dense(rare_groups(s), q0, qrows, R, ldr, s->num_sms, st)
+                      : launch_rare_from_lists(s->dStart, s->dJs, s->n, q0, qrows, R, ldr, s->dErr, s->num_sms, st);
+        if (ce == cudaSuccess) ce = launch_dense_stripe(s, qa, R, ldr, st);
+        const cudaError_t fe = cudaFreeAsync(R, st);
+        if (ce == cudaSuccess) ce = fe;
+        if (ce != cudaSuccess) return e.set("stripe kernel: %s", cudaGetErrorString(ce));
+    }
     return 0;
 }
 
@@ -923,8 +939,8 @@ int tch_run_calls(int device, int n, int L, const uint64_t* calls, int tau, int 
     return rc;
 }
 
-int tch_tau_features(int device, int n, int L, const uint64_t* calls, int max_rows, int* taus, float* feats,
-                     double* est_s, int* rows, char* err, int errlen) {
+int tch_tau_features(int device, int n, int L, const uint64_t* calls, int max_rows, int* taus, int* sub_rows,
+                     int* groups, float* feats, double* est_s, int* rows, char* err, int errlen) {
     Err e{err, errlen};
     uint64_t* d_calls = nullptr;
     DeviceEncoding enc;
@@ -942,6 +958,8 @@ int tch_tau_features(int device, int n, int L, const uint64_t* calls, int max_ro
     *rows = (int)std::min<size_t>(table.taus.size(), (size_t)max_rows);
     for (int r = 0; r < *rows; r++) {
         taus[r] = table.taus[r];
+        if (sub_rows) sub_rows[r] = table.subs[r];
+        if (groups) groups[r] = table.groups[r];
         if (est_s) est_s[r] = table.est_s[r];
         for (int f = 0; f < TCH_TAU_FEATURES; f++) feats[(size_t)r * TCH_TAU_FEATURES + f] =
             table.feats[(size_t)r * TCH_TAU_FEATURES + f];
@@ -991,6 +1009,15 @@ int tch_solver_info(const tch_solver* s, tch_info* info) {
     info->device_bytes = s->bytes;
     info->k_chunks = is_tc(s->kernel) ? s->X.pos.n : 0;
     info->rare_dense = s->dense ? 1 : 0;
+    info->sub_rows = s->sub_rows;
+    info->tile_group = s->tile_group;
+    return 0;
+}
+
+int tch_solver_set_schedule(tch_solver* s, int sub_rows, int tile_group) {
+    if (!s || sub_rows < 0 || tile_group < 0 || tile_group > 256) return 1;
+    s->sub_rows = sub_rows ? (int)up((size_t)sub_rows, 128) : 0;  // sub-stripe outputs stay 16-byte aligned
+    s->tile_group = tile_group;
     return 0;
 }
 

@@ -1,4 +1,4 @@
-"""Training data and training of the learned tau model.
+"""Training data and training of the learned tau and schedule model.
 
     python -m tau_learn sweep  [--datasets 200] [--out tau_sweep_gb300.npz]
     python -m tau_learn train  [--sweep tau_sweep_gb300.npz] [--out tau_mlp_gb300.f32]
@@ -10,15 +10,17 @@ sweep: seeded synthetic profile sets of varied shape (n log-uniform in
 (s in [1.0, 1.4], lognormal distinct-allele counts, 5 % 64-bit ids), 20 %
 founder models (3-60 alleles per locus, 0.2-5 % mutations to new ids), 20 % the
 batched config's law (n <= 5 000); 0-8 % missing.  For each set
-the library's own feature rows (tch_tau_features) and, for each candidate tau
-near the analytic pick, the measured device time of one whole-triangle solve
-(rare counts + tile pass, CUDA events, median of 3).
+the library's own candidate rows (tch_tau_features: tau x sub-stripe rows x
+raster group) and, for each candidate whose tau is near the analytic pick, the
+measured device time of one whole-triangle solve under that schedule (rare
+counts + tile pass, CUDA events, median of 3).
 
 train: the MLP of csrc/k_mlp.cu on ln(ms), trained on the GPU by the library's
 kernels (tch_mlp_train), every fifth profile set held out.  Feature
 standardisation is folded into the first layer, so the saved model takes the
 raw feature rows.  The report compares, on the held-out sets, the measured time
-at the learned pick, at the analytic pick and at the best swept tau.
+at the learned pick (tau and schedule), at the analytic pick (its tau, the
+default schedule) and at the best swept candidate.
 """
 from __future__ import annotations
 
@@ -94,52 +96,66 @@ def make_dataset(p: dict) -> np.ndarray:
     return synth.zipf_profiles(p["n"], p["L"], p["seed"], p["s"], distinct, miss, hashed_frac=0.05)
 
 
-def time_solve(A: np.ndarray, tau: int, reps: int = 3, device: int = 0) -> float:
-    """Median device ms of one whole-triangle stripe (rare counts + tile pass)."""
+DEFAULT_GROUP = 8  # the library's raster group when none is set
+
+
+def time_solve(A: np.ndarray, tau: int, scheds, reps: int = 3, device: int = 0) -> list:
+    """Median device ms of one whole-triangle stripe (rare counts + tile
+    pass) for each schedule (sub-stripe rows, raster group) in scheds, one
+    solver (one encoding) at this tau."""
     import torch
 
     n = A.shape[0]
     ldo = (n + 7) // 8 * 8
     out = torch.empty((n, ldo), dtype=torch.int16, device=f"cuda:{device}")
     stream = torch.cuda.current_stream(device).cuda_stream
+    res = []
     with tch.Solver.from_calls(A, tau=tau, device=device) as s:
-        s.stripe(0, n, out.data_ptr(), ldo, stream)  # warm-up
-        times = []
-        for _ in range(reps):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            s.stripe(0, n, out.data_ptr(), ldo, stream)
-            e1.record()
-            torch.cuda.synchronize()
-            times.append(e0.elapsed_time(e1))
+        for sub, grp in scheds:
+            s.set_schedule(int(sub), int(grp))
+            s.stripe(0, n, out.data_ptr(), ldo, stream)  # warm-up
+            times = []
+            for _ in range(reps):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                s.stripe(0, n, out.data_ptr(), ldo, stream)
+                e1.record()
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1))
+            res.append(float(np.median(times)))
         s.check()
     del out
-    return float(np.median(times))
+    return res
 
 
-def sweep(n_datasets: int, out: str, span: int = 32, device: int = 0) -> None:
-    rows = dict(ds=[], tau=[], feats=[], est=[], ms=[])
+def sweep(n_datasets: int, out: str, span: int = 4, device: int = 0, first: int = 0) -> None:
+    rows = dict(ds=[], tau=[], sub=[], group=[], feats=[], est=[], ms=[])
     params = []
     t0 = time.time()
-    for d in range(n_datasets):
+    for d in range(first, first + n_datasets):
         p = dataset_params(d)
         A = make_dataset(p)
-        taus, feats, est = tch.tau_features(A, device)
-        analytic = int(taus[np.argmin(est)])
-        for t, f, e in zip(taus, feats, est):
+        c = tch.tau_features(A, device)
+        analytic = int(c["taus"][np.argmin(c["est"])])
+        for t in sorted(set(int(x) for x in c["taus"])):
             if t < max(4, analytic // span) or t > analytic * span:
                 continue
-            ms = time_solve(A, int(t), device=device)
-            rows["ds"].append(d)
-            rows["tau"].append(int(t))
-            rows["feats"].append(f)
-            rows["est"].append(float(e))
-            rows["ms"].append(ms)
+            idx = np.nonzero(c["taus"] == t)[0]
+            ms = time_solve(A, t, [(c["subs"][i], c["groups"][i]) for i in idx], device=device)
+            for i, m in zip(idx, ms):
+                rows["ds"].append(d)
+                rows["tau"].append(t)
+                rows["sub"].append(int(c["subs"][i]))
+                rows["group"].append(int(c["groups"][i]))
+                rows["feats"].append(c["feats"][i])
+                rows["est"].append(float(c["est"][i]))
+                rows["ms"].append(m)
         params.append(p)
         print(f"[{time.time() - t0:6.1f}s] set {d}: {p['kind']} n={p['n']} L={p['L']} analytic tau={analytic}",
               flush=True)
     np.savez(out, ds=np.array(rows["ds"], np.int32), tau=np.array(rows["tau"], np.int32),
+             sub=np.array(rows["sub"], np.int32), group=np.array(rows["group"], np.int32),
              feats=np.array(rows["feats"], np.float32), est=np.array(rows["est"]), ms=np.array(rows["ms"]),
              params=json.dumps(params))
 
@@ -161,26 +177,24 @@ def fold_standardisation(w: np.ndarray, mu: np.ndarray, sd: np.ndarray) -> np.nd
     return w.astype(np.float32)
 
 
-GUARD = 1.5  # the solver keeps a learned pick only within 1.5x of the analytic pick's estimate
-
-
 def evaluate(w: np.ndarray, data, device: int = 0) -> dict:
     """Per held-out set: measured ms at the solver's pick with the model set
-    (the learned pick, or the analytic one when the analytic model rates the
-    learned one more than GUARD times slower), at the analytic pick and at the
-    best swept tau."""
+    (the learned candidate: tau and schedule), at the analytic pick (its tau
+    with the default schedule) and at the best swept candidate."""
     ds, tau, X, est, ms = data["ds"], data["tau"], data["feats"], data["est"], data["ms"]
+    sub, grp = data["sub"], data["group"]
     pred = tch.mlp_predict(w, X, device)
+    default = (sub == 0) & (grp == DEFAULT_GROUP)
     out = []
     for d in np.unique(ds[holdout_mask(ds)]):
         m = ds == d
         i_l = np.argmin(np.where(m, pred, np.inf))
-        i_a = np.argmin(np.where(m, est, np.inf))
+        i_a = np.argmin(np.where(m & default, est, np.inf))
         i_b = np.argmin(np.where(m, ms, np.inf))
-        if est[i_l] > GUARD * est[i_a]:
-            i_l = i_a
-        out.append(dict(set=int(d), tau_learned=int(tau[i_l]), tau_analytic=int(tau[i_a]), tau_best=int(tau[i_b]),
-                        ms_learned=float(ms[i_l]), ms_analytic=float(ms[i_a]), ms_best=float(ms[i_b])))
+        out.append(dict(set=int(d), tau_learned=int(tau[i_l]), sub_learned=int(sub[i_l]), group_learned=int(grp[i_l]),
+                        tau_analytic=int(tau[i_a]), tau_best=int(tau[i_b]), sub_best=int(sub[i_b]),
+                        group_best=int(grp[i_b]), ms_learned=float(ms[i_l]), ms_analytic=float(ms[i_a]),
+                        ms_best=float(ms[i_b])))
     tl = sum(r["ms_learned"] for r in out)
     ta = sum(r["ms_analytic"] for r in out)
     tb = sum(r["ms_best"] for r in out)
@@ -217,13 +231,14 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("cmd", choices=["sweep", "train", "report"])
     ap.add_argument("--datasets", type=int, default=200)
+    ap.add_argument("--first", type=int, default=0, help="sweep: first profile set (seed)")
     ap.add_argument("--sweep", default=SWEEP_PATH)
     ap.add_argument("--out", default=None)
     ap.add_argument("--steps", type=int, default=6000)
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args()
     if a.cmd == "sweep":
-        sweep(a.datasets, a.out or SWEEP_PATH, device=a.device)
+        sweep(a.datasets, a.out or SWEEP_PATH, device=a.device, first=a.first)
     elif a.cmd == "report":  # the shipped model on the shipped sweep
         rep = evaluate(np.fromfile(a.out or tch.TAU_MLP_PATH, dtype="<f4"), dict(np.load(a.sweep)), a.device)
         with open(REPORT_PATH, "w") as f:

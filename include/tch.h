@@ -114,6 +114,8 @@ typedef struct tch_info {
     size_t device_bytes; /* device memory held by the solver */
     int k_chunks;        /* separate allocations the operand rows are split into along K */
     int rare_dense;      /* 1 if the rare term is counted per stripe from rare groups */
+    int sub_rows;        /* rows per rare-count + tile-pass pair inside a stripe (0 = the whole stripe) */
+    int tile_group;      /* row blocks per raster group of the tile pass (0 = the library default) */
 } tch_info;
 
 /* Largest single device allocation of a solver's operand rows, in bytes
@@ -173,28 +175,32 @@ int tch_set_dense_rare_rate(double rate);
  * No reference counterpart (the reference always builds pair lists). */
 int tch_set_rare_term(int dense);
 
-/* ---- learned tau (no reference counterpart) --------------------------------
+/* ---- learned tau and schedule (no reference counterpart) ------------------
  * A small MLP predicts ln(ms) of one whole-triangle solve for each candidate
- * tau from TCH_TAU_FEATURES features; a solver built from calls with tau <= 0
- * takes the candidate with the smallest prediction when a model is set
- * (tch_set_tau_mlp), the analytic model's pick otherwise.  Feature row of a
- * candidate: ln n, ln L, quantiles 0.25 / 0.5 / 0.9 of ln(1 + distinct alleles
- * per locus), missing fraction, ln tau, ln(1 + frequent one-hot columns),
- * ln(1 + rare pairs), ln(1 + rare cells), ln(pairs x operand bytes per row),
- * ln(analytic estimate in seconds).  Network: F -> 32 -> 32 -> 1, ReLU, fp32,
- * parameters W1[F][32] | b1[32] | W2[32][32] | b2[32] | w3[32] | b3. */
-#define TCH_TAU_FEATURES 12
+ * (tau, sub-stripe rows, raster group) from TCH_TAU_FEATURES features; a
+ * solver built from calls with tau <= 0 takes the candidate with the smallest
+ * prediction when a model is set (tch_set_tau_mlp): its tau and its schedule
+ * (tch_solver_set_schedule).  Without a model: the analytic model's tau and
+ * the default schedule.  Feature row of a candidate: ln n, ln L, quantiles
+ * 0.25 / 0.5 / 0.9 of ln(1 + distinct alleles per locus), missing fraction,
+ * ln tau, ln(1 + frequent one-hot columns), ln(1 + rare pairs), ln(1 + rare
+ * cells), ln(pairs x operand columns), ln(analytic estimate in seconds),
+ * ln(sub-stripe rows / n) (0 for the whole stripe), ln(raster group).
+ * Network: F -> 32 -> 32 -> 1, ReLU, fp32, parameters W1[F][32] | b1[32] |
+ * W2[32][32] | b2[32] | w3[32] | b3. */
+#define TCH_TAU_FEATURES 14
 #define TCH_MLP_HIDDEN 32
 #define TCH_MLP_PARAMS                                                                             \
     (TCH_TAU_FEATURES * TCH_MLP_HIDDEN + TCH_MLP_HIDDEN + TCH_MLP_HIDDEN * TCH_MLP_HIDDEN + \
      TCH_MLP_HIDDEN + TCH_MLP_HIDDEN + 1)
 
-/* Candidate taus of a profile set (device encoder's counts; those whose
- * encoding fits in free device memory) and their feature rows:
- * taus[r], feats[r * TCH_TAU_FEATURES + f] for r < *rows <= max_rows.
- * est_s[r] (may be NULL) receives the analytic model's estimate. */
-int tch_tau_features(int device, int n, int L, const uint64_t* calls, int max_rows, int* taus, float* feats,
-                     double* est_s, int* rows, char* err, int errlen);
+/* Candidates of a profile set (device encoder's counts; taus whose encoding
+ * fits in free device memory, each with every schedule) and their feature
+ * rows: taus[r], sub_rows[r], groups[r] (0 = whole stripe),
+ * feats[r * TCH_TAU_FEATURES + f] for r < *rows <= max_rows.  est_s[r] (may be
+ * NULL) receives the analytic model's estimate of the candidate's tau. */
+int tch_tau_features(int device, int n, int L, const uint64_t* calls, int max_rows, int* taus, int* sub_rows,
+                     int* groups, float* feats, double* est_s, int* rows, char* err, int errlen);
 
 /* He-normal initial parameters from a seed (host). */
 int tch_mlp_init(float* w, uint64_t seed);
@@ -276,6 +282,15 @@ void tch_batch_destroy(tch_batch* b);
 
 /* Fill *info. */
 int tch_solver_info(const tch_solver* s, tch_info* info);
+/* Schedule of the solver's stripes: every stripe runs as sub-stripes of
+ * sub_rows rows (0 = the whole stripe at once; rounded up to a multiple of
+ * 128), each its rare counts then its tile pass (a smaller rare-count block,
+ * more launches), and the tile pass visits its tiles in raster groups of
+ * `tile_group` 128-row blocks (0 = the library default).  A solver built by
+ * tch_solver_from_calls / _from_ranks with tau <= 0 and a learned model set
+ * (tch_set_tau_mlp) starts with the model's pick.  Every schedule gives the
+ * same distances. */
+int tch_solver_set_schedule(tch_solver* s, int sub_rows, int tile_group);
 
 /* One stripe into caller-owned DEVICE memory, asynchronously on `stream`
  * (a cudaStream_t, NULL = the legacy default stream):

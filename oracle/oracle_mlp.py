@@ -13,7 +13,7 @@ from __future__ import annotations
 
 import numpy as np
 
-F = 12
+F = 14
 H = 32
 NP = F * H + H + H * H + H + H + 1
 

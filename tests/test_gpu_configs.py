@@ -108,3 +108,16 @@ def test_zipf_big_law_reduced(pkg, synth):
     with pkg.Solver.from_calls(A) as s:
         H, _ = s.run(2048)
     spread_rows_equal(H, x)
+
+
+@pytest.mark.parametrize("sub_rows,group", [(0, 1), (256, 4), (1024, 16), (128, 8)])
+def test_schedules_give_the_same_distances(pkg, small, sub_rows, group):
+    """Sub-stripes of the rare counts and tile pass, and raster groups of the
+    tile pass, change the order of the work, never a distance."""
+    A, x, ref = small
+    with pkg.Solver.from_calls(A, tau=256) as s:
+        s.set_schedule(sub_rows, group)
+        info = s.info()
+        H, _ = s.run(2000)
+    assert info["sub_rows"] == sub_rows and info["tile_group"] == group
+    upper_equal(H, ref)

@@ -88,9 +88,9 @@ def test_gpu_training_follows_oracle_adam(tch):
 @pytest.mark.gpu
 def test_shipped_model_gains_over_analytic_on_heldout(tch):
     """Held-out profile sets of the committed sweep: the measured time at the
-    learned pick is within 5% of the best swept tau overall, no slower than the
-    analytic model's pick in total, and closer to the best per set on average
-    (the model is evaluated by the GPU kernel)."""
+    learned pick (tau and schedule) is within 5% of the best swept candidate
+    overall, no slower than the analytic model's pick in total, and closer to
+    the best per set on average (the model is evaluated by the GPU kernel)."""
     tl = importlib.import_module(PKG + ".tau_learn")
     data = dict(np.load(tl.SWEEP_PATH))
     w = np.fromfile(tch.TAU_MLP_PATH, dtype="<f4")
@@ -103,20 +103,25 @@ def test_shipped_model_gains_over_analytic_on_heldout(tch):
 
 @pytest.mark.gpu
 def test_learned_tau_drives_the_solver_and_stays_exact(tch):
+    """With the model set, a solver built with tau = 0 takes the candidate the
+    model predicts fastest (tau and schedule); the distances stay exact; without
+    the model it takes the analytic tau and the default schedule."""
     synth = importlib.import_module(PKG + ".synth")
     A = synth.longtail(n=1500, L=300, seed=8)
     w = tch.load_tau_mlp()
-    taus, feats, est = tch.tau_features(A)
-    il, ia = int(np.argmin(tch.mlp_predict(w, feats))), int(np.argmin(est))
-    # the learned pick, unless the analytic model rates it 1.5x slower than its own
-    pick = int(taus[il]) if est[il] <= 1.5 * est[ia] else int(taus[ia])
+    c = tch.tau_features(A)
+    il = int(np.argmin(tch.mlp_predict(w, c["feats"])))
     with tch.Solver.from_calls(A, tau=0) as s:
         info = s.info()
         H, _ = s.run(512)
-    assert info["tau"] == pick
+    assert (info["tau"], info["sub_rows"], info["tile_group"]) == (int(c["taus"][il]), int(c["subs"][il]),
+                                                                   int(c["groups"][il]))
     x = oracle.dense_ranks(A)[0]
     iu = np.triu_indices(1500, 1)
     np.testing.assert_array_equal(H[iu], oracle.hamming(x)[iu])
     tch.set_tau_mlp(None)
     with tch.Solver.from_calls(A, tau=0) as s:
-        assert s.info()["tau"] == int(taus[np.argmin(est)])  # analytic model again
+        info = s.info()
+    dflt = (c["subs"] == 0) & (c["groups"] == 8)
+    assert info["tau"] == int(c["taus"][np.argmin(np.where(dflt, c["est"], np.inf))])  # analytic model again
+    assert info["sub_rows"] == 0 and info["tile_group"] == 0
