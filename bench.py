@@ -394,7 +394,8 @@ def batch_bench(tch, args, device):
     taus = b.info()["taus"]
     b.close()
     return {"matrices": args.batch_count, "pairs": pairs, "ms_per_batch": ms, "pairs_per_s": pairs / (ms / 1e3),
-            "schedule": tuned, "graph": "one CUDA graph per replay (fork/join over the tuned branch count)",
+            "schedule": tuned, "graph": ("one CUDA graph per replay: " + ("two persistent launches over every set"
+                                       if tuned["branches"] == 0 else "fork/join over the tuned branch count")),
             "tau_per_matrix": {"min": int(min(taus)), "median": int(np.median(taus)), "max": int(max(taus))},
             "encode_s": build_s, "tune_s": tune_s}
 

@@ -4,16 +4,22 @@
 //
 // Every set is encoded on the device once (tch_solver_from_calls; a tau of 0
 // lets the learned model, when set, or the analytic model pick it per set).
-// A run launches every set's rare counts + tile pass (into one preallocated
-// rare-count block per stream, so nothing is allocated inside the graph).  The
-// launches are spread
-// over `branches` streams forked from the caller's stream (largest sets
-// first, each to the branch with the least work so far), so the small sets'
-// kernels, which fill only a few SMs each, run side by side; the whole fork /
-// join is captured once as a CUDA graph and replayed on every later run.
+// Two schedules, each captured once as a CUDA graph (per output buffer) and
+// replayed on every later run; nothing is allocated inside the graph:
+//
+// * branches >= 1: every set's rare counts + tile pass (into one preallocated
+//   rare-count block per stream) spread over `branches` streams forked from
+//   the caller's stream (largest sets first, each to the branch with the least
+//   work so far), so the small sets' kernels, which fill only a few SMs each,
+//   run side by side;
+// * branches == 0 (persistent): two launches for the whole batch, the rare
+//   counts of every row of every set (one CTA per row, a row -> set table) into
+//   one rare-count buffer, then one tile pass over every set's tiles (one CTA
+//   per SM walking a tile -> set table, each set with its own tensor maps and
+//   output).  Needs dense rare counts and sets of at most 65 536 rows.
 //
 // tch_batch_tune is the autotuner of that schedule: it times the graph for
-// every branch count and keeps the fastest.
+// every schedule and keeps the fastest.
 
 #include <math.h>
 #include <string.h>
@@ -37,6 +43,14 @@ struct tch_batch {
     cudaStream_t origin = nullptr;  // the stream the fork / join is captured on
     std::vector<uint16_t*> rbuf;    // per branch: rare-count block of its largest set
     std::vector<size_t> rbytes;
+    // persistent schedule: every set's rare-count block in one buffer, the
+    // job tables of the two launches, the tile pass's error word
+    uint16_t* pbuf = nullptr;
+    size_t pbytes = 0;
+    RareBatchPlan rplan;
+    TcBatchPlan tplan;
+    int* dErr = nullptr;
+    int num_sms = 0;
     cudaGraphExec_t exec = nullptr;
     uint16_t* exec_out = nullptr;
     bool warmed = false;
@@ -84,6 +98,87 @@ fail:
     return 1;
 }
 
+// Largest rare-count buffer of the persistent schedule.
+constexpr size_t kPersistentRareBytes = size_t(8) << 30;
+
+// Whether the persistent schedule can run this batch (why not in *why).
+bool persistent_ready(const tch_batch* b, const char** why) {
+    size_t bytes = 0;
+    for (tch_solver* sv : b->sets) {
+        const int n = solver_size(sv);
+        if (n < 2) continue;
+        RareGroups g;
+        if (!solver_operands(sv) || !solver_rare_groups(sv, &g)) {
+            *why = "a set holds pair lists, not rare groups";
+            return false;
+        }
+        if (rare_ld(n) > 65536) {
+            *why = "a set has more than 65 536 rows";
+            return false;
+        }
+        bytes += (size_t)n * rare_ld(n) * 2;
+    }
+    if (bytes > kPersistentRareBytes) {
+        *why = "the rare counts of all sets exceed 8 GiB";
+        return false;
+    }
+    return true;
+}
+
+// Job tables of the two persistent launches of the whole batch into d_out
+// (device memory written here, before the capture).
+int prepare_persistent(tch_batch* b, uint16_t* d_out, Err& e) {
+    std::vector<int> order(b->sets.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(),
+              [&](int x, int y) { return solver_work(b->sets[x]) > solver_work(b->sets[y]); });
+    std::vector<size_t> roff(b->sets.size(), 0);
+    size_t total = 0;
+    for (int s : order) {
+        const int n = solver_size(b->sets[s]);
+        if (n < 2) continue;
+        roff[s] = total;
+        total += (size_t)n * rare_ld(n);
+    }
+    if (b->pbytes < total * 2) {
+        cudaFree(b->pbuf);
+        b->pbuf = nullptr;
+        b->pbytes = 0;
+        TCH_CK(e, cudaMalloc(&b->pbuf, total * 2));
+        b->pbytes = total * 2;
+    }
+    if (!b->dErr) {
+        TCH_CK(e, cudaMalloc(&b->dErr, sizeof(int)));
+        TCH_CK(e, cudaMemset(b->dErr, 0, sizeof(int)));
+    }
+    {
+        std::vector<RareBatchItem> ri;
+        std::vector<TcBatchItem> ti;
+        for (int s : order) {
+            const int n = solver_size(b->sets[s]);
+            if (n < 2) continue;
+            RareBatchItem r;
+            solver_rare_groups(b->sets[s], &r.g);
+            r.R = b->pbuf + roff[s];
+            r.ldr = rare_ld(n);
+            ri.push_back(r);
+            TcBatchItem t;
+            t.ops = solver_operands(b->sets[s]);
+            t.n = n;
+            t.R = r.R;
+            t.ldr = r.ldr;
+            t.out = d_out + b->off[s];
+            t.ldo = b->ld[s];
+            ti.push_back(t);
+        }
+        TCH_CK(e, rare_batch_prepare(ri, &b->rplan));
+        TCH_CK(e, tc_batch_prepare(ti, &b->tplan, b->dErr));
+    }
+    return 0;
+fail:
+    return 1;
+}
+
 // One eager solve before the first capture, so one-time set-up (kernel
 // attributes) never runs inside it.
 int warm_up(tch_batch* b, uint16_t* d_out, Err& e) {
@@ -118,9 +213,23 @@ int build_graph(tch_batch* b, uint16_t* d_out, Err& e) {
     std::vector<int> branch(b->sets.size());
     std::vector<size_t> need(nb, 0);
     drop_graph(b);
-    if (ensure_streams(b, nb, e)) return 1;
+    if (ensure_streams(b, std::max(nb, 1), e)) return 1;
     if (!b->warmed && warm_up(b, d_out, e)) return 1;
     st = b->origin;
+    if (nb == 0) {
+        const char* why = "";
+        if (!persistent_ready(b, &why)) return e.set("persistent schedule unavailable: %s", why);
+        if (!b->num_sms) TCH_CK(e, cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device));
+        if (prepare_persistent(b, d_out, e)) return 1;
+        TCH_CK(e, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        TCH_CK(e, launch_rare_batch(b->rplan, b->num_sms, st));
+        TCH_CK(e, launch_tc_batch(b->tplan, b->num_sms, st));
+        TCH_CK(e, cudaStreamEndCapture(st, &graph));
+        TCH_CK(e, cudaGraphInstantiate(&b->exec, graph, 0));
+        cudaGraphDestroy(graph);
+        b->exec_out = d_out;
+        return 0;
+    }
     // largest sets first, each to the least-loaded branch; one rare-count block
     // per branch, sized for its largest set (a branch runs its sets in order)
     for (int s : order) {
@@ -235,7 +344,19 @@ int tch_batch_check(tch_batch* b, char* err, int errlen) {
     if (!b) return e.set("null batch");
     for (size_t s = 0; s < b->sets.size(); s++)
         if (solver_check(b->sets[s], e)) return 1;
+    if (b->dErr) {  // the persistent tile pass
+        int h = 0;
+        TCH_CK(e, cudaSetDevice(b->device));
+        TCH_CK(e, cudaMemcpy(&h, b->dErr, sizeof(int), cudaMemcpyDeviceToHost));
+        if (h) {
+            cudaMemset(b->dErr, 0, sizeof(int));
+            return e.set("device reported error 0x%x in the batch's tile pass (%s%s)", h,
+                         (h & DEVERR_OVERFLOW) ? "distance overflow " : "", (h & DEVERR_TIMEOUT) ? "wait timeout" : "");
+        }
+    }
     return 0;
+fail:
+    return 1;
 }
 
 int tch_batch_tune(tch_batch* b, uint16_t* d_out, void* stream, int reps, double* best_ms, int* best_branches,
@@ -245,12 +366,15 @@ int tch_batch_tune(tch_batch* b, uint16_t* d_out, void* stream, int reps, double
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     double best = 1e300;
     int bb = b ? b->branches : 8;
+    const char* why = "";
     if (!b || !d_out) return e.set("null argument");
     if (cudaSetDevice(b->device) != cudaSuccess) return e.set("cudaSetDevice(%d) failed", b->device);
+    const bool persistent = persistent_ready(b, &why);
     reps = std::max(reps, 1);
     TCH_CK(e, cudaEventCreate(&t0));
     TCH_CK(e, cudaEventCreate(&t1));
-    for (int nb : {1, 4, 8, 16, 32}) {
+    for (int nb : {0, 1, 4, 8, 16, 32}) {
+        if (nb == 0 && !persistent) continue;
         b->branches = nb;
         if (build_graph(b, d_out, e)) goto fail;
         TCH_CK(e, cudaGraphLaunch(b->exec, st));  // warm
@@ -276,7 +400,8 @@ fail:
 }
 
 int tch_batch_set_schedule(tch_batch* b, int branches) {
-    if (!b || branches < 1 || branches > 64) return 1;
+    const char* why = "";
+    if (!b || branches < 0 || branches > 64 || (branches == 0 && !persistent_ready(b, &why))) return 1;
     b->branches = branches;
     drop_graph(b);
     return 0;
@@ -302,6 +427,10 @@ void tch_batch_destroy(tch_batch* b) {
     for (auto st : b->streams) cudaStreamDestroy(st);
     if (b->origin) cudaStreamDestroy(b->origin);
     for (auto p : b->rbuf) cudaFree(p);
+    rare_batch_release(&b->rplan);
+    tc_batch_release(&b->tplan);
+    cudaFree(b->pbuf);
+    cudaFree(b->dErr);
     for (auto ev : b->events) cudaEventDestroy(ev);
     for (auto s : b->sets) solver_free(s);
     delete b;

@@ -209,6 +209,52 @@ __device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_
     }
 }
 
+// Many sets' whole triangles in one launch (batched solves): the rows of
+// every job laid end to end (row_job: the job of every row), one CTA per row
+// as in rare_dense_kernel, each row counted in one pass (the launcher checks
+// that every job's width fits the counters).
+struct RareJob {
+    RareGroups g;
+    uint16_t* R;
+    size_t ldr;
+    int cend;  // up(n, 256): the job's stripe is its whole triangle (r0 = 0)
+    int row0;  // the job's first row in the launch
+};
+
+template <int T>
+__global__ void __launch_bounds__(T, 1024 / T)
+    rare_batch_kernel(const RareJob* __restrict__ jobs, const int* __restrict__ row_job, int total_rows,
+                      int cwords) {
+    extern __shared__ uint4 smem_rd[];
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(smem_rd);
+    uint32_t* pre = cnt + cwords;
+    uint32_t* run = pre + (2 * T) + 1;
+    uint32_t* wsum = run + (2 * T);
+    const int tid = threadIdx.x;
+    for (int gr = blockIdx.x; gr < total_rows; gr += gridDim.x) {
+        const RareJob& jb = jobs[__ldg(row_job + gr)];
+        const RareGroups g = jb.g;
+        const int i = gr - jb.row0;
+        const int n = g.n, L = g.L;
+        const int cbeg = i & ~(kRareDenseAlign - 1);  // first column of the row's diagonal tile
+        const int nq = (jb.cend - cbeg) >> 3;
+        for (int w = tid; w < nq; w += T) smem_rd[w] = make_uint4(0, 0, 0, 0);
+        const uint32_t jlo = (uint32_t)(i + 1), jhi = (uint32_t)n;
+        for (int kc = 0; jlo < jhi && kc < L; kc += (2 * T)) {
+            const int k0 = kc + 2 * tid;
+            uint32_t lo0 = 0, lo1 = 0, l0 = 0, l1 = 0;
+            const CellPair c = load_cells(g, i, k0);
+            if (k0 < L) l0 = partner_run(g, i, c.a0, c.m0, g.cnt_off[k0], jlo, jhi, &lo0);
+            if (k0 + 1 < L) l1 = partner_run(g, i, c.a1, c.m1, g.cnt_off[k0 + 1], jlo, jhi, &lo1);
+            count_runs<T>(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, cbeg);
+        }
+        __syncthreads();
+        uint4* dst = reinterpret_cast<uint4*>(jb.R + (size_t)i * jb.ldr + (size_t)cbeg);
+        for (int w = tid; w < nq; w += T) dst[w] = smem_rd[w];
+        __syncthreads();
+    }
+}
+
 template <int T>
 __global__ void __launch_bounds__(T, 1024 / T)
     rare_dense_kernel(const RareGroups g, int r0, int rows, uint16_t* __restrict__ R, size_t ldr, int cend,
@@ -370,6 +416,65 @@ cudaError_t launch_rare_from_lists(const uint32_t* start, const uint32_t* js, in
     rare_lists_kernel<<<std::max(1, std::min(rows, sms)), 1024, cwords * 4, st>>>(start, js, n, r0, rows, R, ldr,
                                                                                  r0 + (int)width, cwords, err);
     return cudaGetLastError();
+}
+
+cudaError_t rare_batch_prepare(const std::vector<RareBatchItem>& items, RareBatchPlan* plan) {
+    std::vector<RareJob> jobs;
+    std::vector<int> row_job;
+    int row0 = 0, cwords = 1;
+    for (const RareBatchItem& it : items) {
+        if (it.g.n < 2) continue;
+        const size_t width = up((size_t)it.g.n, kRareDenseAlign);
+        if (it.ldr < width || (it.ldr & 7) || ((uintptr_t)it.R & 15)) return cudaErrorInvalidValue;
+        if (width > (size_t)2 * RD_WORDS) return cudaErrorInvalidValue;  // one counter pass per row
+        RareJob j;
+        j.g = it.g;
+        j.R = it.R;
+        j.ldr = it.ldr;
+        j.cend = (int)width;
+        j.row0 = row0;
+        row0 += it.g.n;
+        cwords = std::max(cwords, (int)(width / 2));
+        row_job.insert(row_job.end(), (size_t)it.g.n, (int)jobs.size());
+        jobs.push_back(j);
+    }
+    rare_batch_release(plan);
+    plan->njobs = (int)jobs.size();
+    plan->total_rows = row0;
+    plan->cwords = cwords;
+    if (jobs.empty()) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&plan->d_jobs, jobs.size() * sizeof(RareJob));
+    if (e == cudaSuccess) e = cudaMalloc(&plan->d_row_job, row_job.size() * sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(plan->d_jobs, jobs.data(), jobs.size() * sizeof(RareJob), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(plan->d_row_job, row_job.data(), row_job.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    static bool attrs[kMaxDevices] = {};
+    bool& attr = attrs[current_device()];
+    if (!attr) {
+        e = cudaFuncSetAttribute(rare_batch_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 rd_smem<256>(RD_WORDS));
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_rare_batch(const RareBatchPlan& plan, int sms, cudaStream_t st) {
+    if (!plan.njobs || !plan.total_rows) return cudaSuccess;
+    const int grid = std::max(1, std::min(plan.total_rows, sms * 8));
+    rare_batch_kernel<256><<<grid, 256, rd_smem<256>(plan.cwords), st>>>(
+        static_cast<const RareJob*>(plan.d_jobs), static_cast<const int*>(plan.d_row_job), plan.total_rows,
+        plan.cwords);
+    return cudaGetLastError();
+}
+
+void rare_batch_release(RareBatchPlan* plan) {
+    if (plan->d_jobs) cudaFree(plan->d_jobs);
+    if (plan->d_row_job) cudaFree(plan->d_row_job);
+    plan->d_jobs = plan->d_row_job = nullptr;
+    plan->njobs = plan->total_rows = 0;
 }
 
 cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R, size_t ldr, int sms,

@@ -154,6 +154,24 @@ struct TcMaps {
     int n;
 };
 
+// One triangle of a batch: its geometry, K stages, tensor maps and output.
+struct TcJob {
+    int n, rows, kblocks;  // rows [0, rows) against columns [0, n) of one set (r0 = c0 = 0)
+    int nchunks;           // K chunks: A maps at jmaps[map0 ..), B maps at jmaps[map0 + nchunks ..)
+    int kbl[kMaxKChunks];  // K stages of each chunk
+    int map0;
+    int tile0;             // first tile of the job in the launch
+    TileSpace ts;          // one raster group
+    const uint16_t* rdense;
+    size_t ldr;
+    uint16_t* out;
+    size_t ldo;
+    int vec_store;
+};
+
+// One stripe (the fields below `err` unused), or a batch of triangles
+// (MULTI: `jobs`, their tensor maps `jmaps` and the job of every tile
+// `tile_job`, all in device memory, written before the launch).
 struct TcParams {
     int n, r0, rows;  // columns end at n; rows [r0, r0 + rows) of the A operand
     int c0;           // first column: r0 (upper triangle) or 0 (rectangle)
@@ -167,8 +185,33 @@ struct TcParams {
     size_t ldo;
     int vec_store;  // 1: 16-byte stores (ldo a multiple of 8, out 16-byte aligned)
     int* err;
+    const TcJob* jobs;
+    const CUtensorMap* jmaps;
+    const int* tile_job;
 };
 
+// t -> (bi, bj) when the whole triangle is one raster group (a batch job).
+__device__ bool tile_coords_one_group(const TileSpace& ts, int t, int* bi_out, int* bj_out) {
+    const int g1 = ts.nbi;
+    int bj = first_col(ts, 0);
+    for (; bj < ts.nbj; bj++) {
+        const int rows = min(g1 - 1, last_row(ts, bj)) + 1;
+        if (rows == g1) break;
+        if (t < rows) {
+            *bi_out = t;
+            *bj_out = bj;
+            return true;
+        }
+        t -= rows;
+    }
+    bj += t / g1;
+    if (bj >= ts.nbj) return false;
+    *bi_out = t % g1;
+    *bj_out = bj;
+    return true;
+}
+
+template <bool MULTI>
 __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_constant__ TcMaps maps, const TcParams p) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -197,10 +240,11 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
         mbar_init(drain, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        for (int c = 0; c < maps.n; c++) {
-            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&maps.a[c]) : "memory");
-            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&maps.b[c]) : "memory");
-        }
+        if (!MULTI)
+            for (int c = 0; c < maps.n; c++) {
+                asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&maps.a[c]) : "memory");
+                asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&maps.b[c]) : "memory");
+            }
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -232,16 +276,36 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
             uint32_t issued_ph[STAGES];
             for (int q = 0; q < STAGES; q++) issued[q] = 0, issued_ph[q] = 0;
             for (int t = blockIdx.x; ok && t < p.num_tiles; t += gridDim.x) {
-                int bi, bj;
-                if (!tile_coords(p.ts, p.gt, t, &bi, &bj)) break;
-                const int y_a = p.r0 + bi * BM, y_b = p.c0 + bj * BN;
+                int bi, bj, y_a, y_b, kblocks;
+                const CUtensorMap* ma = maps.a;
+                const CUtensorMap* mb = maps.b;
+                const int* kbls = maps.kblocks;
+                if (!MULTI) {
+                    if (!tile_coords(p.ts, p.gt, t, &bi, &bj)) break;
+                    y_a = p.r0 + bi * BM;
+                    y_b = p.c0 + bj * BN;
+                    kblocks = p.kblocks;
+                } else {
+                    const TcJob& jb = p.jobs[__ldg(p.tile_job + t)];
+                    if (!tile_coords_one_group(jb.ts, t - jb.tile0, &bi, &bj)) break;
+                    y_a = bi * BM;
+                    y_b = bj * BN;
+                    kblocks = jb.kblocks;
+                    ma = p.jmaps + jb.map0;
+                    mb = ma + jb.nchunks;
+                    kbls = jb.kbl;
+                }
                 int ch = 0, kbl = 0;  // K chunk and block inside it
-                for (int kb = 0; kb < p.kblocks; kb++) {
+                int kbl_end = kbls[0];
+                for (int kb = 0; kb < kblocks; kb++) {
                     if (!mbar_wait(&empty[s], ph ^ 1, abort_flag, p.err)) { ok = false; break; }
                     mbar_expect_tx(&full[s], STAGE_BYTES);
-                    tma_load_2d(&maps.a[ch], &full[s], stage_a + s * A_BYTES, kbl * BK, y_a);
-                    tma_load_2d(&maps.b[ch], &full[s], stage_b + s * B_BYTES, kbl * BK, y_b);
-                    if (++kbl == maps.kblocks[ch]) kbl = 0, ch++;
+                    tma_load_2d(ma + ch, &full[s], stage_a + s * A_BYTES, kbl * BK, y_a);
+                    tma_load_2d(mb + ch, &full[s], stage_b + s * B_BYTES, kbl * BK, y_b);
+                    if (++kbl == kbl_end) {
+                        kbl = 0;
+                        if (++ch < kMaxKChunks) kbl_end = kbls[ch];
+                    }
                     issued[s] = 1;
                     issued_ph[s] = ph;
                     if (++s == STAGES) s = 0, ph ^= 1;
@@ -272,10 +336,11 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
             uint32_t ph = 0, aph = 0;
             bool ok = true;
             for (int t = blockIdx.x; ok && t < p.num_tiles; t += gridDim.x) {
+                const int kblocks = MULTI ? p.jobs[__ldg(p.tile_job + t)].kblocks : p.kblocks;
                 if (!mbar_wait(&tempty[acc], aph ^ 1, abort_flag, p.err)) { ok = false; break; }
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + (uint32_t)(acc * ACC_STRIDE);
-                for (int kb = 0; kb < p.kblocks; kb++) {
+                for (int kb = 0; kb < kblocks; kb++) {
                     if (!mbar_wait(&full[s], ph, abort_flag, p.err)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t a0 = smem_u32(stage_a + s * A_BYTES), b0 = smem_u32(stage_b + s * B_BYTES);
@@ -300,19 +365,36 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
         // ------------------------------------------------------------ epilogue
         const int q = warp & 3;           // TMEM lanes [32 q, 32 q + 32) belong to this warp
         const int half = (warp - 2) / 4;  // column half of the tile
-        const int iend = p.r0 + p.rows;
-        const bool dense = p.rdense != nullptr;
         int acc = 0;
         uint32_t aph = 0;
         int bad = 0;
         for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x) {
             int bi, bj;
-            if (!tile_coords(p.ts, p.gt, t, &bi, &bj)) break;
-            const int i = p.r0 + bi * BM + q * 32 + lane;  // this lane's row
-            const int j0 = p.c0 + bj * BN;
+            int n = p.n, r0 = p.r0, c0 = p.c0, iend = p.r0 + p.rows, vec_store = p.vec_store;
+            const uint16_t* rdense = p.rdense;
+            uint16_t* out = p.out;
+            size_t ldo = p.ldo, ldr = p.ldr;
+            if (!MULTI) {
+                if (!tile_coords(p.ts, p.gt, t, &bi, &bj)) break;
+            } else {
+                const TcJob& jb = p.jobs[__ldg(p.tile_job + t)];
+                if (!tile_coords_one_group(jb.ts, t - jb.tile0, &bi, &bj)) break;
+                n = jb.n;
+                r0 = 0;
+                c0 = 0;
+                iend = jb.rows;
+                vec_store = jb.vec_store;
+                rdense = jb.rdense;
+                out = jb.out;
+                ldo = jb.ldo;
+                ldr = jb.ldr;
+            }
+            const bool dense = rdense != nullptr;
+            const int i = r0 + bi * BM + q * 32 + lane;  // this lane's row
+            const int j0 = c0 + bj * BN;
             const bool row_ok = i < iend;
-            const size_t orow = (size_t)(i - p.r0) * p.ldo;
-            const size_t rrow = (size_t)(i - p.r0) * p.ldr;
+            const size_t orow = (size_t)(i - r0) * ldo;
+            const size_t rrow = (size_t)(i - r0) * ldr;
             if (!mbar_wait(&tfull[acc], aph, abort_flag, p.err)) break;
             tc_fence_after();
             const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * ACC_STRIDE);
@@ -320,13 +402,13 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
             for (int cc = 0; cc < WARP_CHUNKS; cc++) {
                 const int c = half * WARP_CHUNKS + cc;
                 const int cb = j0 + c * CHUNK;  // first column of the chunk
-                const bool live = row_ok && cb < p.n;
+                const bool live = row_ok && cb < n;
                 // this row's rare counts for the chunk (32 bytes), fetched before
                 // the accumulator read so the two overlap; a row of the block is
                 // at least up(n - c0, 16) wide, so a live chunk is in bounds
                 uint4 r4[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
                 if (dense && live) {
-                    const uint4* src = reinterpret_cast<const uint4*>(p.rdense + rrow + (size_t)(cb - p.c0));
+                    const uint4* src = reinterpret_cast<const uint4*>(rdense + rrow + (size_t)(cb - c0));
                     r4[0] = __ldg(src);
                     r4[1] = __ldg(src + 1);
                 }
@@ -351,9 +433,9 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
                     w[e] = (uint32_t)(x0 & 0xFFFF) | ((uint32_t)(x1 & 0xFFFF) << 16);
                 }
                 if (live) {
-                    uint16_t* dst = p.out + orow + (size_t)(cb - p.c0);
-                    if (cb + CHUNK <= p.n) {
-                        if (p.vec_store) {
+                    uint16_t* dst = out + orow + (size_t)(cb - c0);
+                    if (cb + CHUNK <= n) {
+                        if (vec_store) {
                             uint4* d4 = reinterpret_cast<uint4*>(dst);
                             d4[0] = make_uint4(w[0], w[1], w[2], w[3]);
                             d4[1] = make_uint4(w[4], w[5], w[6], w[7]);
@@ -365,7 +447,7 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
                     } else {
 #pragma unroll
                         for (int e = 0; e < CHUNK; e++)
-                            if (cb + e < p.n) dst[e] = (uint16_t)(w[e / 2] >> (16 * (e & 1)));
+                            if (cb + e < n) dst[e] = (uint16_t)(w[e / 2] >> (16 * (e & 1)));
                     }
                 }
             }
@@ -417,8 +499,8 @@ cudaError_t launch_one(const Fp4Operands& A, const Fp4Operands& B, const uint16_
     static bool attrs[kMaxDevices] = {};
     const int dev = current_device();
     if (!attrs[dev]) {
-        const cudaError_t e = cudaFuncSetAttribute(tc_stripe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   SMEM_BYTES);
+        const cudaError_t e = cudaFuncSetAttribute(tc_stripe_kernel<false>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         if (e != cudaSuccess) return e;
         attrs[dev] = true;
     }
@@ -467,13 +549,110 @@ cudaError_t launch_one(const Fp4Operands& A, const Fp4Operands& B, const uint16_
     p.ldo = a.ldo;
     p.vec_store = ((a.ldo & 7) == 0 && ((uintptr_t)a.out & 15) == 0) ? 1 : 0;
     p.err = a.err;
+    p.jobs = nullptr;
+    p.jmaps = nullptr;
+    p.tile_job = nullptr;
     if (p.num_tiles == 0) return cudaSuccess;
     const int grid = std::min(p.num_tiles, std::max(num_sms, 1));
-    tc_stripe_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(maps, p);
+    tc_stripe_kernel<false><<<grid, THREADS, SMEM_BYTES, st>>>(maps, p);
     return cudaGetLastError();
 }
 
 }  // namespace
+
+cudaError_t tc_batch_prepare(const std::vector<TcBatchItem>& items, TcBatchPlan* plan, int* err) {
+    std::vector<TcJob> jobs;
+    std::vector<CUtensorMap> mh;
+    std::vector<int> tile_job;
+    int tile0 = 0;
+    for (const TcBatchItem& it : items) {
+        const Fp4Operands& A = *it.ops;
+        if (it.n < 2) continue;
+        const KChunks& ka = A.pos;
+        const KChunks& kb = A.neg;
+        if (A.kb <= 0 || (A.kb % BK) || ka.n < 1 || ka.kb != A.kb || !same_chunking(ka, kb) || (ka.width % BK))
+            return cudaErrorInvalidValue;
+        if ((it.ldo & 1) || ((uintptr_t)it.out & 3)) return cudaErrorInvalidValue;
+        if (it.R && ((it.ldr & 7) || ((uintptr_t)it.R & 15))) return cudaErrorInvalidValue;
+        TcJob jb = TcJob{};
+        jb.n = it.n;
+        jb.rows = it.n;
+        jb.kblocks = A.kb / BK;
+        jb.nchunks = ka.n;
+        jb.map0 = (int)mh.size();
+        for (int c = 0; c < ka.n; c++) {
+            CUtensorMap m;
+            if (!make_map(&m, ka.p[c], A.n_rows, ka.width_of(c), BM)) return cudaErrorInvalidValue;
+            mh.push_back(m);
+            jb.kbl[c] = ka.width_of(c) / BK;
+        }
+        for (int c = 0; c < ka.n; c++) {
+            CUtensorMap m;
+            if (!make_map(&m, kb.p[c], A.n_rows, kb.width_of(c), BN)) return cudaErrorInvalidValue;
+            mh.push_back(m);
+        }
+        jb.ts.nbi = (it.n + BM - 1) / BM;
+        jb.ts.nbj = (it.n + BN - 1) / BN;
+        jb.ts.gs = jb.ts.nbi;
+        jb.ts.rect = 0;
+        jb.rdense = it.R;
+        jb.ldr = it.ldr;
+        jb.out = it.out;
+        jb.ldo = it.ldo;
+        jb.vec_store = ((it.ldo & 7) == 0 && ((uintptr_t)it.out & 15) == 0) ? 1 : 0;
+        const long long tiles = tiles_in(jb.ts, 0, jb.ts.nbi);
+        if ((long long)tile0 + tiles > INT32_MAX) return cudaErrorInvalidValue;
+        jb.tile0 = tile0;
+        tile0 += (int)tiles;
+        tile_job.insert(tile_job.end(), (size_t)tiles, (int)jobs.size());
+        jobs.push_back(jb);
+    }
+    tc_batch_release(plan);
+    plan->err = err;
+    plan->njobs = (int)jobs.size();
+    plan->num_tiles = tile0;
+    if (jobs.empty()) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&plan->d_jobs, jobs.size() * sizeof(TcJob));
+    if (e == cudaSuccess) e = cudaMalloc(&plan->d_maps, mh.size() * sizeof(CUtensorMap));
+    if (e == cudaSuccess) e = cudaMalloc(&plan->d_tile_job, tile_job.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(plan->d_jobs, jobs.data(), jobs.size() * sizeof(TcJob), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(plan->d_maps, mh.data(), mh.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(plan->d_tile_job, tile_job.data(), tile_job.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    static bool attrs[kMaxDevices] = {};
+    const int dev = current_device();
+    if (!attrs[dev]) {
+        e = cudaFuncSetAttribute(tc_stripe_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        attrs[dev] = true;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_tc_batch(const TcBatchPlan& plan, int num_sms, cudaStream_t st) {
+    if (plan.num_tiles == 0 || plan.njobs == 0) return cudaSuccess;
+    TcMaps maps;  // the batch's maps are in device memory
+    maps.n = 0;
+    TcParams p = TcParams{};
+    p.gt.ngroups = 0;
+    p.num_tiles = plan.num_tiles;
+    p.err = plan.err;
+    p.jobs = static_cast<const TcJob*>(plan.d_jobs);
+    p.jmaps = static_cast<const CUtensorMap*>(plan.d_maps);
+    p.tile_job = static_cast<const int*>(plan.d_tile_job);
+    const int grid = std::min(plan.num_tiles, std::max(num_sms, 1));
+    tc_stripe_kernel<true><<<grid, THREADS, SMEM_BYTES, st>>>(maps, p);
+    return cudaGetLastError();
+}
+
+void tc_batch_release(TcBatchPlan* plan) {
+    if (plan->d_jobs) cudaFree(plan->d_jobs);
+    if (plan->d_maps) cudaFree(plan->d_maps);
+    if (plan->d_tile_job) cudaFree(plan->d_tile_job);
+    plan->d_jobs = plan->d_maps = plan->d_tile_job = nullptr;
+    plan->njobs = plan->num_tiles = 0;
+}
 
 cudaError_t launch_tc_stripe(const Fp4Operands& ops, const Fp4Operands* bops, const uint16_t* R, size_t ldr,
                              const StripeArgs& a, int num_sms, cudaStream_t st) {

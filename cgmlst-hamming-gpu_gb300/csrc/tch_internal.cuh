@@ -177,6 +177,29 @@ void free_fp4(Fp4Operands* X);
 // counts R (row stride ldr, column j at j - c0; nullptr = no rare term).
 cudaError_t launch_tc_stripe(const Fp4Operands& ops, const Fp4Operands* bops, const uint16_t* R, size_t ldr,
                              const StripeArgs& a, int num_sms, cudaStream_t st);
+// Many whole triangles in one persistent launch (batched solves): item k's
+// upper triangle of its own operand into its own output, minus its own rare
+// counts (R, ldr as for launch_tc_stripe; may be null).  tc_batch_prepare
+// writes the job descriptors, tensor maps and tile -> job table to device
+// memory (the plan owns them); launch_tc_batch runs them (capturable).
+struct TcBatchItem {
+    const Fp4Operands* ops = nullptr;
+    int n = 0;
+    const uint16_t* R = nullptr;
+    size_t ldr = 0;
+    uint16_t* out = nullptr;
+    size_t ldo = 0;
+};
+struct TcBatchPlan {
+    void* d_jobs = nullptr;
+    void* d_maps = nullptr;
+    void* d_tile_job = nullptr;
+    int njobs = 0, num_tiles = 0;
+    int* err = nullptr;
+};
+cudaError_t tc_batch_prepare(const std::vector<TcBatchItem>& items, TcBatchPlan* plan, int* err);
+cudaError_t launch_tc_batch(const TcBatchPlan& plan, int num_sms, cudaStream_t st);
+void tc_batch_release(TcBatchPlan* plan);
 
 // ---- k_encode.cu ------------------------------------------------------------------
 // Rates of the analytic tau model on this GPU.
@@ -216,6 +239,23 @@ cudaError_t launch_rare_query(const RareGroups& g, const uint32_t* xq, int m, ui
                               cudaStream_t st);
 cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R, size_t ldr, int sms,
                               cudaStream_t st);
+// Every set's whole-triangle rare counts in one launch (batched solves):
+// item k's counts into its own block R (ldr >= up(n, 256); row i's columns
+// from its diagonal tile on, as launch_rare_dense with r0 = 0, rows = n).
+// Sets wider than one counter pass (65 536 columns) are rejected.
+struct RareBatchItem {
+    RareGroups g;
+    uint16_t* R = nullptr;
+    size_t ldr = 0;
+};
+struct RareBatchPlan {
+    void* d_jobs = nullptr;
+    void* d_row_job = nullptr;  // the job of every row
+    int njobs = 0, total_rows = 0, cwords = 0;
+};
+cudaError_t rare_batch_prepare(const std::vector<RareBatchItem>& items, RareBatchPlan* plan);
+cudaError_t launch_rare_batch(const RareBatchPlan& plan, int sms, cudaStream_t st);
+void rare_batch_release(RareBatchPlan* plan);
 // The same block from pair lists (partners of row i: js[start[i] .. start[i +
 // 1]), in any order, repeated once per shared rare allele); a partner outside
 // (i, n) sets DEVERR_RARE_PAIR in *err and is skipped.
@@ -286,6 +326,10 @@ int solver_stripe_counts(tch_solver* s, int r0, int rows, uint16_t* d_out, size_
                          cudaStream_t st, Err& e);
 double solver_work(const tch_solver* s);
 int solver_size(const tch_solver* s);
+// The packed fp4 operand of a tensor-core solver (nullptr for the others).
+const Fp4Operands* solver_operands(const tch_solver* s);
+// The rare groups of a dense-rare solver (false: it holds pair lists).
+bool solver_rare_groups(const tch_solver* s, RareGroups* g);
 
 // ---- k_mlp.cu ----------------------------------------------------------------------
 constexpr int kMlpIn = TCH_TAU_FEATURES, kMlpHidden = TCH_MLP_HIDDEN, kMlpParams = TCH_MLP_PARAMS;

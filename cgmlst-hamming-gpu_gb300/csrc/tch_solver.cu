@@ -845,6 +845,14 @@ double solver_work(const tch_solver* s) { return (double)s->n * (double)(s->n - 
 
 int solver_size(const tch_solver* s) { return s->n; }
 
+const Fp4Operands* solver_operands(const tch_solver* s) { return is_tc(s->kernel) ? &s->X : nullptr; }
+
+bool solver_rare_groups(const tch_solver* s, RareGroups* g) {
+    if (!s->dense) return false;
+    *g = rare_groups(s);
+    return true;
+}
+
 }  // namespace tch
 
 // ==================================================================================

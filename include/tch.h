@@ -261,11 +261,17 @@ void tch_server_destroy(tch_server* sv);
  * device once.  tch_batch_run writes every set's whole upper triangle into one
  * device buffer: set s at d_out + offsets[s], row stride ld[s] u16
  * (tch_batch_layout; offsets[count] = total u16 elements), cell (i, j), i < j,
- * at (i * ld[s] + j).  The launches of all sets are spread over parallel
- * streams and captured once as a CUDA graph (per output buffer), replayed on
- * every later run; tch_batch_tune times every schedule (the number of branch
- * streams) and keeps the fastest.
- * Errors found on the device are reported by tch_batch_check. */
+ * at (i * ld[s] + j).  A schedule is captured once as a CUDA graph (per
+ * output buffer) and replayed on every later run:
+ *   branches >= 1  every set's rare counts + tile pass, the sets spread over
+ *                  `branches` parallel streams (default 8);
+ *   branches == 0  persistent: two launches for the whole batch, the rare
+ *                  counts of every row of every set, then one tile pass over
+ *                  every set's tiles (dense rare counts, sets of at most
+ *                  65 536 rows, at most 8 GiB of rare counts in all; otherwise
+ *                  tch_batch_set_schedule(b, 0) returns 1 and the tuner skips it).
+ * tch_batch_tune times every schedule and keeps the fastest (*best_branches,
+ * 0 = persistent).  Errors found on the device are reported by tch_batch_check. */
 typedef struct tch_batch tch_batch;
 int tch_batch_create(int device, int count, const int* n, const int* L, const uint64_t* const* calls, const int* tau,
                      tch_batch** out, char* err, int errlen);
