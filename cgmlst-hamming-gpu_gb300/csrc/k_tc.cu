@@ -275,6 +275,7 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
             int issued[STAGES];
             uint32_t issued_ph[STAGES];
             for (int q = 0; q < STAGES; q++) issued[q] = 0, issued_ph[q] = 0;
+            int last_job = -1;  // MULTI: the job whose maps this thread has acquired
             for (int t = blockIdx.x; ok && t < p.num_tiles; t += gridDim.x) {
                 int bi, bj, y_a, y_b, kblocks;
                 const CUtensorMap* ma = maps.a;
@@ -286,7 +287,8 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
                     y_b = p.c0 + bj * BN;
                     kblocks = p.kblocks;
                 } else {
-                    const TcJob& jb = p.jobs[__ldg(p.tile_job + t)];
+                    const int job = __ldg(p.tile_job + t);
+                    const TcJob& jb = p.jobs[job];
                     if (!tile_coords_one_group(jb.ts, t - jb.tile0, &bi, &bj)) break;
                     y_a = bi * BM;
                     y_b = bj * BN;
@@ -294,6 +296,10 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
                     ma = p.jmaps + jb.map0;
                     mb = ma + jb.nchunks;
                     kbls = jb.kbl;
+                    if (job != last_job) {
+                        for (int c = 0; c < 2 * jb.nchunks; c++) tensormap_acquire(ma + c);
+                        last_job = job;
+                    }
                 }
                 int ch = 0, kbl = 0;  // K chunk and block inside it
                 int kbl_end = kbls[0];
