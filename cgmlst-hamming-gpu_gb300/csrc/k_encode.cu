@@ -14,7 +14,9 @@
 //   3. cell_rank_kernel   every cell -> its rank (u16 matrix x, n x L)
 //      (host)             tau from the counts (analytic model), frequent
 //                         column map and per-locus offsets
-//   4. pack_x_kernel      x -> X rows [presence | one-hot] as e4m3 bytes
+//   4. pack_x_kernel      x -> X rows [presence | one-hot] as packed e2m1
+//                         nibbles (+1.0), the pos copy; negate_onehot_kernel
+//                         derives the neg copy (one-hot part -1.0)
 //   5. group_fill_kernel  rows of each rare (locus, rank) group of size >= 2
 //      group_sort_kernel  ... sorted ascending inside the group
 //   6. rare_rows_kernel   one CTA per row: u16 counters over the columns
@@ -23,8 +25,8 @@
 //                         emits the partners in ascending order with their
 //                         multiplicity.  Run twice: counts, then the CSR.
 //
-// The CSR rows come out ascending, so the stripe kernels subtract them in the
-// tile epilogue.  All ids are compared for equality only; any 64-bit values
+// The CSR rows come out ascending; the tensor-core path counts them into the
+// dense rare-count block that the tile epilogue subtracts.  All ids are compared for equality only; any 64-bit values
 // work (hashed ids included).
 
 #include <chrono>

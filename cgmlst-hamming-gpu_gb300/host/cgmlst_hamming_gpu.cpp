@@ -46,11 +46,12 @@
 namespace {
 
 // GB300 rates for the analytic tau of the host-encoder path (--host-encode):
-// pair-columns/s of the tcgen05 fp8 kernel, and rare pairs/s including their
-// 4-byte upload through tch_run (the device-encoder path builds the pairs on
-// the GPU and uses the library's own model).
-constexpr double kGemmRateGB300 = 1.6e15;
-constexpr double kRareRateGB300 = 1.0e11;
+// pair-columns/s of the tcgen05 fp4 tile pass, and rare pairs/s including
+// their 4-byte upload through tch_run (about 190 GB/s of host link; the
+// device-encoder path builds the rare groups on the GPU and uses the
+// library's own model).
+constexpr double kGemmRateGB300 = 2.9e15;
+constexpr double kRareRateGB300 = 4.5e10;
 
 // Set while a helper thread creates the CUDA context (during the input's
 // load): an error exit then skips the runtime's teardown, which must not run

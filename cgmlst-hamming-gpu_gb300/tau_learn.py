@@ -16,7 +16,8 @@ measured device time of one whole-triangle solve under that schedule (rare
 counts + tile pass, CUDA events, median of 3).
 
 train: the MLP of csrc/k_mlp.cu on ln(ms), trained on the GPU by the library's
-kernels (tch_mlp_train), every fifth profile set held out.  Feature
+kernels (tch_mlp_train), every fifth profile set held out and the longer sets'
+candidates repeated in the training rows (oversample).  Feature
 standardisation is folded into the first layer, so the saved model takes the
 raw feature rows.  The report compares, on the held-out sets, the measured time
 at the learned pick (tau and schedule), at the analytic pick (its tau, the
@@ -204,6 +205,18 @@ def evaluate(w: np.ndarray, data, device: int = 0) -> dict:
                 mean_analytic_over_best=float(np.mean([r["ms_analytic"] / r["ms_best"] for r in out])))
 
 
+def oversample(ds: np.ndarray, ms: np.ndarray, idx: np.ndarray) -> np.ndarray:
+    """Training rows with each profile set's candidates repeated
+    round(log2(best ms / 0.2 ms)) times (1 to 8): the squared error in ln(ms)
+    weighs every set alike, while a wrong pick costs in proportion to the set's
+    time, so the sets that dominate a workload's time get more weight."""
+    best = {}
+    for d, t in zip(ds, ms):
+        best[d] = min(best.get(d, np.inf), t)
+    reps = np.array([int(np.clip(np.round(np.log2(best[d] / 0.2)), 1, 8)) for d in ds[idx]])
+    return np.repeat(idx, reps)
+
+
 def train(sweep_path: str, out: str, steps: int = 6000, lr: float = 3e-3, seed: int = 7, device: int = 0) -> dict:
     data = dict(np.load(sweep_path))
     ds = data["ds"]
@@ -214,14 +227,15 @@ def train(sweep_path: str, out: str, steps: int = 6000, lr: float = 3e-3, seed: 
     sd = X[tr].std(0)
     sd[sd < 1e-6] = 1.0
     Xn = ((X - mu) / sd).astype(np.float32)
+    idx = oversample(ds, data["ms"], np.nonzero(tr)[0])
     w = tch.mlp_init(seed)
     t0 = time.time()
-    w, loss1 = tch.mlp_train(w, Xn[tr], y[tr], steps // 2, lr, device)
-    w, loss2 = tch.mlp_train(w, Xn[tr], y[tr], steps - steps // 2, lr / 5, device)
+    w, loss1 = tch.mlp_train(w, Xn[idx], y[idx], steps // 2, lr, device)
+    w, loss2 = tch.mlp_train(w, Xn[idx], y[idx], steps - steps // 2, lr / 5, device)
     secs = time.time() - t0
     w_raw = fold_standardisation(w, mu, sd)
     rep = evaluate(w_raw, data, device)
-    rep.update(train_rows=int(tr.sum()), holdout_rows=int((~tr).sum()), steps=steps, final_train_mse=loss2,
+    rep.update(train_rows=int(len(idx)), train_sets=int(len(np.unique(ds[tr]))), holdout_rows=int((~tr).sum()), steps=steps, final_train_mse=loss2,
                train_seconds=secs)
     w_raw.astype("<f4").tofile(out)
     return rep
