@@ -706,7 +706,10 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
         TCH_CK(e, dalloc(&sorted, n_members, &tmp_bytes));
         TCH_CK(e, dalloc(&gfill, off_h[L], &tmp_bytes));
         TCH_CK(e, cudaMemset(gfill, 0, std::max<uint64_t>(off_h[L], 1) * 4));
-        if (dense_rare) TCH_CK(e, dalloc(&mpos, (size_t)n * L, &tmp_bytes));
+        if (dense_rare) {  // cells in no rare group keep the sentinel: the rare counts skip them
+            TCH_CK(e, dalloc(&mpos, (size_t)n * L, &tmp_bytes));
+            TCH_CK(e, cudaMemset(mpos, 0xFF, std::max<size_t>((size_t)n * L, 1) * 4));
+        }
         if (ngroups) {
             TCH_CK(e, dalloc(&groups_d, groups.size(), &tmp_bytes));
             TCH_CK(e, cudaMemcpy(groups_d, groups.data(), groups.size() * 8, cudaMemcpyHostToDevice));

@@ -48,11 +48,10 @@ __device__ __forceinline__ uint64_t lower_bound_m(const uint32_t* __restrict__ m
 // len).  a = x[i, k], mp = mpos[i, k], coff = cnt_off[k], loaded by the caller.
 __device__ __forceinline__ uint32_t partner_run(const RareGroups& g, int i, uint32_t a, uint32_t mp, uint64_t coff,
                                                 uint32_t jlo, uint32_t jhi, uint32_t* lo_out) {
-    if (!a) return 0;
-    const uint64_t q = coff + a;
-    const uint64_t g1 = __ldg(g.goff + q + 1);
-    if (g1 - __ldg(g.goff + q) < 2) return 0;  // frequent (no group) or a singleton
-    uint64_t b = (uint64_t)mp + 1, e = g1;
+    if (!a || mp == kNoGroup) return 0;  // missing, or in no rare group: no lookup at all
+    const uint64_t g1 = __ldg(g.goff + coff + a + 1);
+    uint64_t b = (uint64_t)mp + 1, e = g1;  // empty when i is the group's last member
+    if (b >= e) return 0;
     // members after i's own entry are > i; clip to the pass's columns (only a
     // pass that starts after i + 1 or ends before n needs it)
     if (jlo > (uint32_t)i + 1 && b < e && __ldg(g.members + b) < jlo) b = lower_bound_m(g.members, b, e, jlo);
@@ -184,6 +183,49 @@ __device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_
         return;
     }
     uint32_t a = pre[p], b = pre[p + 1], r = run[p];  // this lane's current run
+    if constexpr (T == 768) {
+        // software-pipelined: the member loads of the next 256 items are in
+        // flight while this batch's atomics run (the registers this needs are
+        // there at 768 threads per CTA, 80 per thread)
+        uint32_t jc[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const uint32_t e = e_begin + (uint32_t)(u * 32 + lane);
+            jc[u] = 0;
+            if (e < e_end) {
+                while (e >= b) {
+                    ++p;
+                    a = b;
+                    b = pre[p + 1];
+                    r = run[p];
+                }
+                jc[u] = __ldg(members + r + (e - a));
+            }
+        }
+        for (uint32_t e0 = e_begin; e0 < e_end; e0 += 256) {
+            uint32_t jn[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const uint32_t e = e0 + 256 + (uint32_t)(u * 32 + lane);
+                jn[u] = 0;
+                if (e < e_end) {
+                    while (e >= b) {
+                        ++p;
+                        a = b;
+                        b = pre[p + 1];
+                        r = run[p];
+                    }
+                    jn[u] = __ldg(members + r + (e - a));
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                if (e0 + (uint32_t)(u * 32 + lane) < e_end) count_col(cnt, jc[u] - (uint32_t)wb);
+#pragma unroll
+            for (int u = 0; u < 8; u++) jc[u] = jn[u];
+        }
+        return;
+    }
     for (uint32_t e0 = e_begin; e0 < e_end; e0 += 256) {
         uint32_t idx[8];
 #pragma unroll
@@ -488,6 +530,9 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
         cudaError_t e = cudaFuncSetAttribute(rare_dense_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              rd_smem<1024>(RD_WORDS));
         if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(rare_dense_kernel<768>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     rd_smem<768>(RD_WORDS));
+        if (e == cudaSuccess)
             e = cudaFuncSetAttribute(rare_dense_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      rd_smem<256>(RD_WORDS));
         if (e != cudaSuccess) return e;
@@ -509,9 +554,18 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
         rare_dense_kernel<256><<<std::max(1, rows), 256, rd_smem<256>(cwords), st>>>(g, r0, rows, R, ldr,
                                                                                    r0 + (int)width, cwords);
     } else {
+        static int t768 = -1;
+        if (t768 < 0) {
+            const char* v = getenv("TCH_RARE_T");
+            t768 = (v && atoi(v) == 768) ? 1 : 0;
+        }
         const int grid = std::max(1, std::min(rows, sms));
-        rare_dense_kernel<1024><<<grid, 1024, rd_smem<1024>(cwords), st>>>(g, r0, rows, R, ldr, r0 + (int)width,
+        if (t768)
+            rare_dense_kernel<768><<<grid, 768, rd_smem<768>(cwords), st>>>(g, r0, rows, R, ldr, r0 + (int)width,
                                                                             cwords);
+        else
+            rare_dense_kernel<1024><<<grid, 1024, rd_smem<1024>(cwords), st>>>(g, r0, rows, R, ldr,
+                                                                                r0 + (int)width, cwords);
     }
     return cudaGetLastError();
 }

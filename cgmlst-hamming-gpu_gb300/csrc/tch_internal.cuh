@@ -220,7 +220,7 @@ struct RareGroups {
     const uint64_t* cnt_off = nullptr;  // L + 1: slot of (locus k, rank a) is cnt_off[k] + a
     const uint64_t* goff = nullptr;     // slots + 1: a rare group's rows are members[goff[q] .. goff[q+1])
     const uint32_t* members = nullptr;  // rows of every rare group (count >= 2), ascending per group
-    const uint32_t* mpos = nullptr;     // n x L: index in members of row i's own entry (rare cells only)
+    const uint32_t* mpos = nullptr;     // n x L: index in members of row i's own entry, kNoGroup outside groups
     int n = 0, L = 0;
 };
 
@@ -232,6 +232,8 @@ struct RareGroups {
 constexpr int kRareDenseAlign = 256;
 // Rank of an id that a profile set has never seen (new-profile encoding).
 constexpr uint32_t kNovelRank = 0xFFFFFFFFu;
+// mpos of a cell whose allele is in no rare group (frequent, missing, or seen once).
+constexpr uint32_t kNoGroup = 0xFFFFFFFFu;
 // R[r * ldr + j] = loci where new profile r (ranks xq, m x L u32 in the set's
 // numbering) and row j of the set share an allele that is rare in the set
 // (groups must include single-row groups), for j < n; 0 up to up(n, 256).
