@@ -172,7 +172,7 @@ int prepare_persistent(tch_batch* b, uint16_t* d_out, Err& e) {
             ti.push_back(t);
         }
         TCH_CK(e, rare_batch_prepare(ri, &b->rplan));
-        TCH_CK(e, tc_batch_prepare(ti, &b->tplan, b->dErr));
+        TCH_CK(e, tc_batch_prepare(ti, b->num_sms, &b->tplan, b->dErr));
     }
     return 0;
 fail:
@@ -223,7 +223,7 @@ int build_graph(tch_batch* b, uint16_t* d_out, Err& e) {
         if (prepare_persistent(b, d_out, e)) return 1;
         TCH_CK(e, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         TCH_CK(e, launch_rare_batch(b->rplan, b->num_sms, st));
-        TCH_CK(e, launch_tc_batch(b->tplan, b->num_sms, st));
+        TCH_CK(e, launch_tc_batch(b->tplan, st));
         TCH_CK(e, cudaStreamEndCapture(st, &graph));
         TCH_CK(e, cudaGraphInstantiate(&b->exec, graph, 0));
         cudaGraphDestroy(graph);

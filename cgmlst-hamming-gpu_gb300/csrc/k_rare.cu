@@ -183,49 +183,6 @@ __device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_
         return;
     }
     uint32_t a = pre[p], b = pre[p + 1], r = run[p];  // this lane's current run
-    if constexpr (T == 768) {
-        // software-pipelined: the member loads of the next 256 items are in
-        // flight while this batch's atomics run (the registers this needs are
-        // there at 768 threads per CTA, 80 per thread)
-        uint32_t jc[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-            const uint32_t e = e_begin + (uint32_t)(u * 32 + lane);
-            jc[u] = 0;
-            if (e < e_end) {
-                while (e >= b) {
-                    ++p;
-                    a = b;
-                    b = pre[p + 1];
-                    r = run[p];
-                }
-                jc[u] = __ldg(members + r + (e - a));
-            }
-        }
-        for (uint32_t e0 = e_begin; e0 < e_end; e0 += 256) {
-            uint32_t jn[8];
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const uint32_t e = e0 + 256 + (uint32_t)(u * 32 + lane);
-                jn[u] = 0;
-                if (e < e_end) {
-                    while (e >= b) {
-                        ++p;
-                        a = b;
-                        b = pre[p + 1];
-                        r = run[p];
-                    }
-                    jn[u] = __ldg(members + r + (e - a));
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 8; u++)
-                if (e0 + (uint32_t)(u * 32 + lane) < e_end) count_col(cnt, jc[u] - (uint32_t)wb);
-#pragma unroll
-            for (int u = 0; u < 8; u++) jc[u] = jn[u];
-        }
-        return;
-    }
     for (uint32_t e0 = e_begin; e0 < e_end; e0 += 256) {
         uint32_t idx[8];
 #pragma unroll
@@ -288,6 +245,8 @@ __global__ void __launch_bounds__(T, 1024 / T)
             const CellPair c = load_cells(g, i, k0);
             if (k0 < L) l0 = partner_run(g, i, c.a0, c.m0, g.cnt_off[k0], jlo, jhi, &lo0);
             if (k0 + 1 < L) l1 = partner_run(g, i, c.a1, c.m1, g.cnt_off[k0 + 1], jlo, jhi, &lo1);
+            // a chunk of loci with no partner anywhere in the row skips the scans
+            if (!__syncthreads_or((l0 | l1) != 0u)) continue;
             count_runs<T>(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, cbeg);
         }
         __syncthreads();
@@ -342,6 +301,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
                     if (k0 < L) l0 = partner_run(g, i, c.a0, c.m0, g.cnt_off[k0], jlo, jhi, &lo0);
                     if (k0 + 1 < L) l1 = partner_run(g, i, c.a1, c.m1, g.cnt_off[k0 + 1], jlo, jhi, &lo1);
                 }
+                if (!__syncthreads_or((l0 | l1) != 0u)) continue;  // no partner in this chunk of loci
                 count_runs<T>(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, wb);
             }
             __syncthreads();
@@ -393,6 +353,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
                 uint32_t lo0 = 0, lo1 = 0, l0 = 0, l1 = 0;
                 if (k0 < L) l0 = group_run(g, xq[(size_t)r * L + k0], g.cnt_off[k0], jlo, jhi, &lo0);
                 if (k0 + 1 < L) l1 = group_run(g, xq[(size_t)r * L + k0 + 1], g.cnt_off[k0 + 1], jlo, jhi, &lo1);
+                if (!__syncthreads_or((l0 | l1) != 0u)) continue;  // no partner in this chunk of loci
                 count_runs<T>(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, wb);
             }
             __syncthreads();
@@ -529,9 +490,7 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(rare_dense_kernel<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              rd_smem<1024>(RD_WORDS));
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(rare_dense_kernel<768>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     rd_smem<768>(RD_WORDS));
+
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(rare_dense_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      rd_smem<256>(RD_WORDS));
@@ -554,18 +513,9 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
         rare_dense_kernel<256><<<std::max(1, rows), 256, rd_smem<256>(cwords), st>>>(g, r0, rows, R, ldr,
                                                                                    r0 + (int)width, cwords);
     } else {
-        static int t768 = -1;
-        if (t768 < 0) {
-            const char* v = getenv("TCH_RARE_T");
-            t768 = (v && atoi(v) == 768) ? 1 : 0;
-        }
         const int grid = std::max(1, std::min(rows, sms));
-        if (t768)
-            rare_dense_kernel<768><<<grid, 768, rd_smem<768>(cwords), st>>>(g, r0, rows, R, ldr, r0 + (int)width,
+        rare_dense_kernel<1024><<<grid, 1024, rd_smem<1024>(cwords), st>>>(g, r0, rows, R, ldr, r0 + (int)width,
                                                                             cwords);
-        else
-            rare_dense_kernel<1024><<<grid, 1024, rd_smem<1024>(cwords), st>>>(g, r0, rows, R, ldr,
-                                                                                r0 + (int)width, cwords);
     }
     return cudaGetLastError();
 }

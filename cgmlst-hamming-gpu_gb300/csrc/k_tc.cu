@@ -188,6 +188,7 @@ struct TcParams {
     const TcJob* jobs;
     const CUtensorMap* jmaps;
     const int* tile_job;
+    const int* cta_first;  // MULTI: CTA c runs tiles [cta_first[c], cta_first[c + 1])
 };
 
 // t -> (bi, bj) when the whole triangle is one raster group (a batch job).
@@ -227,6 +228,14 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    // this CTA's tiles: every gridDim.x-th of the stripe's, or (MULTI) one
+    // contiguous range of the batch's, split by work on the host
+    int t_begin = blockIdx.x, t_end = p.num_tiles, t_step = gridDim.x;
+    if (MULTI) {
+        t_begin = __ldg(p.cta_first + blockIdx.x);
+        t_end = __ldg(p.cta_first + blockIdx.x + 1);
+        t_step = 1;
+    }
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
@@ -276,7 +285,7 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
             uint32_t issued_ph[STAGES];
             for (int q = 0; q < STAGES; q++) issued[q] = 0, issued_ph[q] = 0;
             int last_job = -1;  // MULTI: the job whose maps this thread has acquired
-            for (int t = blockIdx.x; ok && t < p.num_tiles; t += gridDim.x) {
+            for (int t = t_begin; ok && t < t_end; t += t_step) {
                 int bi, bj, y_a, y_b, kblocks;
                 const CUtensorMap* ma = maps.a;
                 const CUtensorMap* mb = maps.b;
@@ -341,7 +350,7 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
             int s = 0, acc = 0;
             uint32_t ph = 0, aph = 0;
             bool ok = true;
-            for (int t = blockIdx.x; ok && t < p.num_tiles; t += gridDim.x) {
+            for (int t = t_begin; ok && t < t_end; t += t_step) {
                 const int kblocks = MULTI ? p.jobs[__ldg(p.tile_job + t)].kblocks : p.kblocks;
                 if (!mbar_wait(&tempty[acc], aph ^ 1, abort_flag, p.err)) { ok = false; break; }
                 tc_fence_after();
@@ -374,7 +383,7 @@ __global__ void __launch_bounds__(THREADS, 1) tc_stripe_kernel(const __grid_cons
         int acc = 0;
         uint32_t aph = 0;
         int bad = 0;
-        for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x) {
+        for (int t = t_begin; t < t_end; t += t_step) {
             int bi, bj;
             int n = p.n, r0 = p.r0, c0 = p.c0, iend = p.r0 + p.rows, vec_store = p.vec_store;
             const uint16_t* rdense = p.rdense;
@@ -566,7 +575,7 @@ cudaError_t launch_one(const Fp4Operands& A, const Fp4Operands& B, const uint16_
 
 }  // namespace
 
-cudaError_t tc_batch_prepare(const std::vector<TcBatchItem>& items, TcBatchPlan* plan, int* err) {
+cudaError_t tc_batch_prepare(const std::vector<TcBatchItem>& items, int num_sms, TcBatchPlan* plan, int* err) {
     std::vector<TcJob> jobs;
     std::vector<CUtensorMap> mh;
     std::vector<int> tile_job;
@@ -618,6 +627,25 @@ cudaError_t tc_batch_prepare(const std::vector<TcBatchItem>& items, TcBatchPlan*
     plan->njobs = (int)jobs.size();
     plan->num_tiles = tile0;
     if (jobs.empty()) return cudaSuccess;
+    // one contiguous range of tiles per CTA, equal in work: a tile costs its
+    // K stages plus a fixed share for its epilogue; a CTA then changes set a
+    // few times only, and its consecutive tiles share a column block
+    plan->grid = std::max(1, std::min(tile0, num_sms));
+    {
+        std::vector<long long> cost(tile0 + 1, 0);
+        for (int t = 0; t < tile0; t++) cost[t + 1] = cost[t] + jobs[tile_job[t]].kblocks + 2;
+        const long long total = cost[tile0];
+        int t = 0;
+        for (int c = 0; c <= plan->grid; c++) {
+            const long long target = total * c / plan->grid;
+            while (t < tile0 && cost[t] < target) t++;
+            // at least one tile per CTA (grid <= tiles): first[c] > first[c - 1], and
+            // room for one tile for each CTA after c
+            int f = c == plan->grid ? tile0 : t;
+            if (c > 0 && c < plan->grid) f = std::min(std::max(f, tile_job.back() + 1), tile0 - plan->grid + c);
+            tile_job.push_back(f);
+        }
+    }
     cudaError_t e = cudaMalloc(&plan->d_jobs, jobs.size() * sizeof(TcJob));
     if (e == cudaSuccess) e = cudaMalloc(&plan->d_maps, mh.size() * sizeof(CUtensorMap));
     if (e == cudaSuccess) e = cudaMalloc(&plan->d_tile_job, tile_job.size() * sizeof(int));
@@ -636,7 +664,7 @@ cudaError_t tc_batch_prepare(const std::vector<TcBatchItem>& items, TcBatchPlan*
     return cudaSuccess;
 }
 
-cudaError_t launch_tc_batch(const TcBatchPlan& plan, int num_sms, cudaStream_t st) {
+cudaError_t launch_tc_batch(const TcBatchPlan& plan, cudaStream_t st) {
     if (plan.num_tiles == 0 || plan.njobs == 0) return cudaSuccess;
     TcMaps maps;  // the batch's maps are in device memory
     maps.n = 0;
@@ -647,12 +675,13 @@ cudaError_t launch_tc_batch(const TcBatchPlan& plan, int num_sms, cudaStream_t s
     p.jobs = static_cast<const TcJob*>(plan.d_jobs);
     p.jmaps = static_cast<const CUtensorMap*>(plan.d_maps);
     p.tile_job = static_cast<const int*>(plan.d_tile_job);
-    const int grid = std::min(plan.num_tiles, std::max(num_sms, 1));
-    tc_stripe_kernel<true><<<grid, THREADS, SMEM_BYTES, st>>>(maps, p);
+    p.cta_first = p.tile_job + plan.num_tiles;
+    tc_stripe_kernel<true><<<plan.grid, THREADS, SMEM_BYTES, st>>>(maps, p);
     return cudaGetLastError();
 }
 
 void tc_batch_release(TcBatchPlan* plan) {
+    plan->grid = 0;
     if (plan->d_jobs) cudaFree(plan->d_jobs);
     if (plan->d_maps) cudaFree(plan->d_maps);
     if (plan->d_tile_job) cudaFree(plan->d_tile_job);

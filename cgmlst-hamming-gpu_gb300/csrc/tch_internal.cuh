@@ -193,12 +193,13 @@ struct TcBatchItem {
 struct TcBatchPlan {
     void* d_jobs = nullptr;
     void* d_maps = nullptr;
-    void* d_tile_job = nullptr;
+    void* d_tile_job = nullptr;  // the job of every tile, then the grid + 1 CTA range starts
     int njobs = 0, num_tiles = 0;
+    int grid = 0;  // CTAs of the launch (at most num_sms), each with one contiguous range of tiles
     int* err = nullptr;
 };
-cudaError_t tc_batch_prepare(const std::vector<TcBatchItem>& items, TcBatchPlan* plan, int* err);
-cudaError_t launch_tc_batch(const TcBatchPlan& plan, int num_sms, cudaStream_t st);
+cudaError_t tc_batch_prepare(const std::vector<TcBatchItem>& items, int num_sms, TcBatchPlan* plan, int* err);
+cudaError_t launch_tc_batch(const TcBatchPlan& plan, cudaStream_t st);
 void tc_batch_release(TcBatchPlan* plan);
 
 // ---- k_encode.cu ------------------------------------------------------------------
