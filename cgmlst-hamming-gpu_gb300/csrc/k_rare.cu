@@ -246,7 +246,6 @@ __global__ void __launch_bounds__(T, 1024 / T)
             if (k0 < L) l0 = partner_run(g, i, c.a0, c.m0, g.cnt_off[k0], jlo, jhi, &lo0);
             if (k0 + 1 < L) l1 = partner_run(g, i, c.a1, c.m1, g.cnt_off[k0 + 1], jlo, jhi, &lo1);
             // a chunk of loci with no partner anywhere in the row skips the scans
-            if (!__syncthreads_or((l0 | l1) != 0u)) continue;
             count_runs<T>(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, cbeg);
         }
         __syncthreads();
@@ -301,7 +300,6 @@ __global__ void __launch_bounds__(T, 1024 / T)
                     if (k0 < L) l0 = partner_run(g, i, c.a0, c.m0, g.cnt_off[k0], jlo, jhi, &lo0);
                     if (k0 + 1 < L) l1 = partner_run(g, i, c.a1, c.m1, g.cnt_off[k0 + 1], jlo, jhi, &lo1);
                 }
-                if (!__syncthreads_or((l0 | l1) != 0u)) continue;  // no partner in this chunk of loci
                 count_runs<T>(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, wb);
             }
             __syncthreads();
@@ -353,7 +351,6 @@ __global__ void __launch_bounds__(T, 1024 / T)
                 uint32_t lo0 = 0, lo1 = 0, l0 = 0, l1 = 0;
                 if (k0 < L) l0 = group_run(g, xq[(size_t)r * L + k0], g.cnt_off[k0], jlo, jhi, &lo0);
                 if (k0 + 1 < L) l1 = group_run(g, xq[(size_t)r * L + k0 + 1], g.cnt_off[k0 + 1], jlo, jhi, &lo1);
-                if (!__syncthreads_or((l0 | l1) != 0u)) continue;  // no partner in this chunk of loci
                 count_runs<T>(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, wb);
             }
             __syncthreads();

@@ -193,9 +193,9 @@ struct TcBatchItem {
 struct TcBatchPlan {
     void* d_jobs = nullptr;
     void* d_maps = nullptr;
-    void* d_tile_job = nullptr;  // the job of every tile, then the grid + 1 CTA range starts
+    void* d_tile_job = nullptr;  // the job of every tile
     int njobs = 0, num_tiles = 0;
-    int grid = 0;  // CTAs of the launch (at most num_sms), each with one contiguous range of tiles
+    int grid = 0;  // CTAs of the launch (at most num_sms), each on every grid-th tile
     int* err = nullptr;
 };
 cudaError_t tc_batch_prepare(const std::vector<TcBatchItem>& items, int num_sms, TcBatchPlan* plan, int* err);
