@@ -245,6 +245,53 @@ __global__ void group_sort_kernel(const uint64_t* __restrict__ groups, const uin
     }
 }
 
+// Partner runs of every row (one warp per row, loci in order): the members
+// after the row's own entry in each of its rare groups, when there are any.
+// Pass 0 writes each row's run count; pass 1 the runs' first members, their
+// exclusive item prefix within the row, and the row's item total.
+__global__ void row_runs_kernel(const uint16_t* __restrict__ x, int n, int L, const uint64_t* __restrict__ cnt_off,
+                                const uint64_t* __restrict__ goff, const uint32_t* __restrict__ mpos, int pass,
+                                uint32_t* count, const uint64_t* __restrict__ roff, uint32_t* rlo, uint32_t* rpre,
+                                uint32_t* rtot) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (int)(gridDim.x * blockDim.x / 32);
+    for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32); i < n; i += warps) {
+        uint32_t nrun = 0, items = 0;
+        const uint64_t base = pass ? roff[i] : 0;
+        for (int k0 = 0; k0 < L; k0 += 32) {
+            const int k = k0 + lane;
+            uint32_t lo = 0, len = 0;
+            if (k < L) {
+                const uint32_t mp = mpos[(size_t)i * L + k];
+                if (mp != kNoGroup) {
+                    const uint64_t g1 = goff[cnt_off[k] + x[(size_t)i * L + k] + 1];
+                    if ((uint64_t)mp + 1 < g1) lo = mp + 1, len = (uint32_t)(g1 - mp - 1);
+                }
+            }
+            const unsigned has = __ballot_sync(0xFFFFFFFFu, len > 0);
+            if (pass) {
+                uint32_t inc = len;  // inclusive warp scan of the run lengths
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, d);
+                    if (lane >= d) inc += t;
+                }
+                if (len) {
+                    const uint64_t q = base + nrun + __popc(has & ((1u << lane) - 1u));
+                    rlo[q] = lo;
+                    rpre[q] = items + inc - len;
+                }
+                items += __shfl_sync(0xFFFFFFFFu, inc, 31);
+            }
+            nrun += __popc(has);
+        }
+        if (lane == 0) {
+            if (pass) rtot[i] = items;
+            else count[i] = nrun;
+        }
+    }
+}
+
 __device__ __forceinline__ uint64_t lower_bound_rows(const uint32_t* __restrict__ a, uint64_t lo, uint64_t hi,
                                                      uint32_t key) {
     while (lo < hi) {
@@ -389,8 +436,8 @@ std::vector<TauRow> tau_rows(const std::vector<uint32_t>& cnt_flat, const std::v
             }
         }
         w.kb = (double)fp4_columns(L, w.d);  // K: MACs per pair; the two operand copies take K bytes per row
-        if (dense) {  // ranks, own positions, group members (a stripe's counts come later)
-            w.mem = (double)rows * w.kb + nl * 6.0 + 4.0 * w.cells;
+        if (dense) {  // ranks, own positions, group members, row runs (a stripe's counts come later)
+            w.mem = (double)rows * w.kb + nl * 6.0 + 12.0 * w.cells + 12.0 * n;
             w.t = pairs * w.kb / m.gemm_rate + w.r / m.dense_rate;
             w.fits = w.mem <= (double)free_bytes && w.cells < 4.0e9;
         } else {
@@ -723,6 +770,28 @@ int encode_on_device(int device, int n, int L, const uint64_t* d_calls, int tau_
         }
 
         mark("rare groups");
+        if (dense_rare && !query_maps && n > 1) {  // the partner runs of every row, for triangle solves
+            TCH_CK(e, dalloc(&row_count, (size_t)n, &tmp_bytes));
+            const int rgrid = (int)std::min<size_t>(((size_t)n + 7) / 8, (size_t)sms * 16);
+            row_runs_kernel<<<rgrid, 256>>>(out->x, n, L, cnt_off_d, goff_d, mpos, 0, row_count, nullptr, nullptr,
+                                            nullptr, nullptr);
+            TCH_CK(e, cudaGetLastError());
+            std::vector<uint32_t> rc_h((size_t)n);
+            TCH_CK(e, cudaMemcpy(rc_h.data(), row_count, (size_t)n * 4, cudaMemcpyDeviceToHost));
+            std::vector<uint64_t> roff_h((size_t)n + 1);
+            uint64_t acc = 0;
+            for (int i = 0; i < n; i++) roff_h[i] = acc, acc += rc_h[i];
+            roff_h[n] = acc;
+            TCH_CK(e, dalloc(&out->roff, (size_t)n + 1, &out->bytes));
+            TCH_CK(e, dalloc(&out->rlo, std::max<uint64_t>(acc, 1), &out->bytes));
+            TCH_CK(e, dalloc(&out->rpre, std::max<uint64_t>(acc, 1), &out->bytes));
+            TCH_CK(e, dalloc(&out->rtot, (size_t)n, &out->bytes));
+            TCH_CK(e, cudaMemcpy(out->roff, roff_h.data(), ((size_t)n + 1) * 8, cudaMemcpyHostToDevice));
+            row_runs_kernel<<<rgrid, 256>>>(out->x, n, L, cnt_off_d, goff_d, mpos, 1, nullptr, out->roff, out->rlo,
+                                            out->rpre, out->rtot);
+            TCH_CK(e, cudaGetLastError());
+            mark("row runs");
+        }
         if (dense_rare) {  // the groups themselves are the rare term; no pair list
             TCH_CK(e, cudaDeviceSynchronize());
             out->dense = true;
@@ -809,6 +878,12 @@ void free_device_encoding(DeviceEncoding* d) {
     cudaFree(d->goff);
     cudaFree(d->members);
     cudaFree(d->mpos);
+    cudaFree(d->roff);
+    cudaFree(d->rlo);
+    cudaFree(d->rpre);
+    cudaFree(d->rtot);
+    d->roff = nullptr;
+    d->rlo = d->rpre = d->rtot = nullptr;
     cudaFree(d->slot_ids);
     cudaFree(d->col);
     cudaFree(d->base);

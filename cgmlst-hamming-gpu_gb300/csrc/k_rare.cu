@@ -87,55 +87,16 @@ __device__ __forceinline__ void count_col(uint32_t* cnt, uint32_t c) {
     atomicAdd(cnt + (c >> 1), 1u << ((c & 1u) * 16u));
 }
 
-// Lays this thread's two runs (l0 partners from members[lo0], l1 from
-// members[lo1]) end to end with every other thread's non-empty runs (a block
-// scan of item and run counts compacts them), cuts the items into one equal
-// part per warp, and counts every partner j at column j - wb.  A part of long
-// runs (kWalkMin items or more on average) is walked run by run, the lanes on
-// consecutive members; otherwise 256 items at a time, lane l on items
-// e + l + 32 u, several short runs in one pass, each lane keeping its current
-// run (start, end, first member) in registers.  Called by all threads of the
-// CTA (it synchronises them).
-template <int T>
-__device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_t* run, uint32_t* wsum, uint32_t l0,
-                                           uint32_t lo0, uint32_t l1, uint32_t lo1,
-                                           const uint32_t* __restrict__ members, int wb) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr int NWARPS = T / 32;
-    __shared__ uint32_t tot[2];  // items, runs
-    const uint32_t mi = l0 + l1, mc = (l0 ? 1u : 0u) + (l1 ? 1u : 0u);
-    uint32_t ii = mi, ic = mc;  // inclusive warp scans of items and runs
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t ti = __shfl_up_sync(FULL, ii, d), tc = __shfl_up_sync(FULL, ic, d);
-        if (lane >= d) ii += ti, ic += tc;
-    }
-    if (lane == 31) wsum[warp] = ii, wsum[32 + warp] = ic;
-    __syncthreads();  // also orders the counter zeroing and the previous chunk's readers
-    if (warp == 0) {
-        const uint32_t vi = lane < NWARPS ? wsum[lane] : 0u, vc = lane < NWARPS ? wsum[32 + lane] : 0u;
-        uint32_t xi = vi, xc = vc;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t ti = __shfl_up_sync(FULL, xi, d), tc = __shfl_up_sync(FULL, xc, d);
-            if (lane >= d) xi += ti, xc += tc;
-        }
-        if (lane < NWARPS) wsum[lane] = xi - vi, wsum[32 + lane] = xc - vc;
-        if (lane == 31) tot[0] = xi, tot[1] = xc;
-    }
-    __syncthreads();
-    {
-        const uint32_t ei = wsum[warp] + ii - mi;        // items before this thread's runs
-        uint32_t q = wsum[32 + warp] + ic - mc;          // their places among the non-empty runs
-        if (l0) pre[q] = ei, run[q] = lo0, q++;
-        if (l1) pre[q] = ei + l0, run[q] = lo1;
-        if (tid == 0) pre[tot[1]] = tot[0];
-    }
-    __syncthreads();
-    const uint32_t total = tot[0];
-    const int nr = (int)tot[1];
-    const uint32_t part = (total + NWARPS - 1) / NWARPS;
-    const uint32_t e_begin = min(total, (uint32_t)warp * part), e_end = min(total, e_begin + part);
+// Items [e_begin, e_end) of runs laid end to end (run q: items pre[q] ..
+// pre[q + 1] - 1, members run[q] ..; pre[nr] bounds the last one), counted at
+// column j - wb by one warp.  A part of long runs (kWalkMin items or more on
+// average) is walked run by run, the lanes on consecutive members; otherwise
+// 256 items at a time, lane l on items e + l + 32 u, several short runs in one
+// pass, each lane keeping its current run (start, end, first member) in
+// registers.
+__device__ __forceinline__ void walk_part(uint32_t* cnt, const uint32_t* pre, const uint32_t* run, int nr,
+                                          uint32_t e_begin, uint32_t e_end, const uint32_t* __restrict__ members,
+                                          int wb, int lane) {
     if (e_begin >= e_end) return;
     int p = 0;  // the run holding e_begin: the last p with pre[p] <= e_begin
     {
@@ -208,6 +169,82 @@ __device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_
     }
 }
 
+// Lays this thread's two runs (l0 partners from members[lo0], l1 from
+// members[lo1]) end to end with every other thread's non-empty runs (a block
+// scan of item and run counts compacts them), cuts the items into one equal
+// part per warp, and counts every partner j at column j - wb (walk_part).
+// Called by all threads of the CTA (it synchronises them).
+template <int T>
+__device__ __forceinline__ void count_runs(uint32_t* cnt, uint32_t* pre, uint32_t* run, uint32_t* wsum, uint32_t l0,
+                                           uint32_t lo0, uint32_t l1, uint32_t lo1,
+                                           const uint32_t* __restrict__ members, int wb) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NWARPS = T / 32;
+    __shared__ uint32_t tot[2];  // items, runs
+    const uint32_t mi = l0 + l1, mc = (l0 ? 1u : 0u) + (l1 ? 1u : 0u);
+    uint32_t ii = mi, ic = mc;  // inclusive warp scans of items and runs
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t ti = __shfl_up_sync(FULL, ii, d), tc = __shfl_up_sync(FULL, ic, d);
+        if (lane >= d) ii += ti, ic += tc;
+    }
+    if (lane == 31) wsum[warp] = ii, wsum[32 + warp] = ic;
+    __syncthreads();  // also orders the counter zeroing and the previous chunk's readers
+    if (warp == 0) {
+        const uint32_t vi = lane < NWARPS ? wsum[lane] : 0u, vc = lane < NWARPS ? wsum[32 + lane] : 0u;
+        uint32_t xi = vi, xc = vc;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t ti = __shfl_up_sync(FULL, xi, d), tc = __shfl_up_sync(FULL, xc, d);
+            if (lane >= d) xi += ti, xc += tc;
+        }
+        if (lane < NWARPS) wsum[lane] = xi - vi, wsum[32 + lane] = xc - vc;
+        if (lane == 31) tot[0] = xi, tot[1] = xc;
+    }
+    __syncthreads();
+    {
+        const uint32_t ei = wsum[warp] + ii - mi;        // items before this thread's runs
+        uint32_t q = wsum[32 + warp] + ic - mc;          // their places among the non-empty runs
+        if (l0) pre[q] = ei, run[q] = lo0, q++;
+        if (l1) pre[q] = ei + l0, run[q] = lo1;
+        if (tid == 0) pre[tot[1]] = tot[0];
+    }
+    __syncthreads();
+    const uint32_t total = tot[0];
+    const uint32_t part = (total + NWARPS - 1) / NWARPS;
+    const uint32_t e_begin = min(total, (uint32_t)warp * part), e_end = min(total, e_begin + part);
+    walk_part(cnt, pre, run, (int)tot[1], e_begin, e_end, members, wb, lane);
+}
+
+// Row i's partners from its precomputed runs (RareGroups::roff ..), counted
+// at column j - wb: up to 2T runs at a time are copied into pre / run
+// (coalesced), their items cut into one equal part per warp and walked.  The
+// row's partners must all lie in this pass's columns.  Called by all threads
+// of the CTA after the counters are zeroed (it synchronises them).
+template <int T>
+__device__ __forceinline__ void count_row_runs(uint32_t* cnt, uint32_t* pre, uint32_t* run, const RareGroups& g, int i,
+                                               int wb) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NWARPS = T / 32;
+    const uint64_t q0 = g.roff[i];
+    const uint32_t nrun = (uint32_t)(g.roff[i + 1] - q0);
+    for (uint32_t c0 = 0; c0 < nrun; c0 += 2 * T) {
+        const uint32_t cn = min(2u * T, nrun - c0);
+        __syncthreads();  // the zeroing, or the previous group of runs' readers
+        for (uint32_t t = tid; t < cn; t += T) {
+            pre[t] = __ldg(g.rpre + q0 + c0 + t);
+            run[t] = __ldg(g.rlo + q0 + c0 + t);
+        }
+        if (tid == 0) pre[cn] = c0 + cn < nrun ? __ldg(g.rpre + q0 + c0 + cn) : __ldg(g.rtot + i);
+        __syncthreads();
+        const uint32_t base = pre[0], total = pre[cn] - base;
+        const uint32_t part = (total + NWARPS - 1) / NWARPS;
+        const uint32_t e_begin = base + min(total, (uint32_t)warp * part);
+        const uint32_t e_end = base + min(total, (uint32_t)warp * part + part);
+        walk_part(cnt, pre, run, (int)cn, e_begin, e_end, g.members, wb, lane);
+    }
+}
+
 // Many sets' whole triangles in one launch (batched solves): the rows of
 // every job laid end to end (row_job: the job of every row), one CTA per row
 // as in rare_dense_kernel, each row counted in one pass (the launcher checks
@@ -239,14 +276,17 @@ __global__ void __launch_bounds__(T, 1024 / T)
         const int nq = (jb.cend - cbeg) >> 3;
         for (int w = tid; w < nq; w += T) smem_rd[w] = make_uint4(0, 0, 0, 0);
         const uint32_t jlo = (uint32_t)(i + 1), jhi = (uint32_t)n;
-        for (int kc = 0; jlo < jhi && kc < L; kc += (2 * T)) {
-            const int k0 = kc + 2 * tid;
-            uint32_t lo0 = 0, lo1 = 0, l0 = 0, l1 = 0;
-            const CellPair c = load_cells(g, i, k0);
-            if (k0 < L) l0 = partner_run(g, i, c.a0, c.m0, g.cnt_off[k0], jlo, jhi, &lo0);
-            if (k0 + 1 < L) l1 = partner_run(g, i, c.a1, c.m1, g.cnt_off[k0 + 1], jlo, jhi, &lo1);
-            // a chunk of loci with no partner anywhere in the row skips the scans
-            count_runs<T>(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, cbeg);
+        if (g.roff) {  // the row's precomputed runs
+            count_row_runs<T>(cnt, pre, run, g, i, cbeg);
+        } else {
+            for (int kc = 0; jlo < jhi && kc < L; kc += (2 * T)) {
+                const int k0 = kc + 2 * tid;
+                uint32_t lo0 = 0, lo1 = 0, l0 = 0, l1 = 0;
+                const CellPair c = load_cells(g, i, k0);
+                if (k0 < L) l0 = partner_run(g, i, c.a0, c.m0, g.cnt_off[k0], jlo, jhi, &lo0);
+                if (k0 + 1 < L) l1 = partner_run(g, i, c.a1, c.m1, g.cnt_off[k0 + 1], jlo, jhi, &lo1);
+                count_runs<T>(cnt, pre, run, wsum, l0, lo0, l1, lo1, g.members, cbeg);
+            }
         }
         __syncthreads();
         uint4* dst = reinterpret_cast<uint4*>(jb.R + (size_t)i * jb.ldr + (size_t)cbeg);
@@ -269,7 +309,10 @@ __global__ void __launch_bounds__(T, 1024 / T)
     // with every locus in one scan (L <= 2T) a thread keeps the same two
     // loci for all rows: their count offsets stay in registers and the next
     // row's ranks and positions are fetched while this row is counted
-    const bool one_chunk = L <= (2 * T);
+    // the rows' precomputed runs, when there are any and every row's partners
+    // fit one counter pass; otherwise the runs are found per locus
+    const bool row_runs = g.roff != nullptr && cend - r0 <= 2 * cwords;
+    const bool one_chunk = !row_runs && L <= (2 * T);
     uint64_t co0 = 0, co1 = 0;
     if (one_chunk) {
         if (2 * tid < L) co0 = g.cnt_off[2 * tid];
@@ -288,7 +331,8 @@ __global__ void __launch_bounds__(T, 1024 / T)
             const int nq = (we - wb) >> 3;  // uint4 of counters (8 columns each); we - wb is a multiple of 256
             for (int w = tid; w < nq; w += T) smem_rd[w] = make_uint4(0, 0, 0, 0);
             const uint32_t jlo = (uint32_t)max(wb, i + 1), jhi = (uint32_t)min(we, n);
-            for (int kc = 0; jlo < jhi && kc < L; kc += (2 * T)) {
+            if (row_runs) count_row_runs<T>(cnt, pre, run, g, i, wb);
+            for (int kc = 0; !row_runs && jlo < jhi && kc < L; kc += (2 * T)) {
                 // this thread's two loci, then a block-wide exclusive scan of the run lengths
                 const int k0 = kc + 2 * tid;
                 uint32_t lo0 = 0, lo1 = 0, l0 = 0, l1 = 0;

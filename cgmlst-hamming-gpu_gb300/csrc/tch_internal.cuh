@@ -223,6 +223,14 @@ struct RareGroups {
     const uint32_t* members = nullptr;  // rows of every rare group (count >= 2), ascending per group
     const uint32_t* mpos = nullptr;     // n x L: index in members of row i's own entry, kNoGroup outside groups
     int n = 0, L = 0;
+    // Row runs (optional; null: found per locus from the arrays above): row i's
+    // partners are runs roff[i] .. roff[i + 1] - 1, in locus order; run q is
+    // members[rlo[q] ..) and its items start at rpre[q] within the row (an
+    // exclusive prefix), the row's last run ending at rtot[i].
+    const uint64_t* roff = nullptr;
+    const uint32_t* rlo = nullptr;
+    const uint32_t* rpre = nullptr;
+    const uint32_t* rtot = nullptr;
 };
 
 // R[(i - r0) * ldr + (j - r0)] = number of loci where rows i and j share a
@@ -283,6 +291,11 @@ struct DeviceEncoding {
     uint64_t* goff = nullptr;
     uint32_t* members = nullptr;
     uint32_t* mpos = nullptr;
+    // every row's partner runs (RareGroups::roff ..), built for triangle solves
+    uint64_t* roff = nullptr;
+    uint32_t* rlo = nullptr;
+    uint32_t* rpre = nullptr;
+    uint32_t* rtot = nullptr;
     // query maps (ENC_QUERY): ids in rank order per locus (slot cnt_off[k] + rank,
     // ascending), frequent column of each slot (-1 = rare), per-locus column base
     uint64_t* slot_ids = nullptr;

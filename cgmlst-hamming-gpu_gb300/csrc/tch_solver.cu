@@ -150,6 +150,10 @@ struct tch_solver {
     uint64_t* ggoff = nullptr;
     uint32_t* gmembers = nullptr;
     uint32_t* gmpos = nullptr;
+    uint64_t* groff = nullptr;       // every row's partner runs
+    uint32_t* grlo = nullptr;
+    uint32_t* grpre = nullptr;
+    uint32_t* grtot = nullptr;
     int gL = 0;                      // loci of the rank rows (>= 1)
     int sub_rows = 0;                // rows per rare-count + tile-pass pair inside a stripe (0 = whole)
     int tile_group = 0;              // row blocks per raster group of the tile pass (0 = default)
@@ -182,6 +186,10 @@ void solver_free(tch_solver* s) {
     cudaFree(s->ggoff);
     cudaFree(s->gmembers);
     cudaFree(s->gmpos);
+    cudaFree(s->groff);
+    cudaFree(s->grlo);
+    cudaFree(s->grpre);
+    cudaFree(s->grtot);
     if (s->dense) {  // hand the pool's idle stripe blocks back
         cudaMemPool_t pool;
         if (stripe_pool(s->device, &pool) == cudaSuccess) {
@@ -380,6 +388,12 @@ static int solver_from_input(int device, int n, int L, const uint64_t* calls, co
         s->ggoff = enc.goff;
         s->gmembers = enc.members;
         s->gmpos = enc.mpos;
+        s->groff = enc.roff;
+        s->grlo = enc.rlo;
+        s->grpre = enc.rpre;
+        s->grtot = enc.rtot;
+        enc.roff = nullptr;
+        enc.rlo = enc.rpre = enc.rtot = nullptr;
     } else {
         cudaFree(enc.x);
         enc.bytes -= (size_t)n * Le * 2;
@@ -422,6 +436,10 @@ static RareGroups rare_groups(const tch_solver* s) {
     g.goff = s->ggoff;
     g.members = s->gmembers;
     g.mpos = s->gmpos;
+    g.roff = s->groff;
+    g.rlo = s->grlo;
+    g.rpre = s->grpre;
+    g.rtot = s->grtot;
     g.n = s->n;
     g.L = s->gL;
     return g;
