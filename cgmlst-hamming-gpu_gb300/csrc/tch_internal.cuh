@@ -318,7 +318,9 @@ struct TauTable {
     std::vector<double> est_s;  // analytic estimate per candidate
 };
 // Schedule values the candidates take.
-constexpr int kSchedSubs[3] = {0, 8192, 2048};
+// Sub-stripes of 2 048 rows were the fastest schedule for 1 of 384 training
+// profile sets of the GB300 sweep (and at most 2 % faster there): not offered.
+constexpr int kSchedSubs[2] = {0, 8192};
 constexpr int kSchedGroups[3] = {4, 8, 16};
 
 // With table != nullptr the encoder stops after the counts and fills it.

@@ -2,6 +2,7 @@
 
     python -m tau_learn sweep  [--datasets 200] [--out tau_sweep_gb300.npz]
     python -m tau_learn train  [--sweep tau_sweep_gb300.npz] [--out tau_mlp_gb300.f32]
+    python -m tau_learn cv     [--sweep tau_sweep_gb300.npz] [--out tau_cv_gb300.json]
 
 (run from this directory, or ``python cgmlst-hamming-gpu_gb300/tau_learn.py``).
 
@@ -22,6 +23,10 @@ standardisation is folded into the first layer, so the saved model takes the
 raw feature rows.  The report compares, on the held-out sets, the measured time
 at the learned pick (tau and schedule), at the analytic pick (its tau, the
 default schedule) and at the best swept candidate.
+
+cv: the same recipe five times, each fifth of the sets held out once: the
+learned picks of all 480 sets against the analytic picks (a single fifth's
+total is decided by its two or three longest sets).
 """
 from __future__ import annotations
 
@@ -41,6 +46,7 @@ synth = importlib.import_module("cgmlst-hamming-gpu_gb300.synth")
 
 SWEEP_PATH = os.path.join(HERE, "tau_sweep_gb300.npz")
 REPORT_PATH = os.path.join(HERE, "tau_mlp_gb300.json")
+CV_PATH = os.path.join(HERE, "tau_cv_gb300.json")
 LOCI = (500, 1142, 1343, 2000, 2794, 3016)
 
 
@@ -161,6 +167,17 @@ def sweep(n_datasets: int, out: str, span: int = 4, device: int = 0, first: int 
              params=json.dumps(params))
 
 
+# Sub-stripe rows of the schedules tch_tau_features offers (a sweep taken
+# when more were offered keeps those rows; they are left out here).
+SCHED_SUBS = (0, 8192)
+
+
+def offered(data: dict) -> dict:
+    """The sweep's rows whose schedule the library still offers."""
+    keep = np.isin(data["sub"], SCHED_SUBS)
+    return {k: (v[keep] if isinstance(v, np.ndarray) and v.shape[:1] == keep.shape else v) for k, v in data.items()}
+
+
 def holdout_mask(ds: np.ndarray) -> np.ndarray:
     return ds % 5 == 4
 
@@ -178,16 +195,20 @@ def fold_standardisation(w: np.ndarray, mu: np.ndarray, sd: np.ndarray) -> np.nd
     return w.astype(np.float32)
 
 
-def evaluate(w: np.ndarray, data, device: int = 0) -> dict:
-    """Per held-out set: measured ms at the solver's pick with the model set
-    (the learned candidate: tau and schedule), at the analytic pick (its tau
-    with the default schedule) and at the best swept candidate."""
+def evaluate(w: np.ndarray, data, device: int = 0, mask=None) -> dict:
+    """Per held-out set (mask: rows of the sets to evaluate; default the
+    held-out fifth): measured ms at the solver's pick with the model set (the
+    learned candidate: tau and schedule), at the analytic pick (its tau with
+    the default schedule) and at the best swept candidate."""
+    data = offered(data)
     ds, tau, X, est, ms = data["ds"], data["tau"], data["feats"], data["est"], data["ms"]
     sub, grp = data["sub"], data["group"]
+    if mask is None:
+        mask = holdout_mask(ds)
     pred = tch.mlp_predict(w, X, device)
     default = (sub == 0) & (grp == DEFAULT_GROUP)
     out = []
-    for d in np.unique(ds[holdout_mask(ds)]):
+    for d in np.unique(ds[mask]):
         m = ds == d
         i_l = np.argmin(np.where(m, pred, np.inf))
         i_a = np.argmin(np.where(m & default, est, np.inf))
@@ -196,6 +217,10 @@ def evaluate(w: np.ndarray, data, device: int = 0) -> dict:
                         tau_analytic=int(tau[i_a]), tau_best=int(tau[i_b]), sub_best=int(sub[i_b]),
                         group_best=int(grp[i_b]), ms_learned=float(ms[i_l]), ms_analytic=float(ms[i_a]),
                         ms_best=float(ms[i_b])))
+    return summarise(out)
+
+
+def summarise(out: list) -> dict:
     tl = sum(r["ms_learned"] for r in out)
     ta = sum(r["ms_analytic"] for r in out)
     tb = sum(r["ms_best"] for r in out)
@@ -217,10 +242,10 @@ def oversample(ds: np.ndarray, ms: np.ndarray, idx: np.ndarray) -> np.ndarray:
     return np.repeat(idx, reps)
 
 
-def train(sweep_path: str, out: str, steps: int = 6000, lr: float = 3e-3, seed: int = 7, device: int = 0) -> dict:
-    data = dict(np.load(sweep_path))
+def fit(data: dict, tr: np.ndarray, steps: int, lr: float, seed: int, device: int):
+    """The model trained on the rows of the sets in tr (standardisation folded
+    into the first layer); returns (weights, final loss, rows used)."""
     ds = data["ds"]
-    tr = ~holdout_mask(ds)
     X = data["feats"].astype(np.float64)
     y = np.log(data["ms"]).astype(np.float32)
     mu = X[tr].mean(0)
@@ -229,21 +254,48 @@ def train(sweep_path: str, out: str, steps: int = 6000, lr: float = 3e-3, seed: 
     Xn = ((X - mu) / sd).astype(np.float32)
     idx = oversample(ds, data["ms"], np.nonzero(tr)[0])
     w = tch.mlp_init(seed)
+    w, _ = tch.mlp_train(w, Xn[idx], y[idx], steps // 2, lr, device)
+    w, loss = tch.mlp_train(w, Xn[idx], y[idx], steps - steps // 2, lr / 5, device)
+    return fold_standardisation(w, mu, sd), loss, int(len(idx))
+
+
+def train(sweep_path: str, out: str, steps: int = 6000, lr: float = 3e-3, seed: int = 7, device: int = 0) -> dict:
+    """The shipped model: trained on four fifths of the sets, evaluated on the
+    held-out fifth."""
+    data = offered(dict(np.load(sweep_path)))
+    ds = data["ds"]
+    tr = ~holdout_mask(ds)
     t0 = time.time()
-    w, loss1 = tch.mlp_train(w, Xn[idx], y[idx], steps // 2, lr, device)
-    w, loss2 = tch.mlp_train(w, Xn[idx], y[idx], steps - steps // 2, lr / 5, device)
+    w_raw, loss, rows = fit(data, tr, steps, lr, seed, device)
     secs = time.time() - t0
-    w_raw = fold_standardisation(w, mu, sd)
     rep = evaluate(w_raw, data, device)
-    rep.update(train_rows=int(len(idx)), train_sets=int(len(np.unique(ds[tr]))), holdout_rows=int((~tr).sum()), steps=steps, final_train_mse=loss2,
-               train_seconds=secs)
+    rep.update(train_rows=rows, train_sets=int(len(np.unique(ds[tr]))), holdout_rows=int((~tr).sum()), steps=steps,
+               final_train_mse=loss, train_seconds=secs)
     w_raw.astype("<f4").tofile(out)
     return rep
 
 
+def cross_validate(sweep_path: str, folds: int = 5, steps: int = 6000, lr: float = 3e-3, seed: int = 7,
+                   device: int = 0) -> dict:
+    """The training recipe, k-fold: for each fold a model trained on the
+    other sets picks for the fold's sets; every set is held out once."""
+    data = offered(dict(np.load(sweep_path)))
+    ds = data["ds"]
+    out, per_fold = [], []
+    for f in range(folds):
+        hold = ds % folds == f
+        w_raw, _, _ = fit(data, ~hold, steps, lr, seed, device)
+        rep = evaluate(w_raw, data, device, mask=hold)
+        out += rep["sets"]
+        per_fold.append({k: v for k, v in rep.items() if k != "sets"})
+    res = summarise(out)
+    res.update(folds=folds, per_fold=per_fold)
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["sweep", "train", "report"])
+    ap.add_argument("cmd", choices=["sweep", "train", "report", "cv"])
     ap.add_argument("--datasets", type=int, default=200)
     ap.add_argument("--first", type=int, default=0, help="sweep: first profile set (seed)")
     ap.add_argument("--sweep", default=SWEEP_PATH)
@@ -258,6 +310,11 @@ def main():
         with open(REPORT_PATH, "w") as f:
             json.dump(rep, f, indent=1)
         print(json.dumps({k: v for k, v in rep.items() if k != "sets"}, indent=1))
+    elif a.cmd == "cv":  # the training recipe, 5-fold, on the shipped sweep
+        rep = cross_validate(a.sweep, steps=a.steps, device=a.device)
+        with open(a.out or CV_PATH, "w") as f:
+            json.dump(rep, f, indent=1)
+        print(json.dumps({k: v for k, v in rep.items() if k not in ("sets", "per_fold")}, indent=1))
     else:
         rep = train(a.sweep, a.out or tch.TAU_MLP_PATH, steps=a.steps, device=a.device)
         with open(REPORT_PATH, "w") as f:
