@@ -286,7 +286,12 @@ def serving_bench(tch, synth, args, device):
 
     A = synth.zipf_profiles(n_db + pool_rows, L, 5, 1.2, distinct, lambda rng, L: np.full(L, 0.03),
                             hashed_frac=0.05)
-    db_calls, pool = A[:n_db], A[n_db:]
+    db_calls = A[:n_db]
+    # the query profiles in page-locked memory, as a server receiving them
+    # into pinned buffers has them (a pageable source is staged by the driver
+    # and held up the other requests' copies)
+    pool = tch.pinned_empty(A[n_db:].shape, A.dtype)
+    pool[:] = A[n_db:]
     gen_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     db = tch.Database(db_calls, device=device)

@@ -524,9 +524,14 @@ int choose_tau_query(const std::vector<TauRow>& rows, int n, const TauModel& m, 
     return best;
 }
 
-// tau <= 0: the learned model's pick (tau and schedule) when one is set, else
-// the analytic tau with the default schedule.  *sub / *group receive the
-// schedule (0 = defaults).
+// tau <= 0: the learned model's pick (tau and schedule) when one is set and
+// the set is within the shapes it was trained on, else the analytic tau with
+// the default schedule.  *sub / *group receive the schedule (0 = defaults).
+// The model's sweep timed sets of up to 63 005 rows, every row counted in one
+// rare-count pass; sets wider than a pass (65 536 columns) count their rare
+// term in several and take the analytic pick (on 200 000 x 3 000 Zipf profiles
+// the learned pick ran 440 ms against the analytic 356 ms).
+constexpr int kLearnedMaxRows = 65536;
 int choose_tau_gb300(int device, const std::vector<uint32_t>& cnt_flat, const std::vector<uint64_t>& off, int n,
                      int L, size_t free_bytes, const TauModel& m, bool dense, bool verbose, int* sub, int* group) {
     const std::vector<TauRow> rows = tau_rows(cnt_flat, off, n, L, free_bytes, m, dense);
@@ -535,7 +540,7 @@ int choose_tau_gb300(int device, const std::vector<uint32_t>& cnt_flat, const st
     std::vector<float> pred;
     TauTable t;
     float w[kMlpParams];
-    if (tau_mlp_weights(w)) {
+    if (n <= kLearnedMaxRows && tau_mlp_weights(w)) {
         tau_features(rows, cnt_flat, off, n, L, &t);
         pred.resize(t.taus.size());
         Err quiet{nullptr, 0};

@@ -507,7 +507,10 @@ cudaError_t rare_batch_prepare(const std::vector<RareBatchItem>& items, RareBatc
 
 cudaError_t launch_rare_batch(const RareBatchPlan& plan, int sms, cudaStream_t st) {
     if (!plan.njobs || !plan.total_rows) return cudaSuccess;
-    const int grid = std::max(1, std::min(plan.total_rows, sms * 8));
+    // one CTA per row, as the per-set launches: rows differ widely in work
+    // (the sets' widths and taus), and the block scheduler balances them
+    (void)sms;
+    const int grid = std::max(1, plan.total_rows);
     rare_batch_kernel<256><<<grid, 256, rd_smem<256>(plan.cwords), st>>>(
         static_cast<const RareJob*>(plan.d_jobs), static_cast<const int*>(plan.d_row_job), plan.total_rows,
         plan.cwords);

@@ -179,9 +179,10 @@ int tch_set_rare_term(int dense);
  * A small MLP predicts ln(ms) of one whole-triangle solve for each candidate
  * (tau, sub-stripe rows, raster group) from TCH_TAU_FEATURES features; a
  * solver built from calls with tau <= 0 takes the candidate with the smallest
- * prediction when a model is set (tch_set_tau_mlp): its tau and its schedule
- * (tch_solver_set_schedule).  Without a model: the analytic model's tau and
- * the default schedule.  Feature row of a candidate: ln n, ln L, quantiles
+ * prediction when a model is set (tch_set_tau_mlp) and the set has at most
+ * 65 536 profiles (the shapes the shipped model was trained on): its tau and
+ * its schedule (tch_solver_set_schedule).  Otherwise: the analytic model's tau
+ * and the default schedule.  Feature row of a candidate: ln n, ln L, quantiles
  * 0.25 / 0.5 / 0.9 of ln(1 + distinct alleles per locus), missing fraction,
  * ln tau, ln(1 + frequent one-hot columns), ln(1 + rare pairs), ln(1 + rare
  * cells), ln(pairs x operand columns), ln(analytic estimate in seconds),

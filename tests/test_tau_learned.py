@@ -115,6 +115,23 @@ def test_training_recipe_cross_validated(tch):
 
 
 @pytest.mark.gpu
+def test_learned_pick_limited_to_trained_shapes(tch):
+    """A set wider than one rare-count pass (more than 65 536 profiles) takes
+    the analytic pick and the default schedule even with a model set."""
+    rng = np.random.default_rng(12)
+    A = rng.integers(1, 40, size=(70001, 6)).astype(np.uint64)
+    tch.set_tau_mlp(tch.load_tau_mlp())
+    try:
+        with tch.Solver.from_calls(A, tau=0) as s:
+            info = s.info()
+    finally:
+        tch.set_tau_mlp(None)
+    with tch.Solver.from_calls(A, tau=0) as s:
+        plain = s.info()
+    assert (info["tau"], info["sub_rows"], info["tile_group"]) == (plain["tau"], 0, 0)
+
+
+@pytest.mark.gpu
 def test_learned_tau_drives_the_solver_and_stays_exact(tch):
     """With the model set, a solver built with tau = 0 takes the candidate the
     model predicts fastest (tau and schedule); the distances stay exact; without
