@@ -212,7 +212,10 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
             ce = launch_tc_stripe(QX, &enc.X, R, ldr, a, db->sms, st);
             if (ce != cudaSuccess) goto done;
             mark();
-            ce = cudaMemcpy2DAsync(h_qdb, (size_t)n * 2, out, ldo * 2, (size_t)n * 2, m, cudaMemcpyDeviceToHost, st);
+            // one linear copy when the rows are packed (ldo == n), a pitched one otherwise
+            ce = ldo == (size_t)n ? cudaMemcpyAsync(h_qdb, out, (size_t)m * n * 2, cudaMemcpyDeviceToHost, st)
+                                  : cudaMemcpy2DAsync(h_qdb, (size_t)n * 2, out, ldo * 2, (size_t)n * 2, m,
+                                                      cudaMemcpyDeviceToHost, st);
             if (ce != cudaSuccess) goto done;
         }
         if (qq) {
@@ -221,7 +224,9 @@ int db_query(tch_db* db, int m, const uint64_t* qcalls, uint16_t* h_qdb, uint16_
             qq_kernel<<<grd, blk, 0, st>>>(dq, m, L, qq, ldq);
             ce = cudaGetLastError();
             if (ce == cudaSuccess)
-                ce = cudaMemcpy2DAsync(h_qq, (size_t)m * 2, qq, ldq * 2, (size_t)m * 2, m, cudaMemcpyDeviceToHost, st);
+                ce = ldq == (size_t)m ? cudaMemcpyAsync(h_qq, qq, (size_t)m * m * 2, cudaMemcpyDeviceToHost, st)
+                                      : cudaMemcpy2DAsync(h_qq, (size_t)m * 2, qq, ldq * 2, (size_t)m * 2, m,
+                                                          cudaMemcpyDeviceToHost, st);
             if (ce != cudaSuccess) goto done;
         }
     }
