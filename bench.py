@@ -559,6 +559,42 @@ def step_timing(tch, synth, args, device):
         s.check()
 
 
+def cli_timing(tch, synth, args):
+    """--cli-timing: the command-line tool end to end on the long-tail profiles
+    (--n x --L) written as a TSV (sample ids, '-' for missing calls): the table
+    parsed on the GPU (the default) and on the host cores (--host-parse), the
+    full matrix written as TSV to /dev/null; wall seconds, best of 3 each."""
+    import tempfile
+
+    A = synth.longtail(n=args.n, L=args.L)
+    t0 = time.perf_counter()
+    fd, path = tempfile.mkstemp(suffix=".tsv")
+    with os.fdopen(fd, "w") as f:
+        f.write("FILE\t" + "\t".join(f"locus{k}" for k in range(args.L)) + "\n")
+        for i in range(len(A)):
+            f.write(f"s{i}\t" + "\t".join("-" if v == 0 else str(v) for v in A[i].tolist()) + "\n")
+    gen_s = time.perf_counter() - t0
+    size = os.path.getsize(path)
+    res = {}
+    try:
+        for name, extra in (("gpu_parse", []), ("host_parse", ["--host-parse"])):
+            walls = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                r = subprocess.run([tch.CLI_PATH, "-i", path, "-o", "/dev/null", *extra], capture_output=True,
+                                   text=True)
+                walls.append(time.perf_counter() - t0)
+                if r.returncode:
+                    raise RuntimeError(r.stderr[-2000:])
+            res[name] = {"wall_s": min(walls), "samples_s": [round(w, 3) for w in walls],
+                         "log": [ln for ln in r.stderr.splitlines() if ln.startswith(("Loaded", "Encoded",
+                                                                                         "Computed"))]}
+    finally:
+        os.unlink(path)
+    print(json.dumps({"cli": f"{args.n} x {args.L} long-tail profiles, {size / 1e9:.2f} GB of TSV in, "
+                             f"the full matrix as TSV out", "generate_s": gen_s, **res}), flush=True)
+
+
 def batch_sets(tch, count, device):
     """The batched leg's generator: count sets, n log-uniform in [50, 5 000],
     L from {1 142, 1 343, 2 794, 3 016}, Zipf s in [1.0, 1.4] over lognormal
@@ -642,6 +678,8 @@ def main():
     ap.add_argument("--serving-only", action="store_true", help="run the serving leg alone and print its JSON")
     ap.add_argument("--step-timing", action="store_true",
                     help="time the rare counts and the tile pass of one solve of --n profiles at --tau, --reps times")
+    ap.add_argument("--cli-timing", action="store_true",
+                    help="time the command-line tool on the long-tail profiles as a TSV (GPU and host parse)")
     ap.add_argument("--batch-timing", action="store_true",
                     help="time one batched replay of --batch-count sets with --branches")
     ap.add_argument("--reps", type=int, default=3)
@@ -672,6 +710,9 @@ def main():
         return
     if args.batch_timing:
         batch_timing(tch, args, local)
+        return
+    if args.cli_timing:
+        cli_timing(tch, synth, args)
         return
 
     t0 = time.perf_counter()

@@ -116,6 +116,17 @@ def lib():
         L.tch_host_encoding_free.argtypes, L.tch_host_encoding_free.restype = [P(HostEncoding)], None
         L.tch_solver_from_calls.argtypes = [c_int, c_int, c_int, c_void, c_int, c_int, P(c_void), c_char_p, c_int]
         L.tch_solver_from_calls.restype = c_int
+        L.tch_tsv_parse.argtypes = [c_int, c_void, c_size, ctypes.c_char, c_int, c_char_p, P(c_void), c_char_p,
+                                    c_int]
+        L.tch_tsv_parse.restype = c_int
+        L.tch_tsv_shape.argtypes, L.tch_tsv_shape.restype = [c_void, P(c_int), P(c_int)], c_int
+        L.tch_tsv_ids.argtypes, L.tch_tsv_ids.restype = [c_void, c_void, c_void], c_int
+        L.tch_tsv_filter.argtypes = [c_void, c_double, c_double, c_char_p, c_int]
+        L.tch_tsv_filter.restype = c_int
+        L.tch_tsv_calls.argtypes, L.tch_tsv_calls.restype = [c_void, c_void], c_int
+        L.tch_solver_from_tsv.argtypes = [c_void, c_int, P(c_void), c_char_p, c_int]
+        L.tch_solver_from_tsv.restype = c_int
+        L.tch_tsv_free.argtypes, L.tch_tsv_free.restype = [c_void], None
         L.tch_run_calls.argtypes = [c_int, c_int, c_int, c_void, c_int, c_int, CB, c_void, P(c_double), P(c_int),
                                     c_char_p, c_int]
         L.tch_run_calls.restype = c_int
@@ -434,6 +445,68 @@ def set_rare_term(dense: bool) -> None:
 # ---------------------------------------------------------------------------------------
 # solver (device-resident operands)
 # ---------------------------------------------------------------------------------------
+
+class Tsv:
+    """The allele table parsed on the GPU (tch_tsv_*): `text` is the whole
+    input (bytes, UTF-8); the calls stay in device memory."""
+
+    def __init__(self, text: bytes, sep: str = "\t", skip_repl: bool = False, missing: str = "-",
+                 device: int = 0):
+        self._text = bytes(text)
+        self._h = ctypes.c_void_p()
+        err = _errbuf()
+        buf = ctypes.create_string_buffer(self._text, len(self._text))
+        _check(lib().tch_tsv_parse(device, ctypes.cast(buf, ctypes.c_void_p), len(self._text),
+                                   sep.encode()[:1], 1 if skip_repl else 0, missing.encode(), ctypes.byref(self._h),
+                                   err, len(err)), err)
+
+    def shape(self):
+        n, L = ctypes.c_int(), ctypes.c_int()
+        lib().tch_tsv_shape(self._h, ctypes.byref(n), ctypes.byref(L))
+        return n.value, L.value
+
+    def ids(self) -> list:
+        n, _ = self.shape()
+        b = np.zeros(max(n, 1), np.uint64)
+        e = np.zeros(max(n, 1), np.uint64)
+        lib().tch_tsv_ids(self._h, _ptr(b), _ptr(e))
+        return [self._text[int(b[i]):int(e[i])].decode() for i in range(n)]
+
+    def filter(self, locus_pct=None, sample_pct=None):
+        err = _errbuf()
+        _check(lib().tch_tsv_filter(self._h, -1.0 if locus_pct is None else float(locus_pct),
+                                    -1.0 if sample_pct is None else float(sample_pct), err, len(err)), err)
+
+    def calls(self) -> np.ndarray:
+        n, L = self.shape()
+        out = np.zeros((n, L), np.uint64)
+        if lib().tch_tsv_calls(self._h, _ptr(out)):
+            raise TchError("copying the parsed calls failed")
+        return out
+
+    def solver(self, tau: int = 0) -> "Solver":
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        _check(lib().tch_solver_from_tsv(self._h, tau, ctypes.byref(h), err, len(err)), err)
+        return Solver(h)
+
+    def close(self):
+        if self._h:
+            lib().tch_tsv_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 class Solver:
     def __init__(self, handle):

@@ -338,6 +338,9 @@ int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, 
 // lists reached the device (solvers that upload them stripe by stripe).
 int solver_stripe(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, cudaStream_t st, Err& e,
                   bool lists_uploaded = false);
+// The same from allele calls already in device memory (n x L u64, L >= 1; read only).
+int solver_from_device_calls(int device, int n, int L, const uint64_t* d_calls, int tau, bool verbose,
+                             tch_solver** out, Err& e);
 int solver_check(tch_solver* s, Err& e);
 void solver_free(tch_solver* s);
 int solver_stripe_counts(tch_solver* s, int r0, int rows, uint16_t* d_out, size_t ldo, uint16_t* R, size_t ldr,

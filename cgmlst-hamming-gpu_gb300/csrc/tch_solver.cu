@@ -333,9 +333,11 @@ __global__ void widen_ranks_kernel(const uint16_t* __restrict__ x, size_t count,
         calls[t] = x[t];
 }
 
-// calls: host u64 allele ids, or (ranks != nullptr) host u16 ranks.
+// calls: host u64 allele ids, or (ranks != nullptr) host u16 ranks, or
+// (dev_calls != nullptr, L >= 1) u64 allele ids already in device memory.
 static int solver_from_input(int device, int n, int L, const uint64_t* calls, const uint16_t* ranks, int tau,
-                             int kernel, bool verbose, tch_solver** out, Err& e) {
+                             int kernel, bool verbose, tch_solver** out, Err& e,
+                             const uint64_t* dev_calls = nullptr) {
     tch_solver* s = nullptr;
     uint64_t* d_calls = nullptr;
     uint16_t* d_ranks = nullptr;
@@ -343,7 +345,8 @@ static int solver_from_input(int device, int n, int L, const uint64_t* calls, co
     *out = nullptr;
     if (n < 0 || L < 0) return e.set("negative size (n=%d, L=%d)", n, L);
     if (L > 65535) return e.set("more than 65535 loci (u16 distances)");
-    if ((size_t)n * L && !calls && !ranks) return e.set("null input buffer");
+    if ((size_t)n * L && !calls && !ranks && !dev_calls) return e.set("null input buffer");
+    if (dev_calls && L < 1) return e.set("device calls need L >= 1");
     kernel = resolve_kernel(kernel);
     if (kernel != TCH_KERNEL_TC_F4)
         return e.set("the device encoder feeds the tensor-core kernel (tc_f4); kernel %s is not supported here",
@@ -358,8 +361,10 @@ static int solver_from_input(int device, int n, int L, const uint64_t* calls, co
     TCH_CK(e, cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, device));
     TCH_CK(e, dmalloc(s, (void**)&s->dErr, sizeof(int)));
     TCH_CK(e, cudaMemset(s->dErr, 0, sizeof(int)));
-    TCH_CK(e, cudaMalloc(&d_calls, std::max<size_t>((size_t)n * Le, 1) * 8));
-    if (L && ranks) {
+    if (!dev_calls) TCH_CK(e, cudaMalloc(&d_calls, std::max<size_t>((size_t)n * Le, 1) * 8));
+    if (dev_calls) {
+        // read in place
+    } else if (L && ranks) {
         const size_t count = (size_t)n * L;
         TCH_CK(e, cudaMalloc(&d_ranks, std::max<size_t>(count, 1) * 2));
         if (count) {
@@ -375,7 +380,7 @@ static int solver_from_input(int device, int n, int L, const uint64_t* calls, co
     } else {
         TCH_CK(e, cudaMemset(d_calls, 0, std::max<size_t>((size_t)n, 1) * 8));
     }
-    if (encode_on_device(device, n, Le, d_calls, tau, g_tau_model, verbose, max_chunk_bytes(),
+    if (encode_on_device(device, n, Le, dev_calls ? dev_calls : d_calls, tau, g_tau_model, verbose, max_chunk_bytes(),
                          rare_dense_default() ? ENC_DENSE : 0, &enc, e))
         goto fail;
     cudaFree(d_calls);
@@ -427,6 +432,11 @@ fail:
 int solver_from_calls(int device, int n, int L, const uint64_t* calls, int tau, int kernel, bool verbose,
                       tch_solver** out, Err& e) {
     return solver_from_input(device, n, L, calls, nullptr, tau, kernel, verbose, out, e);
+}
+
+int solver_from_device_calls(int device, int n, int L, const uint64_t* d_calls, int tau, bool verbose,
+                             tch_solver** out, Err& e) {
+    return solver_from_input(device, n, L, nullptr, nullptr, tau, TCH_KERNEL_AUTO, verbose, out, e, d_calls);
 }
 
 static RareGroups rare_groups(const tch_solver* s) {
@@ -782,6 +792,9 @@ static int solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_se
             } else if (solver_stripe(s, r0, rows, dU[b], ldo, st[b], e, false)) {
                 goto fail;
             }
+            // pitched: a stripe's rows are n - r0 wide; with two stripes in flight this ran
+            // 37.1 ms per whole triangle, a device repack to packed rows plus one linear
+            // copy 40.3 ms
             TCH_CK(e, cudaMemcpy2DAsync(hU[b], w * 2, dU[b], ldo * 2, w * 2, rows, cudaMemcpyDeviceToHost, st[b]));
             TCH_CK(e, cudaEventRecord(done[b], st[b]));
         }

@@ -13,8 +13,10 @@
 //   write          main.rs:213-265, 472-490 (gzip: level 3, also for *.gz)
 //
 // Differences that do not change any output byte: the automatic tau uses rates
-// measured on GB300 instead of the L4 constants of main.rs:170-171, and the
-// writer formats on the GPU (tch_solver_write_tsv; --host-format: a thread
+// measured on GB300 instead of the L4 constants of main.rs:170-171, the table is
+// parsed and filtered on the GPU (tch_tsv_parse / tch_tsv_filter, feeding the
+// device encoder; --host-parse or --host-encode: a thread pool on the CPU), and
+// the writer formats on the GPU (tch_solver_write_tsv; --host-format: a thread
 // pool on the CPU) instead of with rayon.
 
 #include <dlfcn.h>
@@ -126,6 +128,7 @@ struct Args {
     bool silent = false;
     bool host_encode = false;
     bool host_format = false;
+    bool host_parse = false;
 };
 
 const char* kUsage =
@@ -153,6 +156,7 @@ const char* kUsage =
     "  -s, --silent                             Suppress progress/log messages on stderr\n"
     "      --host-encode                        Encode on the host and call tch_run (the reference's path)\n"
     "      --host-format                        Format the matrix text on the CPU (default: on the GPU)\n"
+    "      --host-parse                         Parse the input table on the CPU (default: on the GPU)\n"
     "  -h, --help                               Print help\n"
     "  -V, --version                            Print version\n";
 
@@ -198,6 +202,7 @@ Args parse_args(int argc, char** argv) {
                                {nullptr, "tau", true},       {nullptr, "stripe", true},
                                {nullptr, "device", true},    {"s", "silent", false},
                                {nullptr, "host-encode", false},     {nullptr, "host-format", false},
+                               {nullptr, "host-parse", false},
                                {"h", "help", false},         {"V", "version", false}};
     for (int k = 1; k < argc; k++) {
         std::string arg = argv[k];
@@ -287,6 +292,8 @@ Args parse_args(int argc, char** argv) {
             a.host_encode = true;
         } else if (name == "host-format") {
             a.host_format = true;
+        } else if (name == "host-parse") {
+            a.host_parse = true;
         }
     }
     if (!have_input) usage_error("the following required arguments were not provided:\n  --input <INPUT>");
@@ -750,17 +757,43 @@ int main(int argc, char** argv) {
     std::string rerr;
     if (!read_all(args.input, in, rerr, threads)) die(fmt("reading %s: %s", args.input.c_str(), rerr.c_str()));
     const std::string_view text = in.view;
+    if (text.empty()) die("empty input");
+    // the table parsed on the GPU (the calls stay there for the device encoder),
+    // or on the host cores (--host-parse, and the reference's path)
+    const bool gpu_parse = !args.host_parse && !args.host_encode;
+    tch_tsv* tsv = nullptr;
+    size_t n = 0, L = 0;
+    std::vector<std::string> ids;
+    CallMatrix calls;
+    auto tsv_ids = [&]() {
+        int nn = 0, ll = 0;
+        tch_tsv_shape(tsv, &nn, &ll);
+        n = (size_t)nn;
+        L = (size_t)ll;
+        std::vector<size_t> b(n), e(n);
+        tch_tsv_ids(tsv, b.data(), e.data());
+        ids.assign(n, std::string());
+        for (size_t i = 0; i < n; i++) ids[i] = std::string(text.substr(b[i], e[i] - b[i]));
+    };
+    if (gpu_parse) {
+        if (cuda_start.joinable()) cuda_start.join();
+        g_cuda_starting = false;
+        char perr[512] = {0};
+        if (tch_tsv_parse((int)args.device, text.data(), text.size(), sep, args.skip_repl ? 1 : 0,
+                          args.missing.c_str(), &tsv, perr, sizeof perr))
+            die(perr);
+        tsv_ids();
+    } else {
     auto lines = rust_lines(text, threads);
-    if (lines.empty()) die("empty input");
-    size_t L = 1;
+    L = 1;
     for (size_t p = lines[0].first; p < lines[0].second; p++) L += text[p] == sep;
     L -= 1;
     std::vector<std::pair<size_t, size_t>> data;
     for (size_t k = 1; k < lines.size(); k++)
         if (lines[k].second > lines[k].first) data.push_back(lines[k]);
-    size_t n = data.size();
-    std::vector<std::string> ids(n);
-    CallMatrix calls(n * L);  // every cell written by the parse below
+    n = data.size();
+    ids.assign(n, std::string());
+    CallMatrix(n * L).swap(calls);  // every cell written by the parse below
     std::atomic<long> bad_row{-1};
     std::vector<std::string> bad_cell(1);
     std::atomic<bool> bad_taken{false};
@@ -783,11 +816,16 @@ int main(int argc, char** argv) {
         }
     });
     if (bad_row >= 0) die(fmt("sample %s: allele '%s' too large", ids[bad_row].c_str(), bad_cell[0].c_str()));
-    in = InputText();
+    }
     log(fmt("Loaded %zu samples x %zu loci in %.2fs", n, L, now() - t));
 
     // ---- completeness filters (main.rs:313-348), counted and compacted in parallel
-    if (args.has_locus) {
+    if (args.has_locus && tsv) {
+        char ferr[512] = {0};
+        if (tch_tsv_filter(tsv, args.locus_pct, -1.0, ferr, sizeof ferr)) die(ferr);
+        tsv_ids();
+        log(fmt("Locus completeness >= %s%%: kept %zu loci", fmt("%g", args.locus_pct).c_str(), L));
+    } else if (args.has_locus) {
         // non-missing calls per locus: blocks of rows counted apart, then summed
         const size_t parts = std::max<size_t>(1, std::min<size_t>(threads, n / 256 + 1));
         std::vector<std::vector<size_t>> part(parts, std::vector<size_t>(L, 0));
@@ -818,7 +856,12 @@ int main(int argc, char** argv) {
         }
         log(fmt("Locus completeness >= %s%%: kept %zu loci", fmt("%g", args.locus_pct).c_str(), L));
     }
-    if (args.has_sample) {
+    if (args.has_sample && tsv) {
+        char ferr[512] = {0};
+        if (tch_tsv_filter(tsv, -1.0, args.sample_pct, ferr, sizeof ferr)) die(ferr);
+        tsv_ids();
+        log(fmt("Sample completeness >= %s%%: kept %zu samples", fmt("%g", args.sample_pct).c_str(), n));
+    } else if (args.has_sample) {
         std::vector<char> ok(n, 0);
         parallel_for(threads, n, 256, [&](size_t a, size_t b) {
             for (size_t i = a; i < b; i++) {
@@ -845,6 +888,7 @@ int main(int argc, char** argv) {
         }
         log(fmt("Sample completeness >= %s%%: kept %zu samples", fmt("%g", args.sample_pct).c_str(), n));
     }
+    in = InputText();  // the ids are copied out
     if (L > 65535) die("more than 65535 loci (u16 distances)");
 
     // ---- output (main.rs:472-490): a file or stdout, gzip level 3 with -z or *.gz
@@ -865,7 +909,7 @@ int main(int argc, char** argv) {
     };
 
     // ---- encode (main.rs:353-445) and GPU (main.rs:447-465)
-    cuda_start.join();
+    if (cuda_start.joinable()) cuda_start.join();
     g_cuda_starting = false;
     t = now();
     char err[512] = {0};
@@ -876,10 +920,13 @@ int main(int argc, char** argv) {
         const size_t stripe = std::max<size_t>(args.stripe, 8) / 8 * 8;
         if (!args.silent) setenv("TCH_VERBOSE", "1", 1);
         tch_solver* solver = nullptr;
-        if (tch_solver_from_calls((int)args.device, (int)n, (int)L, calls.data(), (int)args.tau, TCH_KERNEL_AUTO,
-                                  &solver, err, sizeof err))
+        if (tsv ? tch_solver_from_tsv(tsv, (int)args.tau, &solver, err, sizeof err)
+                : tch_solver_from_calls((int)args.device, (int)n, (int)L, calls.data(), (int)args.tau,
+                                        TCH_KERNEL_AUTO, &solver, err, sizeof err))
             die(err);
         CallMatrix().swap(calls);
+        tch_tsv_free(tsv);
+        tsv = nullptr;
         tch_info info;
         tch_solver_info(solver, &info);
         log(fmt("Encoded in %.2fs: tau=%d, one-hot cols=%zu, rare equal pairs=%zu", now() - t, info.tau,
@@ -945,6 +992,12 @@ int main(int argc, char** argv) {
     } else {
         // n < 2 or no loci: every distance is 0 and the GPU is not used (main.rs:466-470);
         // the reference still ranks the calls, which enforces its 65535-allele limit
+        if (tsv) {
+            CallMatrix(n * L).swap(calls);
+            if (tch_tsv_calls(tsv, calls.data())) die("copying the parsed calls failed");
+            tch_tsv_free(tsv);
+            tsv = nullptr;
+        }
         std::vector<uint16_t> x(n * L);
         std::vector<uint32_t> nd(L);
         if (tch_dense_ranks(calls.data(), (int)n, (int)L, x.data(), nd.data(), (int)threads, err, sizeof err))

@@ -287,6 +287,34 @@ int tch_batch_set_schedule(tch_batch* b, int branches);
 int tch_batch_info(const tch_batch* b, int* count, int* taus, int* branches);
 void tch_batch_destroy(tch_batch* b);
 
+/* ---- the allele table parsed on the GPU (main.rs:286-348) -------------------------
+ * tch_tsv_parse copies text[0, len) (the whole input, UTF-8 already checked by
+ * the caller) to the device and parses it there as the reference's load does:
+ * its lines as str::lines gives them, line 0 the header (L = its field count -
+ * 1), every later non-empty line a sample: the id up to the first `sep`, then
+ * its cells by parse_allele (main.rs:95-113: Unicode trim, one leading "INF-"
+ * dropped unless skip_repl, `missing` (at most 64 bytes) or empty -> 0, all
+ * ASCII digits -> the u64 value, anything else -> 0; cells past L dropped,
+ * missing ones 0).  A value above 2^64 - 1 fails with "sample <id>: allele
+ * '<cell>' too large".  The calls stay in device memory: tch_solver_from_tsv
+ * builds a solver from them without a host copy. */
+typedef struct tch_tsv tch_tsv;
+int tch_tsv_parse(int device, const char* text, size_t len, char sep, int skip_repl, const char* missing,
+                  tch_tsv** out, char* err, int errlen);
+int tch_tsv_shape(const tch_tsv* t, int* n, int* L);
+/* Sample id of row i: text[begin[i], end[i]) of the parsed text. */
+int tch_tsv_ids(const tch_tsv* t, size_t* begin, size_t* end);
+/* Completeness filters (main.rs:313-348) on the device: loci whose share of
+ * non-missing calls x 100 >= locus_pct, then samples whose share >= sample_pct
+ * (a negative threshold: no filter). */
+int tch_tsv_filter(tch_tsv* t, double locus_pct, double sample_pct, char* err, int errlen);
+/* The calls (n x L u64) copied to host memory. */
+int tch_tsv_calls(const tch_tsv* t, uint64_t* calls);
+/* A solver from the parsed calls (device encoder; tau <= 0: chosen by the
+ * models), as tch_solver_from_calls. */
+int tch_solver_from_tsv(const tch_tsv* t, int tau, tch_solver** out, char* err, int errlen);
+void tch_tsv_free(tch_tsv* t);
+
 /* Fill *info. */
 int tch_solver_info(const tch_solver* s, tch_info* info);
 /* Schedule of the solver's stripes: every stripe runs as sub-stripes of

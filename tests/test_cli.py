@@ -73,18 +73,21 @@ def case_files(tmp_path_factory, golden):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("encoder", ["device", "device-hostformat", "host"])
+@pytest.mark.parametrize("encoder", ["device", "device-hostformat", "device-hostparse", "host"])
 @pytest.mark.parametrize("case_idx", [0, 1, 2])
 @pytest.mark.parametrize("flags_idx", range(len(refgen.CHECKPY_FLAGSETS)))
 def test_checkpy_matrix(pkg, case_files, encoder, case_idx, flags_idx):
-    """device: device encoder + text formatted on the GPU; device-hostformat:
-    device encoder + the CPU writer; host: the reference's path (tch_run)."""
+    """device: table parsed on the GPU, device encoder, text formatted on the
+    GPU; device-hostformat: the CPU writer; device-hostparse: the table parsed
+    on the CPU; host: the reference's path (host parse and encode, tch_run)."""
     c, path, A = case_files[case_idx]
     args, kind = refgen.CHECKPY_FLAGSETS[flags_idx]
     if encoder == "host":
         args = args + ["--host-encode"]
     elif encoder == "device-hostformat":
         args = args + ["--host-format"]
+    elif encoder == "device-hostparse":
+        args = args + ["--host-parse"]
     r = run(pkg, ["-s", "-i", path, *args])
     assert r.returncode == 0, r.stderr
     got = parse(r.stdout, "," if "-D" in args else "\t")
@@ -106,7 +109,7 @@ def test_full_text_equals_oracle(pkg, tmp_path):
     for args, kw in [([], {}), (["-m", "lower-tri", "-D", ";"], dict(mode="lower-tri", osep=";")),
                      (["-m", "upper-tri", "-X", "1", "-x", "ID"], dict(mode="upper-tri", cap=1, index_name="ID")),
                      (["-D", "::"], dict(osep="::"))]:
-        for fmt in ([], ["--host-format"], ["--host-encode"]):
+        for fmt in ([], ["--host-format"], ["--host-parse"], ["--host-encode"]):
             r = run(pkg, ["-s", "-i", str(p), *args, *fmt])
             assert r.returncode == 0, r.stderr
             assert r.stdout == oracle.write_matrix(ids, H, **kw), fmt
@@ -175,9 +178,10 @@ def test_filters_and_cell_options(pkg, tmp_path):
                      (["-L", "50", "-S", "50"], dict(locus_pct=50.0, sample_pct=50.0)),
                      (["-n", "X"], dict(missing="X")), (["-r"], dict(skip_repl=True))]:
         ids, x, cnt, H = oracle.distances_from_text(text, **kw)
-        r = run(pkg, ["-s", "-i", str(p), *args])
-        assert r.returncode == 0, (args, r.stderr)
-        assert r.stdout == oracle.write_matrix(ids, H), args
+        for parse_on in ([], ["--host-parse"]):
+            r = run(pkg, ["-s", "-i", str(p), *args, *parse_on])
+            assert r.returncode == 0, (args, parse_on, r.stderr)
+            assert r.stdout == oracle.write_matrix(ids, H), (args, parse_on)
 
 
 @pytest.mark.gpu
@@ -189,8 +193,9 @@ def test_edge_inputs(pkg, tmp_path):
 
     r = go("")
     assert r.returncode == 1 and "empty input" in r.stderr
-    r = go("F\tL0\nA\t18446744073709551616\n")
-    assert r.returncode == 1 and "sample A: allele '18446744073709551616' too large" in r.stderr
+    for parse_on in ([], ["--host-parse"]):
+        r = go("F\tL0\nA\t18446744073709551616\n", *parse_on)
+        assert r.returncode == 1 and "sample A: allele '18446744073709551616' too large" in r.stderr
     r = go(b"F\tL0\nA\t\xff\n")
     assert r.returncode == 1 and "valid UTF-8" in r.stderr
     r = go("F\tL0\tL1\nA\t1\t2\n")  # one sample: no GPU work, 1x1 matrix
