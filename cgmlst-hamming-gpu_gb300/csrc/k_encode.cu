@@ -414,27 +414,43 @@ struct TauRow {
 // to device memory.
 std::vector<TauRow> tau_rows(const std::vector<uint32_t>& cnt_flat, const std::vector<uint64_t>& off, int n, int L,
                              size_t free_bytes, const TauModel& m, bool dense) {
-    std::vector<double> cs;
+    // the candidates are powers of two, so an allele is frequent at tau = 2^t
+    // exactly when floor(log2(count)) >= t: one pass bins the counts by that,
+    // and every candidate sums whole bins (the sums are integers far below 2^53,
+    // exact in double whatever their order)
+    constexpr int kBins = 33;
+    double bn[kBins] = {}, bsq[kBins] = {}, br[kBins] = {}, bcells[kBins] = {};
     for (int k = 0; k < L; k++)
-        for (uint64_t q = off[k] + 1; q < off[k + 1]; q++)
-            if (cnt_flat[q]) cs.push_back((double)cnt_flat[q]);
+        for (uint64_t q = off[k] + 1; q < off[k + 1]; q++) {
+            const uint32_t c = cnt_flat[q];
+            if (!c) continue;
+            const int b = 31 - __builtin_clz(c);
+            const double v = (double)c;
+            bn[b] += 1.0;
+            bsq[b] += v * v;
+            if (c >= 2) {
+                br[b] += v * (v - 1.0) / 2.0;
+                bcells[b] += v;
+            }
+        }
     const double pairs = (double)n * (double)(n - 1) / 2.0;
     const size_t rows = up((size_t)std::max(n, 1), 256);
     const double nl = (double)n * (double)L;
     std::vector<TauRow> out;
-    for (int tau = 2; tau <= (dense ? 65536 : 4096); tau *= 2) {
+    for (int t = 1; (1 << t) <= (dense ? 65536 : 4096); t++) {
         TauRow w;
-        w.tau = tau;
-        for (double v : cs) {
-            if (v >= tau) w.d++;
-            else {
-                w.sq += v * v;
-                if (v >= 2) {
-                    w.r += v * (v - 1.0) / 2.0;
-                    w.cells += v;
-                }
+        w.tau = 1 << t;
+        double d = 0;
+        for (int b = 0; b < kBins; b++) {
+            if (b >= t) {
+                d += bn[b];
+            } else {
+                w.sq += bsq[b];
+                w.r += br[b];
+                w.cells += bcells[b];
             }
         }
+        w.d = (size_t)d;
         w.kb = (double)fp4_columns(L, w.d);  // K: MACs per pair; the two operand copies take K bytes per row
         if (dense) {  // ranks, own positions, group members, row runs (a stripe's counts come later)
             w.mem = (double)rows * w.kb + nl * 6.0 + 12.0 * w.cells + 12.0 * n;
