@@ -426,8 +426,10 @@ def picks(tch, A, device):
     il = int(np.argmin(pred))
     dflt = (c["subs"] == 0) & (c["groups"] == DEFAULT_GROUP)
     ia = int(np.argmin(np.where(dflt, c["est"], np.inf)))
-    return {"analytic": (int(c["taus"][ia]), 0, 0),
-            "learned": (int(c["taus"][il]), int(c["subs"][il]), int(c["groups"][il]))}
+    analytic = (int(c["taus"][ia]), 0, 0)
+    # the library takes the model's pick for sets of at most 65 536 profiles
+    learned = (int(c["taus"][il]), int(c["subs"][il]), int(c["groups"][il])) if len(A) <= 65536 else analytic
+    return {"analytic": analytic, "learned": learned}
 
 
 def big_config_bench(tch, synth, args, device):
