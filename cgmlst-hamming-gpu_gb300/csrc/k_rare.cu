@@ -26,6 +26,10 @@
 namespace tch {
 namespace {
 
+#ifndef TCH_RARE_NARROW_T
+#define TCH_RARE_NARROW_T 256
+#endif
+constexpr int NT = TCH_RARE_NARROW_T;      // threads per CTA of the narrow-row kernels (one row each)
 constexpr int RD_WORDS = 32768;          // u32 counter words in shared memory (128 KB): 65 536 columns per pass
 
 // Counter words a launch needs (a narrow stripe takes less shared memory, so
@@ -144,7 +148,24 @@ __device__ __forceinline__ void walk_part(uint32_t* cnt, const uint32_t* pre, co
         return;
     }
     uint32_t a = pre[p], b = pre[p + 1], r = run[p];  // this lane's current run
-    for (uint32_t e0 = e_begin; e0 < e_end; e0 += 256) {
+    uint32_t e0 = e_begin;
+    for (; e0 + 256 <= e_end; e0 += 256) {  // whole batches: no bounds checks
+        uint32_t j[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const uint32_t e = e0 + (uint32_t)(u * 32 + lane);
+            while (e >= b) {  // next run (pre[nr] = total > e bounds it)
+                ++p;
+                a = b;
+                b = pre[p + 1];
+                r = run[p];
+            }
+            j[u] = __ldg(members + r + (e - a));
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) count_col(cnt, j[u] - (uint32_t)wb);
+    }
+    for (; e0 < e_end; e0 += 256) {  // the last, partial batch
         uint32_t idx[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) {
@@ -497,8 +518,8 @@ cudaError_t rare_batch_prepare(const std::vector<RareBatchItem>& items, RareBatc
     static bool attrs[kMaxDevices] = {};
     bool& attr = attrs[current_device()];
     if (!attr) {
-        e = cudaFuncSetAttribute(rare_batch_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 rd_smem<256>(RD_WORDS));
+        e = cudaFuncSetAttribute(rare_batch_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 rd_smem<NT>(RD_WORDS));
         if (e != cudaSuccess) return e;
         attr = true;
     }
@@ -511,7 +532,7 @@ cudaError_t launch_rare_batch(const RareBatchPlan& plan, int sms, cudaStream_t s
     // (the sets' widths and taus), and the block scheduler balances them
     (void)sms;
     const int grid = std::max(1, plan.total_rows);
-    rare_batch_kernel<256><<<grid, 256, rd_smem<256>(plan.cwords), st>>>(
+    rare_batch_kernel<NT><<<grid, NT, rd_smem<NT>(plan.cwords), st>>>(
         static_cast<const RareJob*>(plan.d_jobs), static_cast<const int*>(plan.d_row_job), plan.total_rows,
         plan.cwords);
     return cudaGetLastError();
@@ -536,8 +557,8 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
                                              rd_smem<1024>(RD_WORDS));
 
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(rare_dense_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     rd_smem<256>(RD_WORDS));
+            e = cudaFuncSetAttribute(rare_dense_kernel<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     rd_smem<NT>(RD_WORDS));
         if (e != cudaSuccess) return e;
         attr = true;
     }
@@ -554,7 +575,7 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
         small_rows = v ? std::max(0, atoi(v)) : INT_MAX;
     }
     if (rows < small_rows && width <= 8192) {
-        rare_dense_kernel<256><<<std::max(1, rows), 256, rd_smem<256>(cwords), st>>>(g, r0, rows, R, ldr,
+        rare_dense_kernel<NT><<<std::max(1, rows), NT, rd_smem<NT>(cwords), st>>>(g, r0, rows, R, ldr,
                                                                                    r0 + (int)width, cwords);
     } else {
         const int grid = std::max(1, std::min(rows, sms));
