@@ -27,7 +27,7 @@ namespace tch {
 namespace {
 
 #ifndef TCH_RARE_NARROW_T
-#define TCH_RARE_NARROW_T 256
+#define TCH_RARE_NARROW_T 128
 #endif
 constexpr int NT = TCH_RARE_NARROW_T;      // threads per CTA of the narrow-row kernels (one row each)
 constexpr int RD_WORDS = 32768;          // u32 counter words in shared memory (128 KB): 65 536 columns per pass
