@@ -563,12 +563,12 @@ cudaError_t launch_rare_dense(const RareGroups& g, int r0, int rows, uint16_t* R
         attr = true;
     }
     const int cwords = counter_words(width);
-    // a narrow stripe takes CTAs of 256 threads, one row each: four fit on an SM,
-    // so four rows' lookup chains (rank -> group -> partner search) overlap, and
-    // solves that run side by side share the SMs.  Narrow rows carry little
-    // counting work, so their time is those chains: on 512 sets of 50-5 000
-    // profiles (one graph) the batch took 36.5 ms this way and 46.4 ms when only
-    // stripes under 304 rows did.  TCH_RARE_SMALL_ROWS sets a row limit for it.
+    // a narrow stripe takes CTAs of NT (128) threads, one row each: eight fit on
+    // an SM, so eight rows' chains of dependent steps overlap, and solves that
+    // run side by side share the SMs.  Narrow rows carry little counting work,
+    // so their time is those chains: the 512-set batch (50-5 000 profiles each)
+    // took 17.4 ms with 128 threads per row and 18.5 ms with 256.
+    // TCH_RARE_SMALL_ROWS sets a row limit for it.
     static int small_rows = -1;
     if (small_rows < 0) {
         const char* v = getenv("TCH_RARE_SMALL_ROWS");
