@@ -530,6 +530,77 @@ def big_config_bench(tch, synth, args, device):
     return out_legs
 
 
+def linkage_timing(tch, synth, args, device):
+    """--linkage-timing: the consumers of the matrix on the long-tail set of
+    --n profiles.  The full matrix is put in device memory once (the solver's
+    upper triangle, mirrored); then the minimum spanning tree and the k = 10
+    and k = 32 nearest neighbours of every profile are computed from it,
+    --reps times each (wall time of the call: kernels, the copy of the result
+    to host memory, and the sort of the tree's edges), and the tree once more
+    through the solver (its full matrix included).  Checks that need no full
+    oracle matrix: the tree has n - 1 edges and joins every profile (the call
+    checks that itself), every edge's distance equals the count on the ranks,
+    every sampled row's lightest edge is in the tree (the cut property of a
+    single profile), and the sampled rows' neighbours equal the oracle's row."""
+    import torch
+
+    oracle = load_oracle()
+    n = args.n
+    A = synth.longtail(n=n, L=args.L)
+    x, _ = tch.dense_ranks(A)
+    ld = (n + 7) // 8 * 8
+    dev = f"cuda:{device}"
+    out = {"workload": f"longtail {n}x{args.L}", "n": n}
+    with tch.Solver.from_calls(A, device=device) as s:
+        H = torch.empty((n, ld), dtype=torch.int16, device=dev)
+        st = torch.cuda.current_stream().cuda_stream
+        s.stripe(0, n, H.data_ptr(), ld, st)
+        torch.cuda.synchronize()
+        U = torch.triu(H[:, :n], 1)
+        H[:, :n] = U + U.T
+        del U
+        torch.cuda.synchronize()
+        times = {"mst": [], "k10": [], "k32": []}
+        for _ in range(args.reps):
+            t0 = time.perf_counter()
+            u, v, w = tch.mst_device(H.data_ptr(), ld, n, st)
+            times["mst"].append(time.perf_counter() - t0)
+            for k in (10, 32):
+                t0 = time.perf_counter()
+                idx, dist = tch.neighbors_device(H.data_ptr(), ld, n, k, st)
+                times[f"k{k}"].append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        u2, v2, w2 = s.mst()
+        solver_mst_s = time.perf_counter() - t0
+    del H
+    torch.cuda.empty_cache()
+    for key, ts in times.items():
+        out[f"{key}_ms"] = round(float(np.median(ts)) * 1e3, 2)
+        out[f"{key}_samples_ms"] = [round(t * 1e3, 2) for t in ts]
+    out["solver_mst_ms"] = round(solver_mst_s * 1e3, 1)
+    out["mst_weight"] = int(w.astype(np.int64).sum())
+    same = bool((u == u2).all() and (v == v2).all() and (w == w2).all())
+    # checks
+    xu, xv = x[u.astype(np.int64)], x[v.astype(np.int64)]
+    w_ref = ((xu != xv) & (xu > 0) & (xv > 0)).sum(1)
+    del xu, xv
+    tree = set(zip(u.tolist(), v.tolist()))
+    rows = np.linspace(0, n - 1, 64).astype(np.int64)
+    cut_bad = nbr_bad = 0
+    for r in rows.tolist():
+        d = oracle.hamming_block(x, r, r + 1, 0, n)[0].astype(np.int64)
+        key = (d << 42) | (np.minimum(np.arange(n), r) << 21) | np.maximum(np.arange(n), r)
+        key[r] = np.iinfo(np.int64).max
+        j = int(key.argmin())
+        cut_bad += (min(r, j), max(r, j)) not in tree
+        order = np.lexsort((np.arange(n), np.where(np.arange(n) == r, 1 << 20, d)))[:32]
+        nbr_bad += int((idx[r] != order).sum() + (dist[r] != d[order]).sum())
+    out["checks"] = {"edges": int(len(u)), "edge_distance_mismatches": int((w_ref != w).sum()),
+                     "sampled_rows": int(len(rows)), "cut_property_violations": int(cut_bad),
+                     "neighbor_mismatches": int(nbr_bad), "solver_tree_equal": same}
+    print(json.dumps(out), flush=True)
+
+
 def step_timing(tch, synth, args, device):
     """--step-timing: the two passes of one whole-triangle solve of the
     long-tail generator at --n profiles and --tau (rare counts, then the tile
@@ -684,6 +755,8 @@ def main():
                     help="time the command-line tool on the long-tail profiles as a TSV (GPU and host parse)")
     ap.add_argument("--batch-timing", action="store_true",
                     help="time one batched replay of --batch-count sets with --branches")
+    ap.add_argument("--linkage-timing", action="store_true",
+                    help="time the minimum spanning tree and nearest neighbours on the full matrix")
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--branches", type=int, default=32)
     ap.add_argument("--ref-stride", type=int, default=6,
@@ -712,6 +785,9 @@ def main():
         return
     if args.batch_timing:
         batch_timing(tch, args, local)
+        return
+    if args.linkage_timing:
+        linkage_timing(tch, synth, args, local)
         return
     if args.cli_timing:
         cli_timing(tch, synth, args)

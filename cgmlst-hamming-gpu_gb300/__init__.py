@@ -185,6 +185,20 @@ def lib():
         L.tch_solver_write_tsv.argtypes = [c_void, P(c_char_p), c_char_p, c_char_p, c_int, c_int, c_int, TEXT_CB,
                                            c_void, c_char_p, c_int]
         L.tch_solver_write_tsv.restype = c_int
+        L.tch_solver_mst.argtypes = [c_void, c_void, c_void, c_void, P(ctypes.c_uint64), c_char_p, c_int]
+        L.tch_solver_mst.restype = c_int
+        L.tch_solver_clusters.argtypes = [c_void, c_void, c_int, c_void, c_char_p, c_int]
+        L.tch_solver_clusters.restype = c_int
+        L.tch_solver_neighbors.argtypes = [c_void, c_int, c_void, c_void, c_char_p, c_int]
+        L.tch_solver_neighbors.restype = c_int
+        L.tch_mst_device.argtypes = [c_void, c_size, c_int, c_void, c_void, c_void, c_void, P(ctypes.c_uint64),
+                                     c_char_p, c_int]
+        L.tch_mst_device.restype = c_int
+        L.tch_neighbors_device.argtypes = [c_void, c_size, c_int, c_int, c_void, c_void, c_void, c_char_p, c_int]
+        L.tch_neighbors_device.restype = c_int
+        L.tch_mst_clusters.argtypes = [c_int, c_void, c_void, c_void, c_size, c_void, c_int, c_void, c_char_p,
+                                       c_int]
+        L.tch_mst_clusters.restype = c_int
         _lib = L
     return _lib
 
@@ -598,6 +612,34 @@ class Solver:
                                           block_rows, cb, None, err, len(err)), err)
         return None if sink is not None else b"".join(parts).decode()
 
+    def mst(self):
+        """The minimum spanning tree on the device (edges ordered by distance,
+        smaller index, larger index): (u, v, w) of its n - 1 edges, u < v."""
+        m = max(self.info()["n"] - 1, 0)
+        u, v, w = np.zeros(m, np.uint32), np.zeros(m, np.uint32), np.zeros(m, np.uint16)
+        total = ctypes.c_uint64(0)
+        err = _errbuf()
+        _check(lib().tch_solver_mst(self._h, _ptr(u), _ptr(v), _ptr(w), ctypes.byref(total), err, len(err)), err)
+        return u, v, w
+
+    def clusters(self, thresholds) -> np.ndarray:
+        """Single-linkage cluster labels (the smallest index of each profile's
+        cluster), one row per threshold."""
+        thr = np.ascontiguousarray(thresholds, dtype=np.uint32)
+        n = self.info()["n"]
+        labels = np.zeros((len(thr), n), np.uint32)
+        err = _errbuf()
+        _check(lib().tch_solver_clusters(self._h, _ptr(thr), len(thr), _ptr(labels), err, len(err)), err)
+        return labels
+
+    def neighbors(self, k: int):
+        """Every profile's k nearest profiles by (distance, index): (idx, dist), n x k."""
+        n = self.info()["n"]
+        idx, dist = np.zeros((n, max(k, 0)), np.uint32), np.zeros((n, max(k, 0)), np.uint16)
+        err = _errbuf()
+        _check(lib().tch_solver_neighbors(self._h, k, _ptr(idx), _ptr(dist), err, len(err)), err)
+        return idx, dist
+
     def run(self, stripe: int = 512, sink: StripeSink | None = None):
         sink = sink or StripeSink(self.info()["n"])
         cb = CB(sink)
@@ -622,6 +664,44 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------------------
+# consumers of a matrix already in device memory
+# ---------------------------------------------------------------------------------------
+
+def mst_device(d_H: int, ld: int, n: int, stream: int = 0):
+    """Minimum spanning tree of a full symmetric n x n u16 matrix at device
+    address d_H (row stride ld): (u, v, w)."""
+    m = max(n - 1, 0)
+    u, v, w = np.zeros(m, np.uint32), np.zeros(m, np.uint32), np.zeros(m, np.uint16)
+    total = ctypes.c_uint64(0)
+    err = _errbuf()
+    _check(lib().tch_mst_device(ctypes.c_void_p(d_H), ld, n, ctypes.c_void_p(stream) if stream else None, _ptr(u),
+                                _ptr(v), _ptr(w), ctypes.byref(total), err, len(err)), err)
+    return u, v, w
+
+
+def neighbors_device(d_H: int, ld: int, n: int, k: int, stream: int = 0):
+    """The k nearest profiles of every row of a full matrix in device memory."""
+    idx, dist = np.zeros((n, max(k, 0)), np.uint32), np.zeros((n, max(k, 0)), np.uint16)
+    err = _errbuf()
+    _check(lib().tch_neighbors_device(ctypes.c_void_p(d_H), ld, n, k, ctypes.c_void_p(stream) if stream else None,
+                                      _ptr(idx), _ptr(dist), err, len(err)), err)
+    return idx, dist
+
+
+def mst_clusters(n: int, u, v, w, thresholds) -> np.ndarray:
+    """Single-linkage labels at each threshold from a spanning tree's edges (host)."""
+    u = np.ascontiguousarray(u, dtype=np.uint32)
+    v = np.ascontiguousarray(v, dtype=np.uint32)
+    w = np.ascontiguousarray(w, dtype=np.uint16)
+    thr = np.ascontiguousarray(thresholds, dtype=np.uint32)
+    labels = np.zeros((len(thr), n), np.uint32)
+    err = _errbuf()
+    _check(lib().tch_mst_clusters(n, _ptr(u), _ptr(v), _ptr(w), len(u), _ptr(thr), len(thr), _ptr(labels), err,
+                                  len(err)), err)
+    return labels
 
 
 # ---------------------------------------------------------------------------------------

@@ -29,7 +29,8 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["tch_solver.cu", "k_popc.cu", "k_expand.cu", "k_tc.cu", "k_encode.cu", "k_rare.cu", "k_mlp.cu",
-              "serve.cu", "batch.cu", "format.cu", "encode_host.cpp", "noalloc.cu", "k_parse.cu"]
+              "serve.cu", "batch.cu", "format.cu", "encode_host.cpp", "noalloc.cu", "k_parse.cu",
+              "k_linkage.cu"]
 LIBNAME = "libtch.so"
 CLI_NAME = "cgmlst-hamming-gpu"
 

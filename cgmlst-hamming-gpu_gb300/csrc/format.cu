@@ -166,6 +166,14 @@ void text_release() {
 }
 
 }  // namespace
+
+cudaError_t launch_mirror(uint16_t* H, size_t ld, int n, cudaStream_t st) {
+    if (n < 2) return cudaSuccess;
+    const int nt = (n + TT - 1) / TT;
+    mirror_kernel<<<dim3(nt, nt), dim3(TT, 8), 0, st>>>(H, ld, n);
+    return cudaGetLastError();
+}
+
 }  // namespace tch
 
 using namespace tch;
@@ -215,11 +223,7 @@ extern "C" int tch_solver_write_tsv(tch_solver* s, const char* const* ids, const
         if (tch_solver_stripe(s, 0, n, H, ld, st, err, errlen)) goto fail;
         TCH_CK(e, cudaStreamSynchronize(st));
         if (tch_solver_check(s, err, errlen)) goto fail;
-        if (layout != 2) {
-            const int nt = (n + TT - 1) / TT;
-            mirror_kernel<<<dim3(nt, nt), dim3(TT, 8), 0, st>>>(H, ld, n);
-            TCH_CK(e, cudaGetLastError());
-        }
+        if (layout != 2) TCH_CK(e, launch_mirror(H, ld, n, st));
     }
     {
         std::string all_ids;

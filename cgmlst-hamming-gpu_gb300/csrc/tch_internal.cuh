@@ -352,6 +352,11 @@ const Fp4Operands* solver_operands(const tch_solver* s);
 // The rare groups of a dense-rare solver (false: it holds pair lists).
 bool solver_rare_groups(const tch_solver* s, RareGroups* g);
 
+// ---- format.cu ----------------------------------------------------------------------
+// H[i][j] = H[j][i] for j < i < n: the lower half of an n x n matrix (row
+// stride ld) from its upper half.
+cudaError_t launch_mirror(uint16_t* H, size_t ld, int n, cudaStream_t st);
+
 // ---- k_mlp.cu ----------------------------------------------------------------------
 constexpr int kMlpIn = TCH_TAU_FEATURES, kMlpHidden = TCH_MLP_HIDDEN, kMlpParams = TCH_MLP_PARAMS;
 // pred / loss / grad optional; y required for loss and grad.

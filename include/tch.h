@@ -373,6 +373,50 @@ int tch_solver_run(tch_solver* s, int S, tch_cb cb, void* ctx, double* gpu_secs,
 
 void tch_solver_destroy(tch_solver* s);
 
+/* ---- consumers of the matrix: MST, single-linkage clusters, nearest neighbours ----
+ * The uses the reference's documentation names for the matrix (outbreak
+ * clustering, minimum spanning trees, nearest-neighbour searches;
+ * docs/index.html, "The problem"); the reference itself stops at the matrix.
+ * Computed on the device from the full matrix in device memory; only the
+ * result comes back.
+ *
+ * Edges of the complete graph are ordered by (distance, smaller index, larger
+ * index).  That order is strict, so the minimum spanning tree is unique. */
+
+/* The minimum spanning tree of the profiles: n - 1 edges (u[e] < v[e], w[e]
+ * their distance) in the order above, and *total = the sum of w (any output
+ * may be NULL).  The solver's full matrix is computed into device memory
+ * (n * up(n, 8) * 2 bytes) for the call.  n < 2 gives no edges. */
+int tch_solver_mst(tch_solver* s, uint32_t* u, uint32_t* v, uint16_t* w, uint64_t* total, char* err, int errlen);
+
+/* Single-linkage clusters at each of nt thresholds: profiles i and j share a
+ * cluster at threshold t when a chain of profiles joins them with every step
+ * at distance <= t.  labels[k * n + i] = the smallest profile index in i's
+ * cluster at thresholds[k].  (From the minimum spanning tree: the clusters at
+ * t are its components after removing the edges heavier than t.) */
+int tch_solver_clusters(tch_solver* s, const uint32_t* thresholds, int nt, uint32_t* labels, char* err,
+                        int errlen);
+
+/* The k nearest profiles of every profile, 1 <= k <= 32 and k < n, in the
+ * order (distance, index): idx[i * k + r] and dist[i * k + r] for rank r. */
+int tch_solver_neighbors(tch_solver* s, int k, uint32_t* idx, uint16_t* dist, char* err, int errlen);
+
+/* The same on a full symmetric n x n u16 matrix already in device memory
+ * (row stride ld, a multiple of 8; d_H 16-byte aligned; the diagonal and the
+ * columns from n to ld are not read), on `stream` (NULL: a stream of the
+ * call); outputs in host memory; the call synchronises before it returns.
+ * n < 2^21. */
+int tch_mst_device(const uint16_t* d_H, size_t ld, int n, void* stream, uint32_t* u, uint32_t* v, uint16_t* w,
+                   uint64_t* total, char* err, int errlen);
+int tch_neighbors_device(const uint16_t* d_H, size_t ld, int n, int k, void* stream, uint32_t* idx, uint16_t* dist,
+                         char* err, int errlen);
+
+/* Host only: single-linkage cluster labels at nt thresholds from a minimum
+ * spanning tree's m edges (any order; u, v < n), as tch_solver_clusters
+ * labels them. */
+int tch_mst_clusters(int n, const uint32_t* u, const uint32_t* v, const uint16_t* w, size_t m,
+                     const uint32_t* thresholds, int nt, uint32_t* labels, char* err, int errlen);
+
 /* ----------------------------------------------------------------------------
  * Stripe without any device allocation.  No counterpart in the reference: it
  * exists for callers that may not call cudaMalloc (a service with a fixed

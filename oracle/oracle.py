@@ -20,6 +20,17 @@ reference project):
 * ``write_matrix``      main.rs:224-265 (layouts, cap, separators)
 * ``rollhash``          tensorcore/tc_hamming.cu:240-241 (upper-tri checksum)
 
+and the consumers of the matrix that the reference's documentation names
+(docs/index.html, "The problem": outbreak clustering, minimum spanning trees,
+nearest-neighbour searches; the reference has no code for them), from their
+definitions:
+
+* ``mst``               Prim's algorithm, edges ordered by (distance, smaller
+                        index, larger index), which makes the tree unique
+* ``clusters``          single linkage: components of the graph of pairs at
+                        distance <= t, straight from the matrix (not via a tree)
+* ``neighbors``         the k smallest (distance, index) of every row
+
 The heavy brute-force count is in ``oracle.c`` (OpenMP); everything else is
 numpy or plain Python and is meant for sizes that finish in seconds.
 """
@@ -428,3 +439,73 @@ def distances_from_text(text: str, **kw) -> tuple:
     tab = completeness(tab, kw.get("locus_pct"), kw.get("sample_pct"))
     x, cnt = dense_ranks(tab.calls)
     return tab.ids, x, cnt, hamming(x)
+
+
+# --------------------------------------------------------------------------------------
+# consumers of the matrix: minimum spanning tree, single linkage, nearest neighbours
+# --------------------------------------------------------------------------------------
+
+EDGE_BITS = 21
+
+
+def edge_keys(H: np.ndarray, v: int) -> np.ndarray:
+    """Keys of the edges (v, x) for every x: distance, smaller index, larger index."""
+    idx = np.arange(H.shape[0], dtype=np.uint64)
+    a = np.minimum(idx, np.uint64(v))
+    b = np.maximum(idx, np.uint64(v))
+    return (H[v].astype(np.uint64) << np.uint64(2 * EDGE_BITS)) | (a << np.uint64(EDGE_BITS)) | b
+
+
+def mst(H: np.ndarray):
+    """Minimum spanning tree of the complete graph on a full symmetric matrix
+    by Prim's algorithm under the strict edge order (distance, smaller index,
+    larger index): (u, v, w) of its n - 1 edges in that order, u < v."""
+    H = np.asarray(H)
+    n = H.shape[0]
+    if n < 2:
+        return np.zeros(0, np.uint32), np.zeros(0, np.uint32), np.zeros(0, np.uint16)
+    none = np.uint64(np.iinfo(np.uint64).max)
+    in_tree = np.zeros(n, dtype=bool)
+    in_tree[0] = True
+    best = edge_keys(H, 0)
+    keys = []
+    for _ in range(n - 1):
+        cand = np.where(in_tree, none, best)
+        x = int(cand.argmin())
+        keys.append(int(cand[x]))
+        in_tree[x] = True
+        best = np.minimum(best, edge_keys(H, x))
+    k = np.sort(np.array(keys, dtype=np.uint64))
+    m = np.uint64((1 << EDGE_BITS) - 1)
+    return (((k >> np.uint64(EDGE_BITS)) & m).astype(np.uint32), (k & m).astype(np.uint32),
+            (k >> np.uint64(2 * EDGE_BITS)).astype(np.uint16))
+
+
+def clusters(H: np.ndarray, thresholds) -> np.ndarray:
+    """Single-linkage clusters: labels[t, i] = the smallest index of the
+    component of i in the graph whose edges are the pairs i != j with
+    H[i, j] <= thresholds[t]."""
+    from scipy.sparse import csr_matrix
+    from scipy.sparse.csgraph import connected_components
+
+    H = np.asarray(H)
+    n = H.shape[0]
+    out = np.zeros((len(thresholds), n), dtype=np.uint32)
+    for t, thr in enumerate(thresholds):
+        adj = H.astype(np.int64) <= int(thr)
+        np.fill_diagonal(adj, False)
+        _, lab = connected_components(csr_matrix(adj), directed=False)
+        first = np.full(lab.max() + 1 if n else 0, n, dtype=np.int64)
+        np.minimum.at(first, lab, np.arange(n))
+        out[t] = first[lab]
+    return out
+
+
+def neighbors(H: np.ndarray, k: int):
+    """Every row's k nearest other rows by (distance, index): (idx, dist), n x k."""
+    H = np.asarray(H)
+    n = H.shape[0]
+    keys = (H.astype(np.uint64) << np.uint64(32)) | np.arange(n, dtype=np.uint64)[None, :]
+    np.fill_diagonal(keys, np.iinfo(np.uint64).max)
+    keys = np.sort(keys, axis=1)[:, :k]
+    return (keys & np.uint64(0xFFFFFFFF)).astype(np.uint32), (keys >> np.uint64(32)).astype(np.uint16)
