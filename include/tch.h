@@ -402,10 +402,10 @@ int tch_solver_clusters(tch_solver* s, const uint32_t* thresholds, int nt, uint3
 int tch_solver_neighbors(tch_solver* s, int k, uint32_t* idx, uint16_t* dist, char* err, int errlen);
 
 /* The same on a full symmetric n x n u16 matrix already in device memory
- * (row stride ld, a multiple of 8; d_H 16-byte aligned; the diagonal and the
- * columns from n to ld are not read), on `stream` (NULL: a stream of the
- * call); outputs in host memory; the call synchronises before it returns.
- * n < 2^21. */
+ * (row stride ld, a multiple of 8; d_H 16-byte aligned; the values on the
+ * diagonal and in columns n to ld - 1 are ignored, and columns from up(n, 8)
+ * on are not loaded), on `stream` (NULL: a stream of the call); outputs in
+ * host memory; the call synchronises before it returns.  n < 2^21. */
 int tch_mst_device(const uint16_t* d_H, size_t ld, int n, void* stream, uint32_t* u, uint32_t* v, uint16_t* w,
                    uint64_t* total, char* err, int errlen);
 int tch_neighbors_device(const uint16_t* d_H, size_t ld, int n, int k, void* stream, uint32_t* idx, uint16_t* dist,
