@@ -4,8 +4,9 @@ for the matrix, docs/index.html "The problem"; the reference has no code for
 them).
 
 CPU: the oracle's Prim tree equals a plain Kruskal under the same strict edge
-order, its threshold components equal the cut of that tree by the library's
-host cut (tch_mst_clusters), and its neighbours equal a sort of every row.
+order and has the weight of scipy's tree, its threshold components equal the
+cut of that tree by the library's host cut (tch_mst_clusters) and scipy's
+single-linkage clusters, and its neighbours equal a sort of every row.
 GPU: the device MST, clusters and neighbours equal the oracle's exactly, on
 the check.py cases, on the 2 000 x 1 142 synthetic set, on profile sets full
 of ties, and on arbitrary symmetric matrices in device memory (values over the
@@ -66,6 +67,35 @@ def test_tree_cut_equals_threshold_components(pkg, seed):
     perm = rng.permutation(len(u))
     np.testing.assert_array_equal(pkg.mst_clusters(H.shape[0], u[perm], v[perm], w[perm], thr),
                                   oracle.clusters(H, thr))
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_oracle_matches_scipy(seed):
+    """An independent pin of the oracle: scipy's minimum spanning tree has the
+    same total weight (ties may pick other edges, never another weight; the
+    weights are shifted by 1 because scipy reads a 0 as no edge), and scipy's
+    single-linkage hierarchy cut at each threshold gives the same partition as
+    the oracle's threshold components."""
+    from scipy.cluster.hierarchy import fcluster, linkage
+    from scipy.sparse.csgraph import minimum_spanning_tree
+    from scipy.spatial.distance import squareform
+
+    rng = np.random.default_rng(20 + seed)
+    n = int(rng.integers(2, 70))
+    H = tie_heavy(rng, n, L=int(rng.integers(1, 9)))
+    _, _, w = oracle.mst(H)
+    T = minimum_spanning_tree(np.triu(H.astype(np.float64) + 1, 1))
+    assert T.nnz == n - 1
+    assert round(T.sum()) - (n - 1) == int(w.astype(np.int64).sum())
+    Z = linkage(squareform(H.astype(np.float64), checks=False), method="single")
+    thr = [0, 1, 2, 3, 5, 8]
+    lab = oracle.clusters(H, thr)
+    for t, th in enumerate(thr):
+        f = fcluster(Z, th, criterion="distance")
+        first = {}
+        for i, c in enumerate(f.tolist()):
+            first.setdefault(c, i)  # a cluster's label: its smallest member
+        np.testing.assert_array_equal(lab[t], [first[c] for c in f.tolist()])
 
 
 def test_tree_cut_rejects_bad_edges(pkg):
