@@ -257,10 +257,19 @@ def dense_ranks(calls: np.ndarray, threads: int = 0):
     return x, nd
 
 
-def choose_tau(x, nd, stripe=512, free_bytes=None, gemm_rate=REF_GEMM_RATE, rare_rate=REF_RARE_RATE,
-               verbose=False, device=0) -> int:
+def _ranks_args(x, nd):
+    """Ranks (n x L u16) and per-locus distinct counts (L u32), as dense_ranks
+    returns them; the library checks every rank against its locus's count."""
     x = np.ascontiguousarray(x, dtype=np.uint16)
     nd = np.ascontiguousarray(nd, dtype=np.uint32)
+    if x.ndim != 2 or nd.shape != (x.shape[1],):
+        raise TchError(f"ranks must be n x L with one distinct count per locus (got {x.shape} and {nd.shape})")
+    return x, nd
+
+
+def choose_tau(x, nd, stripe=512, free_bytes=None, gemm_rate=REF_GEMM_RATE, rare_rate=REF_RARE_RATE,
+               verbose=False, device=0) -> int:
+    x, nd = _ranks_args(x, nd)
     n, L = x.shape
     if free_bytes is None:
         free_bytes = free_vram(device)
@@ -284,8 +293,7 @@ class Encoding:
 
 
 def encode_host(x, nd, tau: int, threads: int = 0) -> Encoding:
-    x = np.ascontiguousarray(x, dtype=np.uint16)
-    nd = np.ascontiguousarray(nd, dtype=np.uint32)
+    x, nd = _ranks_args(x, nd)
     n, L = x.shape
     h = HostEncoding()
     err = _errbuf()
@@ -393,6 +401,23 @@ def tau_features(calls: np.ndarray, device: int = 0):
                 est=est[:r].copy())
 
 
+def _mlp_args(w, X, y=None):
+    """Weights, samples (m x TAU_FEATURES) and targets (m) as the kernels read
+    them, checked against one another before any pointer reaches C."""
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    if w.size != MLP_PARAMS:
+        raise TchError(f"the model has {MLP_PARAMS} parameters (got {w.size})")
+    if X.ndim != 2 or X.shape[1] != TAU_FEATURES:
+        raise TchError(f"samples must be m x {TAU_FEATURES} (got shape {X.shape})")
+    if y is None:
+        return w, X
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    if y.shape != (X.shape[0],):
+        raise TchError(f"one target per sample: {X.shape[0]} samples, targets of shape {y.shape}")
+    return w, X, y
+
+
 def mlp_init(seed: int) -> np.ndarray:
     w = np.zeros(MLP_PARAMS, np.float32)
     lib().tch_mlp_init(_ptr(w), seed)
@@ -401,9 +426,8 @@ def mlp_init(seed: int) -> np.ndarray:
 
 def mlp_train(w: np.ndarray, X: np.ndarray, y: np.ndarray, steps: int, lr: float, device: int = 0):
     """Adam on the GPU (the library's kernels); returns (new weights, final loss)."""
-    w = np.ascontiguousarray(w, dtype=np.float32).copy()
-    X = np.ascontiguousarray(X, dtype=np.float32)
-    y = np.ascontiguousarray(y, dtype=np.float32)
+    w, X, y = _mlp_args(w, X, y)
+    w = w.copy()
     loss = ctypes.c_float(0)
     err = _errbuf()
     _check(lib().tch_mlp_train(device, _ptr(w), _ptr(X), _ptr(y), len(y), steps, lr, ctypes.byref(loss), err,
@@ -412,8 +436,7 @@ def mlp_train(w: np.ndarray, X: np.ndarray, y: np.ndarray, steps: int, lr: float
 
 
 def mlp_predict(w: np.ndarray, X: np.ndarray, device: int = 0) -> np.ndarray:
-    w = np.ascontiguousarray(w, dtype=np.float32)
-    X = np.ascontiguousarray(X, dtype=np.float32)
+    w, X = _mlp_args(w, X)
     out = np.zeros(len(X), np.float32)
     err = _errbuf()
     _check(lib().tch_mlp_predict(device, _ptr(w), _ptr(X), len(X), _ptr(out), err, len(err)), err)
@@ -421,9 +444,7 @@ def mlp_predict(w: np.ndarray, X: np.ndarray, device: int = 0) -> np.ndarray:
 
 
 def mlp_loss_grad(w: np.ndarray, X: np.ndarray, y: np.ndarray, device: int = 0):
-    w = np.ascontiguousarray(w, dtype=np.float32)
-    X = np.ascontiguousarray(X, dtype=np.float32)
-    y = np.ascontiguousarray(y, dtype=np.float32)
+    w, X, y = _mlp_args(w, X, y)
     g = np.zeros(MLP_PARAMS, np.float32)
     loss = ctypes.c_float(0)
     err = _errbuf()
@@ -697,6 +718,8 @@ def mst_clusters(n: int, u, v, w, thresholds) -> np.ndarray:
     v = np.ascontiguousarray(v, dtype=np.uint32)
     w = np.ascontiguousarray(w, dtype=np.uint16)
     thr = np.ascontiguousarray(thresholds, dtype=np.uint32)
+    if not (len(u) == len(v) == len(w)):
+        raise TchError(f"u, v and w must have one entry per edge (got {len(u)}, {len(v)}, {len(w)})")
     labels = np.zeros((len(thr), n), np.uint32)
     err = _errbuf()
     _check(lib().tch_mst_clusters(n, _ptr(u), _ptr(v), _ptr(w), len(u), _ptr(thr), len(thr), _ptr(labels), err,
@@ -721,6 +744,17 @@ def pinned_empty(shape, dtype=np.uint16) -> np.ndarray:
     a = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
     weakref.finalize(buf, lib().tch_host_free, p)
     return a
+
+
+def _result_buffer(buf, shape, name: str, zero: bool = False) -> np.ndarray:
+    """A caller's u16 result buffer checked against the call's shape (the
+    library writes shape[0] x shape[1] cells through its pointer), or a new one."""
+    if buf is None:
+        return np.zeros(shape, np.uint16) if zero else np.empty(shape, np.uint16)
+    if buf.shape != shape or buf.dtype != np.uint16 or not buf.flags.c_contiguous:
+        raise TchError(f"{name} must be a C-contiguous {shape[0]} x {shape[1]} uint16 array "
+                       f"(got {buf.dtype} {buf.shape})")
+    return buf
 
 
 class Database:
@@ -752,8 +786,8 @@ class Database:
         m = q.shape[0]
         if q.shape[1] != self.L:
             raise TchError(f"queries have {q.shape[1]} loci, the database {self.L}")
-        qdb = out if out is not None else np.empty((m, self.n), np.uint16)  # every cell is written
-        qq = (out_qq if out_qq is not None else np.zeros((m, m), np.uint16)) if want_qq else None
+        qdb = _result_buffer(out, (m, self.n), "out")  # every cell is written
+        qq = _result_buffer(out_qq, (m, m), "out_qq", zero=True) if want_qq else None
         err = _errbuf()
         _check(lib().tch_db_query(self._h, m, _ptr(q), _ptr(qdb), _ptr(qq) if want_qq else None,
                                   ctypes.c_void_p(stream) if stream else None, err, len(err)), err)
@@ -789,10 +823,10 @@ class Server:
         page-locked ones, see pinned_empty, arrive fastest)."""
         q = np.ascontiguousarray(q, dtype=np.uint64)
         m = q.shape[0]
-        qdb = out if out is not None else np.empty((m, self.db.n), np.uint16)  # every cell is written
-        if qdb.shape != (m, self.db.n) or qdb.dtype != np.uint16 or not qdb.flags.c_contiguous:
-            raise TchError("out must be a C-contiguous m x n uint16 array")
-        qq = (out_qq if out_qq is not None else np.zeros((m, m), np.uint16)) if want_qq else None
+        if q.ndim != 2 or q.shape[1] != self.db.L:
+            raise TchError(f"queries must be m x {self.db.L} (the database's loci), got shape {q.shape}")
+        qdb = _result_buffer(out, (m, self.db.n), "out")  # every cell is written
+        qq = _result_buffer(out_qq, (m, m), "out_qq", zero=True) if want_qq else None
         rid = lib().tch_server_submit(self._h, m, _ptr(q), _ptr(qdb), _ptr(qq) if want_qq else None)
         if rid < 0:
             raise TchError("request rejected")

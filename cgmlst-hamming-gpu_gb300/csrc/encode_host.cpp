@@ -70,19 +70,40 @@ struct Counts {
     std::vector<uint32_t> cnt;
 };
 
-Counts count_ranks(const uint16_t* x, const uint32_t* nd, int n, int L, int threads) {
-    Counts c;
-    c.off.resize((size_t)L + 1, 0);
-    for (int k = 0; k < L; k++) c.off[k + 1] = c.off[k] + nd[k] + 1;
+// The ranks x (n x L) and the distinct counts nd (L) come from the caller:
+// every nd[k] must be at most 65 535 and every rank at most its locus's
+// nd[k] (tch_dense_ranks gives both), else the counters of a locus would be
+// indexed past their range.  A violation is an error, not a count.
+int count_ranks(const uint16_t* x, const uint32_t* nd, int n, int L, int threads, Counts& c, char* err,
+                int errlen) {
+    if ((size_t)n * L != 0 && !x) return set_err(err, errlen, "null ranks");
+    if (L > 0 && !nd) return set_err(err, errlen, "null distinct counts");
+    c.off.assign((size_t)L + 1, 0);
+    for (int k = 0; k < L; k++) {
+        if (nd[k] > 65535) return set_err(err, errlen, "locus %d: %u distinct alleles (limit 65535)", k, nd[k]);
+        c.off[k + 1] = c.off[k] + nd[k] + 1;
+    }
     c.cnt.assign(c.off[L], 0);
+    std::atomic<long long> bad{-1};  // a cell i * L + k whose rank is above nd[k]
     // loci in blocks: each worker owns whole loci and walks rows in tiles
     parallel_for(threads, (size_t)L, 16, [&](size_t k0, size_t k1) {
         for (int i = 0; i < n; i++) {
             const uint16_t* row = x + (size_t)i * L;
-            for (size_t k = k0; k < k1; k++) c.cnt[c.off[k] + row[k]]++;
+            for (size_t k = k0; k < k1; k++) {
+                if (row[k] > nd[k]) {
+                    long long expect = -1;
+                    bad.compare_exchange_strong(expect, (long long)i * L + (long long)k);
+                    continue;
+                }
+                c.cnt[c.off[k] + row[k]]++;
+            }
         }
     });
-    return c;
+    const long long b = bad.load();
+    if (b >= 0)
+        return set_err(err, errlen, "row %lld, locus %lld: rank %u is above the locus's %u distinct alleles", b / L,
+                       b % L, (unsigned)x[b], nd[b % L]);
+    return 0;
 }
 
 }  // namespace
@@ -127,7 +148,9 @@ int tch_dense_ranks(const uint64_t* calls, int n, int L, uint16_t* x, uint32_t* 
 int tch_choose_tau(const uint16_t* x, const uint32_t* nd, int n, int L, int stripe, size_t free_bytes,
                    double gemm_rate, double rare_rate, int verbose, int* tau_out, char* err, int errlen) {
     if (!tau_out) return set_err(err, errlen, "null output");
-    Counts c = count_ranks(x, nd, n, L, 0);
+    if (n < 0 || L < 0) return set_err(err, errlen, "negative size");
+    Counts c;
+    if (count_ranks(x, nd, n, L, 0, c, err, errlen)) return 1;
     std::vector<double> cs;
     cs.reserve(c.cnt.size());
     for (int k = 0; k < L; k++)
@@ -167,7 +190,8 @@ int tch_encode_host(const uint16_t* x, const uint32_t* nd, int n, int L, int tau
     memset(out, 0, sizeof(*out));
     if (n < 0 || L < 0) return set_err(err, errlen, "negative size");
     if (tau < 1) return set_err(err, errlen, "tau must be >= 1");
-    Counts c = count_ranks(x, nd, n, L, threads);
+    Counts c;
+    if (count_ranks(x, nd, n, L, threads, c, err, errlen)) return 1;
     // frequent column of (locus, rank), -1 otherwise (main.rs:367-385)
     std::vector<int32_t> col(c.cnt.size(), -1);
     std::vector<size_t> base((size_t)L + 1, 0);

@@ -455,6 +455,9 @@ int tch_stripe_noalloc(int device, int n, const uint8_t* d_O, size_t K1, const u
 /* ----------------------------------------------------------------------------
  * Host encoder (restates the reference host, main.rs:134-198 and 366-444).
  * Multi-threaded C++; `threads` <= 0 uses every hardware thread.
+ * tch_choose_tau and tch_encode_host take ranks and distinct counts as
+ * tch_dense_ranks gives them and fail when a count exceeds 65535 or a rank
+ * exceeds its locus's count.
  * ------------------------------------------------------------------------- */
 
 /* Dense per-locus ranks (main.rs:134-165): for each locus, the sorted unique

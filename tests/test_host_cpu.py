@@ -31,6 +31,66 @@ def test_library_exports_every_declared_symbol(pkg):
     assert set(syms) <= exported
 
 
+def test_bindings_check_shapes_before_the_library(pkg):
+    """Arrays whose shapes disagree with one another are rejected in Python,
+    before a pointer reaches C (which would read or write past them).  The
+    serving calls are made on stand-ins for a database and a server, which
+    are never reached."""
+    from types import SimpleNamespace
+
+    w = np.zeros(pkg.MLP_PARAMS, np.float32)
+    X = np.zeros((5, pkg.TAU_FEATURES), np.float32)
+    with pytest.raises(pkg.TchError, match="parameters"):
+        pkg.mlp_predict(w[:-1], X)
+    with pytest.raises(pkg.TchError, match="samples must be"):
+        pkg.mlp_predict(w, X[:, :-1])
+    with pytest.raises(pkg.TchError, match="samples must be"):
+        pkg.mlp_predict(w, X.ravel())
+    with pytest.raises(pkg.TchError, match="one target per sample"):
+        pkg.mlp_loss_grad(w, X, np.zeros(4, np.float32))
+    with pytest.raises(pkg.TchError, match="one target per sample"):
+        pkg.mlp_train(w, X, np.zeros(6, np.float32), steps=1, lr=1e-3)
+    db = SimpleNamespace(n=10, L=7, _h=None)
+    q = np.ones((3, 7), np.uint64)
+    with pytest.raises(pkg.TchError, match="loci"):
+        pkg.Database.query(db, np.ones((3, 6), np.uint64))
+    with pytest.raises(pkg.TchError, match="out must be"):
+        pkg.Database.query(db, q, out=np.zeros((3, 9), np.uint16))
+    with pytest.raises(pkg.TchError, match="out_qq must be"):
+        pkg.Database.query(db, q, out_qq=np.zeros((3, 3), np.uint32))
+    sv = SimpleNamespace(db=db, _h=None, _live={})
+    with pytest.raises(pkg.TchError, match="queries must be"):
+        pkg.Server.submit(sv, np.ones((3, 6), np.uint64))
+    with pytest.raises(pkg.TchError, match="out must be"):
+        pkg.Server.submit(sv, q, out=np.zeros((10, 3), np.uint16))
+    with pytest.raises(pkg.TchError, match="out_qq must be"):
+        pkg.Server.submit(sv, q, out_qq=np.zeros((3, 6), np.uint16)[:, ::2])  # not contiguous
+
+
+def test_encoder_rejects_ranks_above_their_counts(pkg):
+    """The host encoder and the tau model count ranks per (locus, rank): a rank
+    above its locus's distinct count, a count above 65 535 or counts of the
+    wrong length are errors (a C caller could otherwise index past the
+    counters)."""
+    rng = np.random.default_rng(5)
+    A = rng.integers(0, 9, size=(50, 12)).astype(np.uint64)
+    x, nd = pkg.dense_ranks(A)
+    bad = nd.copy()
+    bad[7] = max(int(x[:, 7].max()) - 1, 0)
+    with pytest.raises(pkg.TchError, match="locus 7: rank"):
+        pkg.encode_host(x, bad, tau=4)
+    with pytest.raises(pkg.TchError, match="locus 7: rank"):
+        pkg.choose_tau(x, bad, free_bytes=1 << 40)
+    big = nd.copy()
+    big[3] = 70000
+    with pytest.raises(pkg.TchError, match="locus 3: 70000 distinct"):
+        pkg.encode_host(x, big, tau=4)
+    with pytest.raises(pkg.TchError, match="one distinct count per locus"):
+        pkg.encode_host(x, nd[:-1], tau=4)
+    enc = pkg.encode_host(x, nd, tau=4)  # the consistent pair still encodes
+    assert enc.n == 50 and enc.L == 12
+
+
 def test_kernel_names(pkg):
     assert pkg.kernel_name(1) == "popc" and pkg.kernel_name(99) == "?"
     assert pkg.kernel_available("popc")

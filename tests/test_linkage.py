@@ -103,6 +103,8 @@ def test_tree_cut_rejects_bad_edges(pkg):
         pkg.mst_clusters(3, [0], [3], [1], [1])
     with pytest.raises(pkg.TchError, match="not between"):
         pkg.mst_clusters(3, [1], [1], [1], [1])
+    with pytest.raises(pkg.TchError, match="one entry per edge"):
+        pkg.mst_clusters(3, [0, 1], [1, 2], [1], [1])
     assert pkg.mst_clusters(0, [], [], [], [4]).shape == (1, 0)
     np.testing.assert_array_equal(pkg.mst_clusters(1, [], [], [], [0, 9]), [[0], [0]])
 
