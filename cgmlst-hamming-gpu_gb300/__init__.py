@@ -838,7 +838,7 @@ class Server:
         qs, ls = ctypes.c_double(), ctypes.c_double()
         err = _errbuf()
         rc = lib().tch_server_wait(self._h, rid, ctypes.byref(qs), ctypes.byref(ls), err, len(err))
-        q, qdb, qq = self._live.pop(rid)
+        q, qdb, qq = self._live.pop(rid, (None, None, None))  # each id is waited for once
         _check(rc, err)
         return qdb, qq, qs.value, ls.value
 

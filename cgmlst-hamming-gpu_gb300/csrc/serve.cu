@@ -472,8 +472,10 @@ int tch_server_wait(tch_server* sv, int64_t id, double* queued_s, double* latenc
         auto it = sv->reqs.find(id);
         if (it == sv->reqs.end()) return e.set("unknown request %lld", (long long)id);
         r = it->second;
-        sv->cv.wait(lk, [&] { return r->done; });
+        // claimed before the wait releases the lock: a second wait on the
+        // same id finds it unknown instead of sharing (and deleting) it
         sv->reqs.erase(it);
+        sv->cv.wait(lk, [&] { return r->done; });
     }
     if (queued_s) *queued_s = r->t_start - r->t_submit;
     if (latency_s) *latency_s = r->t_done - r->t_submit;

@@ -252,7 +252,10 @@ int tch_server_create(tch_db* db, int slots, size_t budget, tch_server** out, ch
 /* Returns a request id (> 0), or -1 on bad arguments. */
 int64_t tch_server_submit(tch_server* sv, int m, const uint64_t* qcalls, uint16_t* qdb, uint16_t* qq);
 /* Blocks until the request is done; *queued_s = submit -> start, *latency_s =
- * submit -> results in host memory. */
+ * submit -> results in host memory.  Each id is waited for once: a second
+ * wait on it (or one that starts after the first) fails as unknown.
+ * tch_server_destroy finishes the queued requests; call it after every
+ * wait has returned. */
 int tch_server_wait(tch_server* sv, int64_t id, double* queued_s, double* latency_s, char* err, int errlen);
 void tch_server_destroy(tch_server* sv);
 
