@@ -294,7 +294,6 @@ int tch_batch_add(tch_batch* b, int n, int L, const uint64_t* calls, int tau, ch
     if (solver_from_calls(b->device, n, L, calls, tau, TCH_KERNEL_AUTO, false, &sv, e)) return 1;
     drop_graph(b);
     const size_t acc = b->off.back();
-    b->off.back() = acc;
     b->sets.push_back(sv);
     b->ld.push_back(up((size_t)n, 8));
     b->off.push_back(acc + (size_t)n * up((size_t)n, 8));
