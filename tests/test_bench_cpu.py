@@ -64,3 +64,29 @@ def test_strided_rows_cover_the_triangle():
         tot += acc.value
     assert tot_pairs == pairs_full == 301 * 300 // 2
     assert tot == full.value == int(np.triu(oracle.hamming(x), 1).astype(np.int64).sum())
+
+
+def test_parity_rows_counts_planted_mismatches():
+    """The bench's check of its timed output (the line's `parity`): the
+    oracle's own matrix gives 0 mismatches, and one wrong cell planted in a
+    sampled row (in a CPU tensor) is counted once."""
+    import importlib.util
+
+    import numpy as np
+    import pytest
+
+    torch = pytest.importorskip("torch")
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    rng = np.random.default_rng(8)
+    x = rng.integers(0, 6, size=(211, 37)).astype(np.uint16)
+    H = oracle.hamming(x)
+    out = torch.from_numpy(H.view(np.int16).copy())
+    r = bench.parity_rows(x, out, rows=16)
+    assert r["mismatches"] == 0 and r["rows"] >= 16 and r["cells"] > 0
+    out[0, 5] += 1  # row 0 is always sampled
+    assert bench.parity_rows(x, out, rows=16)["mismatches"] == 1
